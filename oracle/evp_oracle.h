@@ -1,0 +1,68 @@
+/*
+ * CPU restatement of SRX's EVP-FFT increment loop (TEST INFRASTRUCTURE ONLY).
+ *
+ * This is the oracle: the checker the GPU path is compared against, and the
+ * timed CPU baseline. It restates, in plain C with the reference's order of
+ * floating-point operations, the functions of the reference that the
+ * equilibrium iteration runs (citations in evp_oracle.c). It is pinned
+ * against the reference's own sources compiled with single-rank shims
+ * (oracle/_ref, built by oracle/Makefile) through the fixtures under
+ * tests/golden/. Only tests/, __graft_entry__.smoke() and bench.py's CPU
+ * baseline legs may load it.
+ */
+#ifndef SRX_EVP_ORACLE_H
+#define SRX_EVP_ORACLE_H
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct evo_job evo_job;
+
+/* GetNameList + SetupJob (io.c:96-164, init.c:728-1216). File names inside
+ * the namelist are resolved against the directory of `input_path`.
+ * `rho0_path` (nullable): N doubles, per-voxel initial SSD density
+ * (1e12 m^-2), applied to every slip system after set-up. Returns NULL and
+ * fills `err` on failure. */
+evo_job *evo_open(const char *input_path, const char *rho0_path, char *err, int errlen);
+void evo_close(evo_job *j);
+
+/* Worker threads for the per-voxel loops and FFT pencils (results are
+ * bit-identical for any thread count). */
+void evo_set_threads(int n);
+
+int evo_nvox(const evo_job *j);
+
+/* 0: plain NR (evolution.c:372-377, the top-level build); 1: NR_MODIFIED
+ * backtracking line search (evolution.c:280-371, on in the FFTW3 variant,
+ * fftw3version-NOSMOOTHING/evpFlags.h:21). */
+void evo_set_nr_mode(evo_job *j, int mode);
+int evo_nsteps(const evo_job *j);
+
+/* One increment of Evolution() (evolution.c:726-1520) without file output.
+ * Returns 0, or a nonzero status: 1 NaN in the flow rule, 2 singular LU. */
+int evo_increment(evo_job *j, int istep, int *iters);
+
+/* Whole Evolution() into `outdir`: vm.out, dd.out, err.out, iters.txt
+ * (one line per increment: istep iterations) and errors.txt (the per-iteration
+ * lines the reference prints, evolution.c:1254-1255); with write_iout the
+ * reference's .iout dumps at PrintControl steps (io.c:322-995; the
+ * new_position record is written as zeros). nsteps < 0 means N_steps. */
+int evo_run(evo_job *j, const char *outdir, int nsteps, int write_iout);
+
+/* Raw pointers into the AoS state (reference layout, evp.h:429-456):
+ * "Sig","DisGrad","Eps","Edot","VelGrad","TranMat" ([N][3][3]);
+ * "rho_s","rho_m","rho_F","rho_P","gamdot","gam_acum","trial_gam_acum",
+ * "rho_dipole","rho_forest","rho_inplane" ([N][12]); "rho_tot" ([N]);
+ * "C_gr" ([N][6][6]); "Schm_gr" ([N][12][5]); "scalars" (see .c). */
+double *evo_field(evo_job *j, const char *name);
+
+/* Building blocks, for unit parity of single stages. */
+void evo_update_schmid(evo_job *j);                          /* kinematics.c:430-463 */
+int evo_update_stress(evo_job *j, double *err_e, double *err_s); /* evolution.c:157-427 */
+void evo_get_smacro(evo_job *j);                             /* evolution.c:590-664 */
+void evo_spectral(evo_job *j);                               /* evolution.c:1157-1201 */
+
+#ifdef __cplusplus
+}
+#endif
+#endif

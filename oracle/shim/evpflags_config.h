@@ -1,0 +1,31 @@
+/*
+ * Compile-time configuration for the oracle build of the reference.
+ *
+ * TEST INFRASTRUCTURE ONLY. Pre-included (gcc -include) before every
+ * reference translation unit. It defines EVPFLAGS_H, so the reference's own
+ * evpFlags.h (evpFlags.h:1-46) is skipped by its include guard, and it sets
+ * the same macros with one change: DD_CU is left undefined, so the elastic
+ * constants come from the namelist's ElastConst_PhaseI instead of the
+ * temperature formula at init.c:822-826 (the reference README.txt:2 allows
+ * this). Every other flag matches evpFlags.h as shipped.
+ */
+#ifndef EVPFLAGS_H
+#define EVPFLAGS_H
+
+#define NPHMAX 2
+#define NSYSMX 12
+
+#define DD_BASED_FLAG
+#ifdef DD_BASED_FLAG
+/* DD_CU intentionally off (see header comment). */
+#define FORWARD_PLUS_BACKWARD
+#ifdef SRX_ORACLE_NR_MODIFIED
+#define NR_MODIFIED /* line-search NR of the FFTW3 variant */
+#endif
+#define PF_DRX
+#ifdef PF_DRX
+#define GB_BULGING_ONLY
+#endif
+#endif
+
+#endif
