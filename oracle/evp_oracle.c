@@ -761,6 +761,14 @@ double *evo_field(evo_job *j, const char *n)
     if (!strcmp(n, "rho_inplane")) return &j->rho_inplane[0][0];
     if (!strcmp(n, "rho_tot")) return j->rho_tot;
     if (!strcmp(n, "Schm_gr")) return &j->Schm_gr[0][0][0];
+    if (!strcmp(n, "C066")) return &j->C066[0][0];
+    if (!strcmp(n, "S066")) return &j->S066[0][0];
+    if (!strcmp(n, "S0")) return &j->S0[0][0][0][0];
+    if (!strcmp(n, "Chi")) return &j->Chi[0][0][0];
+    if (!strcmp(n, "Chi_1")) return &j->Chi_1[0][0][0];
+    if (!strcmp(n, "Shear_G")) return j->Shear_G;
+    if (!strcmp(n, "bb_B")) return &j->bb_B[0][0];
+    if (!strcmp(n, "Schm_xt")) return &j->Schm_xt[0][0][0];
     if (!strcmp(n, "scalars")) {
         /* 0..8 SigAvg, 9..17 SigAvg1, 18..26 dDisGradAvg_acum, 27 e_vm, 28 d_vm,
          * 29 s_vm, 30 s_vm1, 31 TimeTot */
@@ -1351,6 +1359,40 @@ static void avg_dislocation(evo_job *j)
 }
 
 static FILE *g_err_log = 0;
+
+/* One pass of the equilibrium loop body (evolution.c:1151-1257) on the
+ * current state; the increment head must have run (evo_begin). Used as the
+ * bounded CPU sample of the hot path. */
+int evo_iteration(evo_job *j)
+{
+    double ee, es;
+    int st;
+    evo_spectral(j);
+    st = evo_update_stress(j, &ee, &es);
+    if (st) return st;
+    j->Err_e = ee * j->WGT;
+    j->Err_s = es * j->WGT;
+    evo_get_smacro(j);
+    if (fabs(j->e_vm) < 1E-5) j->Err_e = 0.0;
+    else j->Err_e /= j->e_vm;
+    j->Err_s /= j->s_vm;
+    return 0;
+}
+
+/* Increment head (evolution.c:1030-1141) without the loop. */
+void evo_begin(evo_job *j)
+{
+    int v, a, b;
+    for (v = 0; v < j->N; v++)
+        for (a = 0; a < 3; a++)
+            for (b = 0; b < 3; b++) {
+                j->VelGrad[v][a][b] = j->DisGrad[v][a][b];
+                j->DisGrad[v][a][b] += j->Udot[a][b] * j->nl.TimeStep;
+            }
+    evo_update_schmid(j);
+    memset(j->dDisGradAvg, 0, sizeof(t2));
+    memset(j->dDisGradAvg_acum, 0, sizeof(t2));
+}
 
 int evo_increment(evo_job *j, int istep, int *iters)
 {

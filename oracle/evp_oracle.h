@@ -53,7 +53,9 @@ int evo_run(evo_job *j, const char *outdir, int nsteps, int write_iout);
  * "Sig","DisGrad","Eps","Edot","VelGrad","TranMat" ([N][3][3]);
  * "rho_s","rho_m","rho_F","rho_P","gamdot","gam_acum","trial_gam_acum",
  * "rho_dipole","rho_forest","rho_inplane" ([N][12]); "rho_tot" ([N]);
- * "C_gr" ([N][6][6]); "Schm_gr" ([N][12][5]); "scalars" (see .c). */
+ * "Schm_gr" ([N][12][5]); set-up arrays "C066","S066" (6x6), "S0" (3^4),
+ * "Chi","Chi_1" ([2][12][12]), "Shear_G" ([2]), "bb_B" ([2][12]),
+ * "Schm_xt" ([2][12][5]); "scalars" (see evp_oracle.c). */
 double *evo_field(evo_job *j, const char *name);
 
 /* Building blocks, for unit parity of single stages. */
@@ -61,6 +63,8 @@ void evo_update_schmid(evo_job *j);                          /* kinematics.c:430
 int evo_update_stress(evo_job *j, double *err_e, double *err_s); /* evolution.c:157-427 */
 void evo_get_smacro(evo_job *j);                             /* evolution.c:590-664 */
 void evo_spectral(evo_job *j);                               /* evolution.c:1157-1201 */
+void evo_begin(evo_job *j);      /* increment head, evolution.c:1030-1141 */
+int evo_iteration(evo_job *j);   /* one pass of the loop body, evolution.c:1151-1257 */
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,709 @@
+// C ABI of include/evpg.h: context set-up, state transfer and the
+// equilibrium-loop orchestration on the context's stream.
+#include "evpg.h"
+#include "evpg_ctx.h"
+
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <vector>
+
+namespace evpg {
+
+static thread_local char g_err[512] = "";
+
+static int fail(int st, const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof g_err, fmt, ap);
+    va_end(ap);
+    return st;
+}
+
+#define CK(call)                                                                        \
+    do {                                                                                \
+        cudaError_t e_ = (call);                                                        \
+        if (e_ != cudaSuccess)                                                          \
+            return fail(EVPG_ERR_CUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+                        __FILE__, __LINE__);                                            \
+    } while (0)
+
+// -------------------------------------------------------------- FFT plans
+
+static void make_plan(int n, FftPlan& p) {
+    memset(&p, 0, sizeof p);
+    p.n = n;
+    int m = n, nf = 0;
+    const int pref[] = {8, 4, 2, 3, 5};
+    for (int r : pref)
+        while (m % r == 0 && nf < 12) {
+            p.radix[nf++] = r;
+            m /= r;
+        }
+    for (int q = 7; m > 1 && nf < 12; q += 2)
+        while (m % q == 0 && nf < 12) {
+            p.radix[nf++] = q;
+            m /= q;
+        }
+    p.nf = nf;
+    int ns = 1;
+    for (int s = 0; s < nf; s++) {
+        p.ns[s] = ns;
+        ns *= p.radix[s];
+    }
+}
+
+// exp(-2 pi i t / n) with exact axis values and quadrant symmetry
+static void unit_root(long t, long n, double* c, double* s) {
+    t %= n;
+    if (t < 0) t += n;
+    const long q = (4 * t) / n, r = 4 * t - q * n;
+    long double c0, s0;
+    if (r == 0) {
+        c0 = 1.0L;
+        s0 = 0.0L;
+    } else if (2 * r <= n) {
+        const long double th = 1.57079632679489661923132169163975144L * ((long double)r / (long double)n);
+        c0 = cosl(th);
+        s0 = sinl(th);
+    } else {
+        const long double th = 1.57079632679489661923132169163975144L * ((long double)(n - r) / (long double)n);
+        c0 = sinl(th);
+        s0 = cosl(th);
+    }
+    long double cc, ss;
+    switch (q & 3) {
+        case 0: cc = c0; ss = s0; break;
+        case 1: cc = -s0; ss = c0; break;
+        case 2: cc = -c0; ss = -s0; break;
+        default: cc = s0; ss = -c0; break;
+    }
+    *c = (double)cc;
+    *s = -(double)ss;  // forward sign
+}
+
+// ------------------------------------------------------------- materials
+
+template <typename T>
+static void fill_material(const evpg_rve_desc* d, Material<T>& m) {
+    memset(&m, 0, sizeof m);
+    for (int p = 0; p < 2; p++) {
+        const evpg_phase_desc& s = d->phase[p];
+        PhaseK<T>& k = m.ph[p];
+        k.crystal = s.crystal;
+        k.n_sys = s.n_sys;
+        const double kT = d->kT;
+        for (int i = 0; i < NS; i++) {
+            for (int j = 0; j < NS; j++) {
+                k.chi[i][j] = (T)s.chi[i][j];
+                k.chi1[i][j] = (T)s.chi1[i][j];
+            }
+            const double b = s.burgers[i];
+            k.k_tpass[i] = (T)(s.c1 * s.shear_g * b * 1.0E-3);
+            k.k_tcut[i] = (T)((kT / 0.62415063631) / s.c2 / s.c3 / b / b * 0.1);
+            k.k_rhom[i] = (T)(2.0 * kT / s.c1 / s.c2 / s.c3 / s.shear_g / (b * b * b) * 160.2177);
+            k.k_gamo[i] = (T)(1E-3 * 1.0E10 * s.c2 * b * exp(-1.0 * s.q_slip));
+            for (int q = 0; q < 5; q++) k.schm_xt[i][q] = (T)s.schm_xt[i][q];
+            for (int q = 0; q < 3; q++) {
+                k.bn[i][q] = (T)s.bn[i][q];
+                k.bb[i][q] = (T)s.bb[i][q];
+            }
+            k.burgers[i] = (T)b;
+        }
+        k.tau0 = (T)s.tau0;
+        k.shear_g = (T)s.shear_g;
+        k.c4 = (T)s.c4;
+        k.c5 = (T)s.c5;
+        k.c6 = (T)s.c6;
+        k.q_bulk = (T)s.q_bulk;
+    }
+    for (int i = 0; i < 6; i++)
+        for (int j = 0; j < 6; j++) {
+            m.c066[i][j] = (T)d->c066[i][j];
+            m.s066[i][j] = (T)d->s066[i][j];
+        }
+    for (int i = 0; i < 81; i++) {
+        (&m.c0[0][0][0][0])[i] = (T)(&d->c0[0][0][0][0])[i];
+        (&m.s0[0][0][0][0])[i] = (T)(&d->s0[0][0][0][0])[i];
+    }
+    m.dt = (T)d->dt;
+    m.kT = (T)d->kT;
+    m.temperature = (T)d->temperature;
+    m.nu = (T)d->nu;
+    m.d0 = (T)d->d0;
+    m.elast_bc = d->elast_bc;
+}
+
+// ---------------------------------------------------------- field helpers
+
+static void tensor_to_9(const double t[3][3], double* o) {
+    sym_to_b6<double>(t, o);
+    o[6] = 0.5 * (t[0][1] - t[1][0]);
+    o[7] = 0.5 * (t[0][2] - t[2][0]);
+    o[8] = 0.5 * (t[1][2] - t[2][1]);
+}
+
+static void nine_to_tensor(const double* v, double t[3][3]) {
+    b6_to_sym<double>(v, t);
+    t[0][1] += v[6]; t[1][0] -= v[6];
+    t[0][2] += v[7]; t[2][0] -= v[7];
+    t[1][2] += v[8]; t[2][1] -= v[8];
+}
+
+struct Alloc {
+    Ctx* c;
+    template <typename P> cudaError_t get(P** p, size_t n) {
+        const size_t b = n * sizeof(P);
+        c->bytes += b;
+        cudaError_t e = cudaMalloc((void**)p, b ? b : 1);
+        if (e == cudaSuccess) e = cudaMemsetAsync(*p, 0, b ? b : 1, c->stream);
+        return e;
+    }
+};
+
+static void prof_flush(Ctx& c) {
+    Profiler& p = c.prof;
+    if (!p.n) return;
+    cudaStreamSynchronize(c.stream);
+    for (int i = 0; i < p.n; i++) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, p.recs[i].a, p.recs[i].b) == cudaSuccess) {
+            p.ms[p.recs[i].group] += ms;
+            p.launches[p.recs[i].group] += 1;
+        }
+    }
+    p.n = 0;
+}
+
+void prof_mark(Ctx& c, int group, bool begin) {
+    Profiler& p = c.prof;
+    if (begin) c.launches++;
+    if (!p.on) return;
+    if (begin) {
+        if (p.n == p.cap) prof_flush(c);
+        if (p.n == p.cap) return;
+        p.recs[p.n].group = group;
+        cudaEventRecord(p.recs[p.n].a, c.stream);
+    } else {
+        cudaEventRecord(p.recs[p.n].b, c.stream);
+        p.n++;
+    }
+}
+
+static void prof_free(Ctx& c) {
+    Profiler& p = c.prof;
+    for (int i = 0; i < p.cap; i++) {
+        cudaEventDestroy(p.recs[i].a);
+        cudaEventDestroy(p.recs[i].b);
+    }
+    delete[] p.recs;
+    p.recs = nullptr;
+    p.cap = p.n = 0;
+    p.on = false;
+}
+
+static void free_ctx(Ctx* c) {
+    if (!c) return;
+    prof_free(*c);
+    void* ptrs[] = {c->sig64, c->dg64, c->dg_old, c->epsp, c->edot64, c->rho_s, c->rho_m,
+                    c->gamdot64, c->gam_acum, c->tranmat, c->schm64, c->fc64, c->sgr64, c->orient,
+                    c->phase, c->sig32, c->ddg32, c->b6_32, c->schm32, c->fc32, c->sgr32, c->spec,
+                    c->part_nr, c->part_end, c->macro, c->tw64[0], c->tw64[1], c->tw64[2],
+                    c->tw32[0], c->tw32[1], c->tw32[2]};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    if (c->macro_host) cudaFreeHost(c->macro_host);
+    if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+}  // namespace evpg
+
+using namespace evpg;
+
+extern "C" {
+
+const char* evpg_version(void) { return "evpg 0.1 (sm_103a)"; }
+
+const char* evpg_last_error(void) { return g_err; }
+
+const char* evpg_status_string(int st) {
+    switch (st) {
+        case EVPG_OK: return "ok";
+        case EVPG_ERR_ARG: return "invalid argument";
+        case EVPG_ERR_CUDA: return "CUDA error";
+        case EVPG_ERR_NOMEM: return "out of memory";
+        case EVPG_ERR_NAN: return "NaN in the flow rule";
+        case EVPG_ERR_SINGULAR: return "singular 6x6 system";
+        case EVPG_ERR_LINESEARCH: return "line search found no descent direction";
+        case EVPG_ERR_ITERMAX: return "equilibrium loop reached IterMax";
+        case EVPG_ERR_IO: return "input file error";
+        case EVPG_ERR_NO_DEVICE: return "no CUDA device";
+        default: return "unknown status";
+    }
+}
+
+int evpg_create(const evpg_rve_desc* d, void** out) {
+    if (!d || !out) return fail(EVPG_ERR_ARG, "null argument");
+    *out = nullptr;
+    for (int i = 0; i < 3; i++)
+        if (d->n[i] < 1 || d->n[i] > 1024) return fail(EVPG_ERR_ARG, "grid size %d out of range", d->n[i]);
+    const long long NN = (long long)d->n[0] * d->n[1] * d->n[2];
+    if (NN > (1LL << 30)) return fail(EVPG_ERR_ARG, "grid too large");
+    if (d->precision != EVPG_FP64 && d->precision != EVPG_FP32_BULK)
+        return fail(EVPG_ERR_ARG, "precision %d", d->precision);
+    if (d->nr_mode != EVPG_NR_PLAIN && d->nr_mode != EVPG_NR_LINESEARCH)
+        return fail(EVPG_ERR_ARG, "nr_mode %d", d->nr_mode);
+    if (!d->voxel_orient || !d->voxel_phase || !d->tranmat || !d->sig0 || !d->rho_s0 ||
+        (d->n_orient > 0 && (!d->c_gr || !d->s_gr)))
+        return fail(EVPG_ERR_ARG, "missing RVE arrays");
+    for (int p = 0; p < 2; p++)
+        if (d->phase[p].n_sys < 0 || d->phase[p].n_sys > EVPG_NSYS)
+            return fail(EVPG_ERR_ARG, "n_sys %d", d->phase[p].n_sys);
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+        return fail(EVPG_ERR_NO_DEVICE, "no CUDA device");
+    const int N = (int)NN;
+    for (int v = 0; v < N; v++) {
+        const int ph = d->voxel_phase[v];
+        if (ph < 1 || ph > 2) return fail(EVPG_ERR_ARG, "voxel %d: phase %d", v, ph);
+        if (d->phase[ph - 1].crystal && (d->voxel_orient[v] < 0 || d->voxel_orient[v] >= d->n_orient))
+            return fail(EVPG_ERR_ARG, "voxel %d: orientation %d", v, d->voxel_orient[v]);
+    }
+    Ctx* c = new Ctx();
+    memset((void*)c, 0, sizeof(Ctx));
+    c->g.n0 = d->n[0]; c->g.n1 = d->n[1]; c->g.n2 = d->n[2];
+    c->g.nh = d->n[2] / 2 + 1;
+    c->g.N = N;
+    c->g.Nh = (long long)d->n[0] * d->n[1] * c->g.nh;
+    c->precision = d->precision;
+    c->nr_mode = d->nr_mode;
+    c->n_orient = d->n_orient;
+    c->nr_itmax = 500;
+    c->nr_tol64 = 1E-10;
+    c->nr_tol32 = 2E-6;
+    c->delta_tau_drx = d->delta_tau_drx;
+    c->tau_drx = d->tau_drx;
+    memcpy(c->udot_a, d->udot_a, sizeof c->udot_a);
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete c;
+        return fail(EVPG_ERR_CUDA, "stream creation failed");
+    }
+    c->own_stream = true;
+    for (int a = 0; a < 3; a++) make_plan(d->n[a], c->pl[a]);
+    fill_material<double>(d, c->m64);
+    fill_material<float>(d, c->m32);
+    memcpy(c->cfg.s0, d->s0, sizeof c->cfg.s0);
+    memcpy(c->cfg.scauchy, d->scauchy, sizeof c->cfg.scauchy);
+    for (int i = 0; i < 6; i++) {
+        c->cfg.vflag[i] = d->velgrad_bc_flag[i];
+        c->cfg.sflag[i] = d->stress_bc_flag[i];
+    }
+    c->cfg.wgt = 1. / N;
+    c->cfg.wgt_ph1 = d->wgt_ph1;
+    c->cfg.err_tol = d->err_tol;
+    c->cfg.iter_max = d->iter_max;
+    c->nb_nr = (N + NR_BLOCK - 1) / NR_BLOCK;
+    c->nb_end = (N + END_BLOCK - 1) / END_BLOCK;
+
+    Alloc A{c};
+    const size_t n = (size_t)N;
+    const bool f32 = c->precision == EVPG_FP32_BULK;
+    cudaError_t e = cudaSuccess;
+#define AL(p, cnt) \
+    if (e == cudaSuccess) e = A.get(&(p), (cnt))
+    AL(c->sig64, 6 * n); AL(c->dg64, 9 * n); AL(c->dg_old, 9 * n); AL(c->epsp, 6 * n);
+    AL(c->edot64, 5 * n); AL(c->rho_s, 12 * n); AL(c->rho_m, 12 * n); AL(c->gamdot64, 12 * n);
+    AL(c->gam_acum, 12 * n); AL(c->tranmat, 9 * n); AL(c->schm64, 60 * n); AL(c->fc64, 48 * n);
+    AL(c->sgr64, 36 * (size_t)(d->n_orient > 0 ? d->n_orient : 1));
+    AL(c->orient, n); AL(c->phase, n);
+    if (f32) {
+        AL(c->sig32, 6 * n); AL(c->ddg32, 9 * n); AL(c->b6_32, 6 * n); AL(c->schm32, 60 * n);
+        AL(c->fc32, 48 * n); AL(c->sgr32, 36 * (size_t)(d->n_orient > 0 ? d->n_orient : 1));
+        float2* sp = nullptr;
+        AL(sp, 9 * (size_t)c->g.Nh);
+        c->spec = sp;
+    } else {
+        double2* sp = nullptr;
+        AL(sp, 9 * (size_t)c->g.Nh);
+        c->spec = sp;
+    }
+    AL(c->part_nr, (size_t)c->nb_nr * NPART_NR);
+    AL(c->part_end, (size_t)c->nb_end * NPART_END);
+    AL(c->macro, 1);
+    for (int a = 0; a < 3; a++) {
+        AL(c->tw64[a], (size_t)d->n[a]);
+        AL(c->tw32[a], (size_t)d->n[a]);
+    }
+#undef AL
+    if (e == cudaSuccess) e = cudaMallocHost((void**)&c->macro_host, sizeof(Macro));
+    if (e != cudaSuccess) {
+        free_ctx(c);
+        cudaGetLastError();
+        return fail(e == cudaErrorMemoryAllocation ? EVPG_ERR_NOMEM : EVPG_ERR_CUDA,
+                    "allocation: %s", cudaGetErrorString(e));
+    }
+    memset(c->macro_host, 0, sizeof(Macro));
+
+    // host-side layout changes: AoS tensors -> SoA planes in the B basis
+    std::vector<double> h(60 * n);
+    auto put = [&](void* dst, const void* src, size_t bytes) -> cudaError_t {
+        cudaError_t r = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, c->stream);
+        if (r == cudaSuccess) r = cudaStreamSynchronize(c->stream);
+        return r;
+    };
+    for (size_t v = 0; v < n; v++) {
+        double t[3][3], o[6];
+        memcpy(t, d->sig0 + 9 * v, sizeof t);
+        sym_to_b6<double>(t, o);
+        for (int q = 0; q < 6; q++) h[q * n + v] = o[q];
+    }
+    e = put(c->sig64, h.data(), 6 * n * sizeof(double));
+    if (e == cudaSuccess && f32) {
+        std::vector<float> hf(6 * n);
+        for (size_t i = 0; i < 6 * n; i++) hf[i] = (float)h[i];
+        e = put(c->sig32, hf.data(), 6 * n * sizeof(float));
+    }
+    for (size_t v = 0; v < n; v++)
+        for (int q = 0; q < 9; q++) h[q * n + v] = d->tranmat[9 * v + q];
+    if (e == cudaSuccess) e = put(c->tranmat, h.data(), 9 * n * sizeof(double));
+    for (size_t v = 0; v < n; v++)
+        for (int q = 0; q < 12; q++) h[q * n + v] = d->rho_s0[12 * v + q];
+    if (e == cudaSuccess) e = put(c->rho_s, h.data(), 12 * n * sizeof(double));
+    if (e == cudaSuccess) e = put(c->orient, d->voxel_orient, n * sizeof(int32_t));
+    if (e == cudaSuccess) e = put(c->phase, d->voxel_phase, n * sizeof(int32_t));
+    if (e == cudaSuccess && d->n_orient > 0) {
+        e = put(c->sgr64, d->s_gr, 36 * (size_t)d->n_orient * sizeof(double));
+        if (e == cudaSuccess && f32) {
+            std::vector<float> hf(36 * (size_t)d->n_orient);
+            for (size_t i = 0; i < hf.size(); i++) hf[i] = (float)d->s_gr[i];
+            e = put(c->sgr32, hf.data(), hf.size() * sizeof(float));
+        }
+    }
+    for (int a = 0; a < 3 && e == cudaSuccess; a++) {
+        const int na = d->n[a];
+        std::vector<double2> t64(na);
+        std::vector<float2> t32(na);
+        for (int t = 0; t < na; t++) {
+            double cc, ss;
+            unit_root(t, na, &cc, &ss);
+            t64[t] = make_double2(cc, ss);
+            t32[t] = make_float2((float)cc, (float)ss);
+        }
+        e = put(c->tw64[a], t64.data(), na * sizeof(double2));
+        if (e == cudaSuccess) e = put(c->tw32[a], t32.data(), na * sizeof(float2));
+    }
+    if (e != cudaSuccess) {
+        free_ctx(c);
+        return fail(EVPG_ERR_CUDA, "upload: %s", cudaGetErrorString(e));
+    }
+    *out = c;
+    return EVPG_OK;
+}
+
+int evpg_destroy(void* ctx) {
+    Ctx* c = (Ctx*)ctx;
+    if (!c) return EVPG_OK;
+    cudaStreamSynchronize(c->stream);
+    free_ctx(c);
+    return EVPG_OK;
+}
+
+int evpg_set_stream(void* ctx, void* s) {
+    Ctx* c = (Ctx*)ctx;
+    if (!c) return fail(EVPG_ERR_ARG, "null context");
+    CK(cudaStreamSynchronize(c->stream));
+    if (c->own_stream) cudaStreamDestroy(c->stream);
+    if (s) {
+        c->stream = (cudaStream_t)s;
+        c->own_stream = false;
+    } else {
+        CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+        c->own_stream = true;
+    }
+    return EVPG_OK;
+}
+
+int evpg_device_bytes(void* ctx, int64_t* bytes) {
+    Ctx* c = (Ctx*)ctx;
+    if (!c || !bytes) return fail(EVPG_ERR_ARG, "null argument");
+    *bytes = (int64_t)c->bytes;
+    return EVPG_OK;
+}
+
+int evpg_profile(void* ctx, int32_t enable) {
+    Ctx* c = (Ctx*)ctx;
+    if (!c) return fail(EVPG_ERR_ARG, "null context");
+    if (enable && !c->prof.recs) {
+        c->prof.cap = 4096;
+        c->prof.recs = new Profiler::Rec[c->prof.cap];
+        for (int i = 0; i < c->prof.cap; i++) {
+            CK(cudaEventCreate(&c->prof.recs[i].a));
+            CK(cudaEventCreate(&c->prof.recs[i].b));
+        }
+    }
+    prof_flush(*c);
+    for (int g = 0; g < PG_COUNT; g++) {
+        c->prof.ms[g] = 0.0;
+        c->prof.launches[g] = 0;
+    }
+    c->prof.on = enable != 0;
+    return EVPG_OK;
+}
+
+int evpg_launch_count(void* ctx, int64_t* n) {
+    Ctx* c = (Ctx*)ctx;
+    if (!c || !n) return fail(EVPG_ERR_ARG, "null argument");
+    *n = c->launches;
+    return EVPG_OK;
+}
+
+int evpg_profile_read(void* ctx, double* ms, int64_t* launches, int32_t n) {
+    Ctx* c = (Ctx*)ctx;
+    if (!c || !ms || !launches) return fail(EVPG_ERR_ARG, "null argument");
+    prof_flush(*c);
+    for (int g = 0; g < n && g < PG_COUNT; g++) {
+        ms[g] = c->prof.ms[g];
+        launches[g] = c->prof.launches[g];
+    }
+    return EVPG_OK;
+}
+
+int evpg_synchronize(void* ctx) {
+    Ctx* c = (Ctx*)ctx;
+    if (!c) return fail(EVPG_ERR_ARG, "null context");
+    CK(cudaStreamSynchronize(c->stream));
+    return EVPG_OK;
+}
+
+}  // extern "C"
+
+namespace evpg {
+
+__global__ void k_macro_begin(Macro* m, double drx, double err0) {
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) {
+            m->dE[i][j] = 0.0;
+            m->dE_acum[i][j] = 0.0;
+        }
+    for (int q = 0; q < 9; q++) m->dE9[q] = 0.0;
+    m->err_e = err0;
+    m->err_s = err0;
+    m->iter = 0;
+    m->done = 0;
+    m->converged = 0;
+    m->status = 0;
+    m->nr_iters = 0;
+    m->tpass_drx = drx;
+}
+
+__global__ void k_set_evm(Macro* m, double e_vm) { m->e_vm = e_vm; }
+
+static int read_macro(Ctx* c) {
+    CK(cudaMemcpyAsync(c->macro_host, c->macro, sizeof(Macro), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return EVPG_OK;
+}
+
+static void fill_iter_out(const Macro& m, evpg_iter_out* o) {
+    o->err_e = m.err_e;
+    o->err_s = m.err_s;
+    o->err_e_sum = m.err_e_sum;
+    o->err_s_sum = m.err_s_sum;
+    memcpy(o->sig_avg, m.sig_avg, sizeof o->sig_avg);
+    memcpy(o->sig_avg_ph1, m.sig_avg1, sizeof o->sig_avg_ph1);
+    memcpy(o->ddisgrad, m.dE, sizeof o->ddisgrad);
+    memcpy(o->ddisgrad_acum, m.dE_acum, sizeof o->ddisgrad_acum);
+    o->s_vm = m.s_vm;
+    o->s_vm1 = m.s_vm1;
+    o->iter = m.iter;
+    o->converged = m.converged;
+}
+
+static int launch_iteration(Ctx* c) {
+    CK(launch_spectral(*c));
+    CK(launch_nr(*c, 0));
+    CK(launch_macro(*c));
+    return EVPG_OK;
+}
+
+}  // namespace evpg
+
+extern "C" {
+
+int evpg_increment_begin(void* ctx, const double udot_dt[3][3], int32_t creep,
+                         const double dgavg[3][3], double time_tot) {
+    Ctx* c = (Ctx*)ctx;
+    if (!c || !udot_dt) return fail(EVPG_ERR_ARG, "null argument");
+    double u9[9], g9[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    tensor_to_9(udot_dt, u9);
+    if (creep) {
+        if (!dgavg) return fail(EVPG_ERR_ARG, "creep needs disgrad_avg_actual");
+        tensor_to_9(dgavg, g9);
+    }
+    // DeltaTau_DRX*exp((t_last-TimeTot)/TimeStep/tau_DRX), t_last = -1E3*tau_DRX*TimeStep
+    const double dt = c->m64.dt;
+    const double t_last = -1E3 * c->tau_drx * dt;
+    const double drx = c->delta_tau_drx * exp((t_last - time_tot) / dt / c->tau_drx);
+    k_macro_begin<<<1, 1, 0, c->stream>>>(c->macro, drx, 2. * c->cfg.err_tol);
+    c->launches++;
+    CK(cudaGetLastError());
+    CK(launch_begin(*c, u9, creep ? 1 : 0, g9, drx));
+    return EVPG_OK;
+}
+
+int evpg_equilibrium_iteration(void* ctx, double e_vm, evpg_iter_out* out) {
+    Ctx* c = (Ctx*)ctx;
+    if (!c) return fail(EVPG_ERR_ARG, "null context");
+    k_set_evm<<<1, 1, 0, c->stream>>>(c->macro, e_vm);
+    c->launches++;
+    CK(cudaGetLastError());
+    int st = launch_iteration(c);
+    if (st) return st;
+    st = read_macro(c);
+    if (st) return st;
+    if (out) fill_iter_out(*c->macro_host, out);
+    if (c->macro_host->status) return fail(c->macro_host->status, "%s", evpg_status_string(c->macro_host->status));
+    return EVPG_OK;
+}
+
+int evpg_equilibrium_solve(void* ctx, double e_vm, evpg_iter_out* out) {
+    Ctx* c = (Ctx*)ctx;
+    if (!c) return fail(EVPG_ERR_ARG, "null context");
+    k_set_evm<<<1, 1, 0, c->stream>>>(c->macro, e_vm);
+    c->launches++;
+    CK(cudaGetLastError());
+    int batch = c->prof.on ? 1 : 2;
+    for (;;) {
+        for (int b = 0; b < batch; b++) {
+            const int st = launch_iteration(c);
+            if (st) return st;
+        }
+        const int st = read_macro(c);
+        if (st) return st;
+        if (c->macro_host->done) break;
+        if (!c->prof.on && batch < 16) batch *= 2;
+    }
+    if (out) fill_iter_out(*c->macro_host, out);
+    if (c->macro_host->status) return fail(c->macro_host->status, "%s", evpg_status_string(c->macro_host->status));
+    return EVPG_OK;
+}
+
+int evpg_increment_end(void* ctx, int32_t reorient, evpg_incr_out* out) {
+    Ctx* c = (Ctx*)ctx;
+    if (!c) return fail(EVPG_ERR_ARG, "null context");
+    if (c->precision == EVPG_FP32_BULK) {
+        CK(launch_fold(*c));
+        CK(launch_nr(*c, 1));
+    }
+    CK(launch_end(*c, reorient ? 1 : 0));
+    int st = read_macro(c);
+    if (st) return st;
+    const Macro& m = *c->macro_host;
+    if (out) {
+        double e6[6], d6[6];
+        memcpy(e6, m.eps_avg6, sizeof e6);
+        memcpy(d6, m.edot_avg6, sizeof d6);
+        b6_to_sym<double>(e6, out->eps_avg);
+        b6_to_sym<double>(d6, out->edot_avg);
+        memcpy(out->rho_avg, m.rho_avg, sizeof out->rho_avg);
+        out->nr_iterations = m.nr_iters;
+    }
+    if (m.status) return fail(m.status, "%s", evpg_status_string(m.status));
+    return EVPG_OK;
+}
+
+int evpg_download(void* ctx, int32_t field, double* host, size_t count) {
+    Ctx* c = (Ctx*)ctx;
+    if (!c || !host) return fail(EVPG_ERR_ARG, "null argument");
+    const size_t n = (size_t)c->g.N;
+    const double* src = nullptr;
+    int planes = 0;
+    switch (field) {
+        case EVPG_F_SIG: case EVPG_F_SIG6: src = c->sig64; planes = 6; break;
+        case EVPG_F_DISGRAD: src = c->dg64; planes = 9; break;
+        case EVPG_F_EPS: src = c->epsp; planes = 6; break;
+        case EVPG_F_EDOT: src = c->edot64; planes = 5; break;
+        case EVPG_F_TRANMAT: src = c->tranmat; planes = 9; break;
+        case EVPG_F_RHO_S: src = c->rho_s; planes = 12; break;
+        case EVPG_F_RHO_M: src = c->rho_m; planes = 12; break;
+        case EVPG_F_GAMDOT: src = c->gamdot64; planes = 12; break;
+        case EVPG_F_GAM_ACUM: src = c->gam_acum; planes = 12; break;
+        case EVPG_F_VELGRAD: src = c->dg_old; planes = 9; break;
+        default: return fail(EVPG_ERR_ARG, "unknown field %d", field);
+    }
+    const int outw = (field == EVPG_F_SIG6) ? 6 : (planes == 12 ? 12 : 9);
+    if (count < (size_t)outw * n) return fail(EVPG_ERR_ARG, "buffer too small");
+    std::vector<double> h((size_t)planes * n);
+    CK(cudaMemcpyAsync(h.data(), src, h.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    for (size_t v = 0; v < n; v++) {
+        double q[12] = {0};
+        for (int p = 0; p < planes; p++) q[p] = h[p * n + v];
+        double* o = host + (size_t)outw * v;
+        if (planes == 12) {
+            memcpy(o, q, 12 * sizeof(double));
+        } else if (field == EVPG_F_TRANMAT) {
+            memcpy(o, q, 9 * sizeof(double));
+        } else {
+            double t[3][3];
+            if (planes == 9) nine_to_tensor(q, t);
+            else b6_to_sym<double>(q, t);  // EDOT: q[5] = 0
+            if (field == EVPG_F_SIG6) {
+                o[0] = t[0][0]; o[1] = t[1][1]; o[2] = t[2][2];
+                o[3] = t[1][2]; o[4] = t[0][2]; o[5] = t[0][1];
+            } else {
+                memcpy(o, t, sizeof t);
+            }
+        }
+    }
+    return EVPG_OK;
+}
+
+int evpg_upload(void* ctx, int32_t field, const double* host, size_t count) {
+    Ctx* c = (Ctx*)ctx;
+    if (!c || !host) return fail(EVPG_ERR_ARG, "null argument");
+    const size_t n = (size_t)c->g.N;
+    double* dst = nullptr;
+    int planes = 0;
+    switch (field) {
+        case EVPG_F_SIG: dst = c->sig64; planes = 6; break;
+        case EVPG_F_DISGRAD: dst = c->dg64; planes = 9; break;
+        case EVPG_F_EPS: dst = c->epsp; planes = 6; break;
+        case EVPG_F_TRANMAT: dst = c->tranmat; planes = 9; break;
+        case EVPG_F_RHO_S: dst = c->rho_s; planes = 12; break;
+        case EVPG_F_RHO_M: dst = c->rho_m; planes = 12; break;
+        case EVPG_F_GAM_ACUM: dst = c->gam_acum; planes = 12; break;
+        default: return fail(EVPG_ERR_ARG, "field %d cannot be uploaded", field);
+    }
+    const int inw = planes == 12 ? 12 : 9;
+    if (count < (size_t)inw * n) return fail(EVPG_ERR_ARG, "buffer too small");
+    std::vector<double> h((size_t)planes * n);
+    for (size_t v = 0; v < n; v++) {
+        const double* s = host + (size_t)inw * v;
+        double q[12];
+        if (planes == 12 || field == EVPG_F_TRANMAT) {
+            memcpy(q, s, inw * sizeof(double));
+        } else {
+            double t[3][3];
+            memcpy(t, s, sizeof t);
+            if (planes == 9) tensor_to_9(t, q);
+            else sym_to_b6<double>(t, q);
+        }
+        for (int p = 0; p < planes; p++) h[p * n + v] = q[p];
+    }
+    CK(cudaMemcpyAsync(dst, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (field == EVPG_F_SIG && c->precision == EVPG_FP32_BULK) {
+        std::vector<float> hf(6 * n);
+        for (size_t i = 0; i < hf.size(); i++) hf[i] = (float)h[i];
+        CK(cudaMemcpyAsync(c->sig32, hf.data(), hf.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+    }
+    return EVPG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,164 @@
+// Shared-memory Stockham FFT for batches of pencils (radix 8/4/2/3/5 and a
+// generic O(p^2) stage for other primes). Replaces the FFTW 2 transforms of
+// the reference (fftwnd_mpi, evolution.c:1163,1195): unnormalised, exponent
+// sign -1 forward and +1 inverse.
+//
+// A CTA holds `npen` pencils of length n, pencil-major in shared memory, and
+// runs all stages with two buffers (ping-pong), one __syncthreads per stage.
+// Twiddles W_n^t = exp(-2 pi i t / n) come from a table in shared memory; the
+// inverse uses their conjugates.
+#pragma once
+#include "evpg_common.cuh"
+
+namespace evpg {
+
+template <typename T, int SIGN>
+__device__ __forceinline__ C2<T> mul_isign(C2<T> a) {
+    // (SIGN*i) * a
+    return SIGN < 0 ? mk<T>(a.y, -a.x) : mk<T>(-a.y, a.x);
+}
+
+template <typename T, int SIGN>
+__device__ __forceinline__ void dft4(C2<T>& a0, C2<T>& a1, C2<T>& a2, C2<T>& a3) {
+    const C2<T> s02 = cadd<T>(a0, a2), d02 = csub<T>(a0, a2);
+    const C2<T> s13 = cadd<T>(a1, a3), d13 = mul_isign<T, SIGN>(csub<T>(a1, a3));
+    a0 = cadd<T>(s02, s13);
+    a2 = csub<T>(s02, s13);
+    a1 = cadd<T>(d02, d13);
+    a3 = csub<T>(d02, d13);
+}
+
+template <typename T, int SIGN>
+__device__ __forceinline__ void dft8(C2<T>* v) {
+    C2<T> e0 = v[0], e1 = v[2], e2 = v[4], e3 = v[6];
+    C2<T> o0 = v[1], o1 = v[3], o2 = v[5], o3 = v[7];
+    dft4<T, SIGN>(e0, e1, e2, e3);
+    dft4<T, SIGN>(o0, o1, o2, o3);
+    const T h = (T)0.70710678118654752440;
+    // W8 = h(1 + SIGN i), W8^2 = SIGN i, W8^3 = h(-1 + SIGN i)
+    const C2<T> w1 = mk<T>(h * (o1.x - (T)SIGN * o1.y), h * (o1.y + (T)SIGN * o1.x));
+    const C2<T> w2 = mul_isign<T, SIGN>(o2);
+    const C2<T> w3 = mk<T>(h * (-o3.x - (T)SIGN * o3.y), h * (-o3.y + (T)SIGN * o3.x));
+    v[0] = cadd<T>(e0, o0); v[4] = csub<T>(e0, o0);
+    v[1] = cadd<T>(e1, w1); v[5] = csub<T>(e1, w1);
+    v[2] = cadd<T>(e2, w2); v[6] = csub<T>(e2, w2);
+    v[3] = cadd<T>(e3, w3); v[7] = csub<T>(e3, w3);
+}
+
+template <typename T, int SIGN>
+__device__ __forceinline__ void dft3(C2<T>* v) {
+    const T s = (T)SIGN * (T)0.86602540378443864676;
+    const C2<T> t1 = cadd<T>(v[1], v[2]), t2 = csub<T>(v[1], v[2]);
+    const C2<T> m = mk<T>(v[0].x - (T)0.5 * t1.x, v[0].y - (T)0.5 * t1.y);
+    const C2<T> r = mk<T>(-s * t2.y, s * t2.x);  // i*s*t2
+    v[0] = cadd<T>(v[0], t1);
+    v[1] = cadd<T>(m, r);
+    v[2] = csub<T>(m, r);
+}
+
+template <typename T, int SIGN>
+__device__ __forceinline__ void dft5(C2<T>* v) {
+    const T c1 = (T)0.30901699437494742410, c2 = (T)-0.80901699437494742410;
+    const T s1 = (T)SIGN * (T)0.95105651629515357212, s2 = (T)SIGN * (T)0.58778525229247312917;
+    const C2<T> a1 = cadd<T>(v[1], v[4]), b1 = csub<T>(v[1], v[4]);
+    const C2<T> a2 = cadd<T>(v[2], v[3]), b2 = csub<T>(v[2], v[3]);
+    const C2<T> x0 = v[0];
+    const C2<T> m1 = mk<T>(x0.x + c1 * a1.x + c2 * a2.x, x0.y + c1 * a1.y + c2 * a2.y);
+    const C2<T> m2 = mk<T>(x0.x + c2 * a1.x + c1 * a2.x, x0.y + c2 * a1.y + c1 * a2.y);
+    const C2<T> q1 = mk<T>(s1 * b1.x + s2 * b2.x, s1 * b1.y + s2 * b2.y);
+    const C2<T> q2 = mk<T>(s2 * b1.x - s1 * b2.x, s2 * b1.y - s1 * b2.y);
+    // i*q = (-q.y, q.x)
+    v[0] = mk<T>(x0.x + a1.x + a2.x, x0.y + a1.y + a2.y);
+    v[1] = mk<T>(m1.x - q1.y, m1.y + q1.x);
+    v[4] = mk<T>(m1.x + q1.y, m1.y - q1.x);
+    v[2] = mk<T>(m2.x - q2.y, m2.y + q2.x);
+    v[3] = mk<T>(m2.x + q2.y, m2.y - q2.x);
+}
+
+template <typename T, int SIGN>
+__device__ __forceinline__ C2<T> twid(const C2<T>* tw, int t) {
+    const C2<T> w = tw[t];
+    return SIGN < 0 ? w : mk<T>(w.x, -w.y);
+}
+
+// Run every stage of `pl` on npen pencils held in `a` (pencil p starts at
+// element p*ps, ps >= n; scratch `b` has the same layout). Returns the buffer
+// holding the result. Must be called by all threads of the CTA; ends with a
+// __syncthreads.
+template <typename T, int SIGN>
+__device__ C2<T>* fft_batch(C2<T>* a, C2<T>* b, int npen, int ps, const FftPlan& pl,
+                            const C2<T>* tw) {
+    const int n = pl.n;
+    C2<T>* in = a;
+    C2<T>* out = b;
+    for (int s = 0; s < pl.nf; s++) {
+        const int r = pl.radix[s], Ns = pl.ns[s], m = n / r, tws = n / (Ns * r);
+        const int total = npen * m;
+        for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+            const int pen = idx / m, j = idx - pen * m;
+            const int jm = j % Ns;
+            const C2<T>* src = in + pen * ps + j;
+            C2<T>* dst = out + pen * ps + (j / Ns) * Ns * r + jm;
+            C2<T> v[8];
+            if (r == 8) {
+#pragma unroll
+                for (int q = 0; q < 8; q++) {
+                    v[q] = src[q * m];
+                    if (q) v[q] = cmul<T>(v[q], twid<T, SIGN>(tw, q * jm * tws));
+                }
+                dft8<T, SIGN>(v);
+#pragma unroll
+                for (int q = 0; q < 8; q++) dst[q * Ns] = v[q];
+            } else if (r == 4) {
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    v[q] = src[q * m];
+                    if (q) v[q] = cmul<T>(v[q], twid<T, SIGN>(tw, q * jm * tws));
+                }
+                dft4<T, SIGN>(v[0], v[1], v[2], v[3]);
+#pragma unroll
+                for (int q = 0; q < 4; q++) dst[q * Ns] = v[q];
+            } else if (r == 2) {
+                v[0] = src[0];
+                v[1] = cmul<T>(src[m], twid<T, SIGN>(tw, jm * tws));
+                dst[0] = cadd<T>(v[0], v[1]);
+                dst[Ns] = csub<T>(v[0], v[1]);
+            } else if (r == 3) {
+#pragma unroll
+                for (int q = 0; q < 3; q++) {
+                    v[q] = src[q * m];
+                    if (q) v[q] = cmul<T>(v[q], twid<T, SIGN>(tw, q * jm * tws));
+                }
+                dft3<T, SIGN>(v);
+#pragma unroll
+                for (int q = 0; q < 3; q++) dst[q * Ns] = v[q];
+            } else if (r == 5) {
+#pragma unroll
+                for (int q = 0; q < 5; q++) {
+                    v[q] = src[q * m];
+                    if (q) v[q] = cmul<T>(v[q], twid<T, SIGN>(tw, q * jm * tws));
+                }
+                dft5<T, SIGN>(v);
+#pragma unroll
+                for (int q = 0; q < 5; q++) dst[q * Ns] = v[q];
+            } else {
+                // generic prime radix: O(r^2) with the table (W_r^k = W_n^{k n/r})
+                const int step = n / r;
+                for (int q = 0; q < r; q++) {
+                    C2<T> acc = mk<T>((T)0, (T)0);
+                    for (int p = 0; p < r; p++) {
+                        C2<T> x = src[p * m];
+                        if (p) x = cmul<T>(x, twid<T, SIGN>(tw, p * jm * tws));
+                        acc = cadd<T>(acc, cmul<T>(x, twid<T, SIGN>(tw, ((p * q) % r) * step)));
+                    }
+                    dst[q * Ns] = acc;
+                }
+            }
+        }
+        __syncthreads();
+        C2<T>* t = in; in = out; out = t;
+    }
+    return in;
+}
+
+}  // namespace evpg

@@ -1,0 +1,984 @@
+// Per-voxel kernels of the equilibrium iteration and of the increment head
+// and tail, plus the device-side macro update.
+//
+//   k_nr         UpdateStress (evolution.c:157-427) with StrainRate_Orowan
+//                (constitutive.c:507-728): Newton on
+//                R(s) = s - lambda + C066 (Eps + edot(s) dt + S s - eps)
+//                one thread per voxel. The Newton step J^-1 R with
+//                J = I + C066 (S + dt d_edot) is computed as
+//                M^-1 (S066 R), M = S066 + S + dt d_edot (C066 S066 = I), which
+//                is symmetric positive definite, so an unpivoted LDL^T
+//                suffices. Plain update or the NR_MODIFIED line search.
+//   k_macro      error Allreduce + get_smacro + normalisation + loop test
+//                (evolution.c:1227-1252, 590-664), one CTA, FP64.
+//   k_begin      increment head: VelGrad <- DisGrad, DisGrad += Udot dt,
+//                update_schmid, flow-rule constants of this increment.
+//   k_end        increment tail: VelGrad, Eps, update_orient,
+//                DislocationEvolution, partial sums of the averages.
+//   k_end_reduce AvgDislocation and the Eps/Edot averages.
+#include "evpg_ctx.h"
+
+#include <stdio.h>
+
+namespace evpg {
+
+
+// ------------------------------------------------------------ reductions
+
+// Compensated (two-sum) accumulation, used for FP32 partials.
+struct KSum {
+    float s, c;
+    __device__ __forceinline__ void add(float x) {
+        const float t = s + x;
+        const float bp = t - s;
+        c += (s - (t - bp)) + (x - bp);
+        s = t;
+    }
+};
+
+template <int NQ>
+__device__ __forceinline__ void block_reduce_store(double (&v)[NQ], double* out) {
+    __shared__ double red[NQ][32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int q = 0; q < NQ; q++) {
+        double x = v[q];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+        if (lane == 0) red[q][wid] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < NQ) {
+        double s = 0.0;
+        for (int w = 0; w < nw; w++) s += red[threadIdx.x][w];
+        out[threadIdx.x] = s;
+    }
+}
+
+template <int NQ>
+__device__ __forceinline__ void block_reduce_store_f(float (&v)[NQ], double* out) {
+    __shared__ double red[NQ][32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int q = 0; q < NQ; q++) {
+        KSum k{v[q], 0.0f};
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float s = __shfl_xor_sync(0xffffffffu, k.s, o);
+            const float c = __shfl_xor_sync(0xffffffffu, k.c, o);
+            k.add(s);
+            k.c += c;
+        }
+        if (lane == 0) red[q][wid] = (double)k.s + (double)k.c;
+    }
+    __syncthreads();
+    if (threadIdx.x < NQ) {
+        double s = 0.0;
+        for (int w = 0; w < nw; w++) s += red[threadIdx.x][w];
+        out[threadIdx.x] = s;
+    }
+}
+
+__device__ __forceinline__ void set_status(Macro* m, int st) { atomicCAS(&m->status, 0, st); }
+
+// ------------------------------------------------------------------- NR
+
+template <typename T> struct NrArgs {
+    Material<T> mat;
+    Grid g;
+    T* sig;               // [6][N] lambda in, sigma out
+    const T* dg;          // [9][N] strain source ([0..5] used)
+    const T* epsb;        // [6][N] a = epsb - dg: Eps (FP64) or Eps - eps_begin (FP32)
+    const T* schm;        // [60][N]
+    const T* fc;          // [48][N]
+    const int32_t* orient;
+    const int32_t* phase;
+    const T* sgr;         // [n_orient][36]
+    T* edot;              // [5][N] or null
+    T* gamdot;            // [12][N] or null
+    Macro* macro;
+    double* part;         // [gridDim][NPART_NR]
+    T tol;
+    int itmax, nr_mode;
+    int stale_mode;       // 1: the first flow-rule call of the increment uses the stored rho_m
+    int check_done;
+};
+
+template <typename T> struct Eval {
+    T edot[5];
+    T d[15];   // upper triangle of d_edot (5x5)
+    T gam[NS];
+};
+
+__device__ __forceinline__ void sinh_cosh(double x, double& sh, double& ch) {
+    if (x < 700.0) {
+        const double e = exp(x), ei = 1.0 / e;
+        sh = 0.5 * (e - ei);
+        ch = 0.5 * (e + ei);
+    } else {
+        sh = sinh(x);
+        ch = cosh(x);
+    }
+}
+// FP32 overflows at x ~ 89 (FP64 at ~710): the argument is capped at 85,
+// where the rate is ~1e37 gam_o and any line-search trial is rejected anyway.
+__device__ __forceinline__ void sinh_cosh(float x, float& sh, float& ch) {
+    const float e = __expf(fminf(x, 85.0f)), ei = __fdividef(1.0f, e);
+    sh = 0.5f * (e - ei);
+    ch = 0.5f * (e + ei);
+}
+
+// StrainRate_Orowan at stress s (constitutive.c:585-725): per system the
+// resolved shear stress, sinh glide law and its derivative; returns edot,
+// d_edot and the shear rates. bad |= NaN seen.
+template <typename T>
+__device__ __forceinline__ void flow_eval(const NrArgs<T>& a, const PhaseK<T>& P, int v,
+                                          const T* s, bool stale, Eval<T>& e, bool& bad) {
+    const size_t N = a.g.N;
+#pragma unroll
+    for (int q = 0; q < 5; q++) e.edot[q] = (T)0;
+#pragma unroll
+    for (int q = 0; q < 15; q++) e.d[q] = (T)0;
+#pragma unroll
+    for (int i = 0; i < NS; i++) {
+        e.gam[i] = (T)0;
+        if (i >= P.n_sys) continue;
+        T sc[5];
+#pragma unroll
+        for (int q = 0; q < 5; q++) sc[q] = __ldg(a.schm + (size_t)(i * 5 + q) * N + v);
+        const T rss = sc[0] * s[0] + sc[1] * s[1] + sc[2] * s[2] + sc[3] * s[3] + sc[4] * s[4];
+        const T tp = __ldg(a.fc + (size_t)((stale ? 36 : 0) + i) * N + v);
+        const T ar = fabs(rss);
+        if (ar > tp) {
+            const T itc = __ldg(a.fc + (size_t)(12 + i) * N + v);
+            const T go = __ldg(a.fc + (size_t)(24 + i) * N + v);
+            T sh, ch;
+            sinh_cosh((ar - tp) * itc, sh, ch);
+            const T g = (rss > (T)0) ? go * sh : -(go * sh);
+            const T g2 = go * ch * itc;
+            if (isnan(g) || isnan(g2)) bad = true;
+            e.gam[i] = g;
+#pragma unroll
+            for (int q = 0; q < 5; q++) e.edot[q] += sc[q] * g;
+            int k = 0;
+#pragma unroll
+            for (int p = 0; p < 5; p++) {
+                const T w = sc[p] * g2;
+#pragma unroll
+                for (int q = p; q < 5; q++) e.d[k++] += w * sc[q];
+            }
+        }
+    }
+    // constitutive.c:707,718 assert on NaN in edot and d_edot
+#pragma unroll
+    for (int q = 0; q < 5; q++) bad = bad || isnan(e.edot[q]);
+#pragma unroll
+    for (int q = 0; q < 15; q++) bad = bad || isnan(e.d[q]);
+}
+
+// Packed symmetric 6x6: index of (i,j), i <= j.
+__host__ __device__ constexpr int sidx(int i, int j) { return i * 6 - i * (i - 1) / 2 + (j - i); }
+
+// Solve M x = b for symmetric positive definite M (packed upper, 21 entries)
+// by LDL^T without pivoting. Returns false when a pivot is not positive.
+template <typename T>
+__device__ __forceinline__ bool ldl_solve(const T (&m)[21], const T (&b)[6], T (&x)[6]) {
+    T L[6][6], d[6], id[6];
+#pragma unroll
+    for (int j = 0; j < 6; j++) {
+        T s = m[sidx(j, j)];
+#pragma unroll
+        for (int k = 0; k < j; k++) s -= L[j][k] * L[j][k] * d[k];
+        d[j] = s;
+        id[j] = (T)1 / s;
+#pragma unroll
+        for (int i = j + 1; i < 6; i++) {
+            T t = m[sidx(j, i)];
+#pragma unroll
+            for (int k = 0; k < j; k++) t -= L[i][k] * L[j][k] * d[k];
+            L[i][j] = t * id[j];
+        }
+    }
+    bool ok = true;
+#pragma unroll
+    for (int j = 0; j < 6; j++) ok = ok && (d[j] > (T)0);
+    T y[6];
+#pragma unroll
+    for (int i = 0; i < 6; i++) {
+        T s = b[i];
+#pragma unroll
+        for (int k = 0; k < i; k++) s -= L[i][k] * y[k];
+        y[i] = s;
+    }
+#pragma unroll
+    for (int i = 5; i >= 0; i--) {
+        T s = y[i] * id[i];
+#pragma unroll
+        for (int k = i + 1; k < 6; k++) s -= L[k][i] * x[k];
+        x[i] = s;
+    }
+    return ok;
+}
+
+template <typename T>
+__device__ __forceinline__ void mat6v(const T (&m)[6][6], const T* x, T* y) {
+#pragma unroll
+    for (int i = 0; i < 6; i++) {
+        T s = (T)0;
+#pragma unroll
+        for (int j = 0; j < 6; j++) s += m[i][j] * x[j];
+        y[i] = s;
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(NR_BLOCK) k_nr(const __grid_constant__ NrArgs<T> a) {
+    if (a.check_done && a.macro->done) return;
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    const int N = a.g.N;
+    const double dtd = (double)a.mat.dt;
+    const T dt = a.mat.dt;
+    T pe = 0, ps = 0, ss[6] = {0, 0, 0, 0, 0, 0}, s1[6] = {0, 0, 0, 0, 0, 0};
+    int nr = 0;
+    bool bad = false, sing = false, lsfail = false;
+    const bool stale0 = a.stale_mode && a.macro->iter == 0;
+    if (v < N) {
+        const int ph = a.phase[v];
+        const PhaseK<T>& P = a.mat.ph[ph - 1];
+        if (!P.crystal) {
+#pragma unroll
+            for (int c = 0; c < 6; c++) a.sig[(size_t)c * N + v] = (T)0;
+            if (a.edot)
+#pragma unroll
+                for (int c = 0; c < 5; c++) a.edot[(size_t)c * N + v] = (T)0;
+        } else {
+            const T* sg = a.sgr + (size_t)a.orient[v] * 36;
+            T S[6][6];
+#pragma unroll
+            for (int i = 0; i < 6; i++)
+#pragma unroll
+                for (int j = 0; j < 6; j++) S[i][j] = __ldg(sg + i * 6 + j);
+            T lam[6], sig[6], av[6], m0[21];
+#pragma unroll
+            for (int c = 0; c < 6; c++) {
+                lam[c] = a.sig[(size_t)c * N + v];
+                sig[c] = lam[c];
+                av[c] = a.epsb[(size_t)c * N + v] - a.dg[(size_t)c * N + v];
+            }
+#pragma unroll
+            for (int i = 0; i < 6; i++)
+#pragma unroll
+                for (int j = i; j < 6; j++)
+                    m0[sidx(i, j)] = a.mat.s066[i][j] + (T)0.5 * (S[i][j] + S[j][i]);
+            T signorm = 0;
+#pragma unroll
+            for (int c = 0; c < 6; c++) signorm += lam[c] * lam[c];
+            signorm = sqrt(signorm);
+            T erral = (T)10 * a.tol, ce = 0, cs = 0;
+            Eval<T> ev, et;
+            bool have = false;
+            T edot_out[5] = {0, 0, 0, 0, 0};
+            T gl[NS];  // shear rates of the last flow-rule call (gamdot)
+#pragma unroll
+            for (int i = 0; i < NS; i++) gl[i] = (T)0;
+            int it = 0;
+            while (it < a.itmax && fabs(erral) > fabs(a.tol)) {
+                it++;
+                T old[6];
+#pragma unroll
+                for (int c = 0; c < 6; c++) old[c] = sig[c];
+                if (!have) flow_eval<T>(a, P, v, sig, stale0 && it == 1, ev, bad);
+                have = false;
+#pragma unroll
+                for (int i = 0; i < NS; i++) gl[i] = ev.gam[i];
+                if (bad) break;
+#pragma unroll
+                for (int q = 0; q < 5; q++) edot_out[q] = ev.edot[q];
+                // te = tot_eps - strain = (Eps - strain) + edot dt + S sig
+                T te[6], Ss[6];
+                mat6v<T>(S, sig, Ss);
+#pragma unroll
+                for (int c = 0; c < 6; c++) te[c] = av[c] + (c < 5 ? ev.edot[c] * dt : (T)0) + Ss[c];
+                T m[21];
+#pragma unroll
+                for (int k = 0; k < 21; k++) m[k] = m0[k];
+                {
+                    int k = 0;
+#pragma unroll
+                    for (int p = 0; p < 5; p++)
+#pragma unroll
+                        for (int q = p; q < 5; q++) m[sidx(p, q)] += dt * ev.d[k++];
+                }
+                // rhs = S066 R = S066 (sig - lam) + te
+                T dl[6], rhs[6], step[6];
+#pragma unroll
+                for (int c = 0; c < 6; c++) dl[c] = sig[c] - lam[c];
+                mat6v<T>(a.mat.s066, dl, rhs);
+#pragma unroll
+                for (int c = 0; c < 6; c++) rhs[c] += te[c];
+                if (!ldl_solve<T>(m, rhs, step)) sing = true;
+                if (a.nr_mode == 0) {
+#pragma unroll
+                    for (int c = 0; c < 6; c++) sig[c] -= step[c];
+                } else {
+                    // NR_MODIFIED (evolution.c:280-371). The reference evaluates
+                    // slope = (J^T R).step with step = -J^-1 R (capped at length 10);
+                    // that product is -|R|^2 times the cap factor, used here directly:
+                    // through an ill-conditioned J its rounded value can change sign.
+                    T R[6], CR[6], f_old = 0;
+                    mat6v<T>(a.mat.c066, te, CR);
+#pragma unroll
+                    for (int c = 0; c < 6; c++) {
+                        R[c] = dl[c] + CR[c];
+                        f_old += R[c] * R[c];
+                    }
+                    T slope = -f_old;
+                    f_old *= (T)0.5;
+                    T nrm = 0;
+#pragma unroll
+                    for (int c = 0; c < 6; c++) {
+                        step[c] = -step[c];
+                        nrm += step[c] * step[c];
+                    }
+                    nrm = sqrt(nrm);
+                    if (nrm > (T)10) {
+                        const T cap = (T)10 / nrm;
+#pragma unroll
+                        for (int c = 0; c < 6; c++) step[c] *= cap;
+                        slope *= cap;
+                    }
+                    if (!(slope < (T)0)) {
+                        // R == 0: already at the root
+                        if (slope == (T)0) {
+#pragma unroll
+                            for (int c = 0; c < 6; c++) sig[c] = old[c];
+                        } else {
+                            lsfail = true;
+                            break;
+                        }
+                    } else {
+                        T test = 0;
+    #pragma unroll
+                        for (int c = 0; c < 6; c++) {
+                            const T tt = fabs(step[c]) / fmax(fabs(old[c]), (T)1);
+                            if (tt > test) test = tt;
+                        }
+                        const T alamin = (T)1e-7 / test;
+                        T alam = 1, alam2 = 0, tmplam = 0;
+                        const T f2 = 0;  // never updated in the reference
+                        for (int ls = 0; ls < 200; ls++) {
+    #pragma unroll
+                            for (int c = 0; c < 6; c++) sig[c] = old[c] + alam * step[c];
+                            flow_eval<T>(a, P, v, sig, false, et, bad);
+    #pragma unroll
+                            for (int i = 0; i < NS; i++) gl[i] = et.gam[i];
+                            if (bad) break;
+                            T Rt[6], tt6[6], fnew = 0;
+                            mat6v<T>(S, sig, Ss);
+    #pragma unroll
+                            for (int c = 0; c < 6; c++) tt6[c] = av[c] + (c < 5 ? et.edot[c] * dt : (T)0) + Ss[c];
+                            mat6v<T>(a.mat.c066, tt6, Rt);
+    #pragma unroll
+                            for (int c = 0; c < 6; c++) {
+                                const T r = sig[c] - lam[c] + Rt[c];
+                                fnew += r * r;
+                            }
+                            fnew *= (T)0.5;
+                            if (alam < alamin) {
+    #pragma unroll
+                                for (int c = 0; c < 6; c++) sig[c] = old[c];
+                                break;
+                            } else if (fnew <= f_old + (T)1e-4 * alam * slope) {
+                                ev = et;
+                                have = true;
+                                break;
+                            } else {
+                                if (fabs(alam - (T)1) < (T)1e-4) {
+                                    tmplam = -slope / ((T)2 * (fnew - f_old - slope));
+                                } else {
+                                    const T rhs1 = fnew - f_old - alam * slope;
+                                    const T rhs2 = f2 - f_old - alam2 * slope;
+                                    const T ac = (rhs1 / (alam * alam) - rhs2 / (alam2 * alam2)) / (alam - alam2);
+                                    const T bc = (-alam2 * rhs1 / (alam * alam) + alam * rhs2 / (alam2 * alam2)) /
+                                                 (alam - alam2);
+                                    if (fabs(ac) < (T)1e-4) {
+                                        tmplam = -slope / ((T)2 * bc);
+                                    } else {
+                                        const T disc = bc * bc - (T)3 * ac * slope;
+                                        if (disc < (T)0) tmplam = (T)0.5 * alam;
+                                        else if (bc <= (T)0) tmplam = (-bc + sqrt(disc)) / ((T)3 * ac);
+                                        else tmplam = -slope / (bc + sqrt(disc));
+                                    }
+                                    if (tmplam > (T)0.5 * alam) tmplam = (T)0.5 * alam;
+                                }
+                            }
+                            alam2 = alam;
+                            alam = fmax(tmplam, (T)0.1 * alam);
+                        }
+                    }
+                }
+                T cnr = 0;
+                ce = 0;
+                cs = 0;
+#pragma unroll
+                for (int c = 0; c < 6; c++) {
+                    cnr += (sig[c] - old[c]) * (sig[c] - old[c]);
+                    ce += te[c] * te[c];
+                    cs += (sig[c] - lam[c]) * (sig[c] - lam[c]);
+                }
+                erral = sqrt(cnr) / signorm;
+                ce = sqrt(ce);
+                cs = sqrt(cs);
+                if (bad || sing) break;
+            }
+            nr = it;
+#pragma unroll
+            for (int c = 0; c < 6; c++) a.sig[(size_t)c * N + v] = sig[c];
+            if (a.edot)
+#pragma unroll
+                for (int c = 0; c < 5; c++) a.edot[(size_t)c * N + v] = edot_out[c];
+            if (a.gamdot)
+#pragma unroll
+                for (int i = 0; i < NS; i++)
+                    if (i < P.n_sys) a.gamdot[(size_t)i * N + v] = gl[i];
+            pe = ce;
+            ps = cs;
+#pragma unroll
+            for (int c = 0; c < 6; c++) {
+                ss[c] = sig[c];
+                s1[c] = (ph == 1) ? sig[c] : (T)0;
+            }
+        }
+    }
+    (void)dtd;
+    if (bad) set_status(a.macro, 4);
+    if (sing) set_status(a.macro, 5);
+    if (lsfail) set_status(a.macro, 6);
+    double* out = a.part + (size_t)blockIdx.x * NPART_NR;
+    if (sizeof(T) == 8) {
+        double q[NPART_NR];
+        q[0] = (double)pe; q[1] = (double)ps;
+#pragma unroll
+        for (int c = 0; c < 6; c++) { q[2 + c] = (double)ss[c]; q[8 + c] = (double)s1[c]; }
+        q[14] = (double)nr;
+        block_reduce_store<NPART_NR>(q, out);
+    } else {
+        float q[NPART_NR];
+        q[0] = (float)pe; q[1] = (float)ps;
+#pragma unroll
+        for (int c = 0; c < 6; c++) { q[2 + c] = (float)ss[c]; q[8 + c] = (float)s1[c]; }
+        q[14] = (float)nr;
+        block_reduce_store_f<NPART_NR>(q, out);
+    }
+}
+
+// ---------------------------------------------------------------- macro
+
+struct MacroArgs {
+    LoopCfg cfg;
+    Macro* macro;
+    const double* part;
+    int nblocks;
+};
+
+// Sum of the NR partials, then get_smacro (evolution.c:590-664), the error
+// normalisation (evolution.c:1233-1252) and the loop test (evolution.c:1150).
+__global__ void __launch_bounds__(256) k_macro(const __grid_constant__ MacroArgs a) {
+    Macro* m = a.macro;
+    if (m->done) return;
+    __shared__ double tot[NPART_NR];
+    {
+        double v[NPART_NR];
+#pragma unroll
+        for (int q = 0; q < NPART_NR; q++) v[q] = 0.0;
+        for (int b = threadIdx.x; b < a.nblocks; b += blockDim.x)
+#pragma unroll
+            for (int q = 0; q < NPART_NR; q++) v[q] += a.part[(size_t)b * NPART_NR + q];
+        double o[NPART_NR];
+        block_reduce_store<NPART_NR>(v, o);
+        if (threadIdx.x < NPART_NR) tot[threadIdx.x] = o[threadIdx.x];
+    }
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    const LoopCfg& c = a.cfg;
+    double s6[6], s16[6], sa[3][3], s1a[3][3];
+    for (int q = 0; q < 6; q++) {
+        s6[q] = tot[2 + q];
+        s16[q] = tot[8 + q];
+    }
+    b6_to_sym<double>(s6, sa);
+    b6_to_sym<double>(s16, s1a);
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) {
+            m->sig_avg[i][j] = sa[i][j] * c.wgt;
+            m->sig_avg1[i][j] = s1a[i][j] * (c.wgt / c.wgt_ph1);
+        }
+    static const int IJV[2][6] = {{0, 1, 2, 1, 0, 0}, {0, 1, 2, 2, 2, 1}};
+    for (int i = 0; i < 6; i++) {
+        const int ii = IJV[0][i], jj = IJV[1][i];
+        double d = 0.0;
+        if (c.vflag[i] == 0)
+            for (int k = 0; k < 6; k++) {
+                const int kk = IJV[0][k], ll = IJV[1][k];
+                d += c.s0[ii][jj][kk][ll] * c.sflag[k] * (c.scauchy[kk][ll] - m->sig_avg[kk][ll]);
+            }
+        m->dE[ii][jj] = d;
+    }
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) m->dE_acum[i][j] += m->dE[i][j];
+    {
+        double e6[6];
+        sym_to_b6<double>(m->dE, e6);
+        for (int q = 0; q < 6; q++) m->dE9[q] = e6[q];
+        m->dE9[6] = 0.5 * (m->dE[0][1] - m->dE[1][0]);
+        m->dE9[7] = 0.5 * (m->dE[0][2] - m->dE[2][0]);
+        m->dE9[8] = 0.5 * (m->dE[1][2] - m->dE[2][1]);
+    }
+    // s_vm: the reference's trace term reads SigDevAvg[3][3], one element past
+    // the array; in its global layout that is SigAvg1[0][0].
+    {
+        double v6[6], dev[3][3];
+        sym_to_b6<double>(m->sig_avg, v6);
+        v6[5] = 0.0;
+        b6_to_sym<double>(v6, dev);
+        const double oob = m->sig_avg1[0][0];
+        double s = 0.0;
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) {
+                if (i != j) s += dev[i][j] * dev[i][j];
+                else {
+                    const double d = dev[i][j] - (dev[1][1] + dev[2][2] + oob) / 3.0;
+                    s += d * d;
+                }
+            }
+        m->s_vm = sqrt(1.5 * s);
+        sym_to_b6<double>(m->sig_avg1, v6);
+        v6[5] = 0.0;
+        b6_to_sym<double>(v6, dev);
+        s = 0.0;
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) s += dev[i][j] * dev[i][j];
+        m->s_vm1 = sqrt(1.5 * s);
+    }
+    m->err_e_sum = tot[0];
+    m->err_s_sum = tot[1];
+    double ee = tot[0] * c.wgt, es = tot[1] * c.wgt;
+    if (fabs(m->e_vm) < 1E-5) ee = 0.0;
+    else ee /= m->e_vm;
+    es /= m->s_vm;
+    m->err_e = ee;
+    m->err_s = es;
+    m->nr_iters += (long long)tot[14];
+    m->iter += 1;
+    const double mx = (fabs(es) > fabs(ee)) ? fabs(es) : fabs(ee);
+    m->converged = !(mx > c.err_tol);
+    m->done = m->converged || m->iter >= c.iter_max || m->status != 0;
+}
+
+// ------------------------------------------------------ increment head
+
+struct BeginArgs {
+    Material<double> mat;
+    Grid g;
+    double udot9[9];     // applied Udot*dt in the field representation
+    double dgavg9[9];    // uniform DisGrad for creep
+    int creep;
+    double drx;          // DeltaTau_DRX*exp(...) of this increment
+    double* dg64;        // [9][N]
+    double* dg_old;      // [9][N]
+    const double* tranmat;
+    const double* rho_s;
+    const double* rho_m;
+    const int32_t* phase;
+    double* schm64;      // [60][N]
+    double* fc64;        // [48][N]
+    // FP32 bulk
+    float* schm32;
+    float* fc32;
+    float* b6_32;
+    float* ddg32;
+    const double* epsp;
+};
+
+// update_schmid (kinematics.c:430-463) and the rho-dependent products of the
+// flow rule that stay fixed during an increment (constitutive.c:559-633).
+__global__ void __launch_bounds__(128) k_begin(const __grid_constant__ BeginArgs a) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    const int N = a.g.N;
+    if (v >= N) return;
+#pragma unroll
+    for (int c = 0; c < 9; c++) {
+        const double d = a.dg64[(size_t)c * N + v];
+        a.dg_old[(size_t)c * N + v] = d;
+        a.dg64[(size_t)c * N + v] = a.creep ? a.dgavg9[c] : d + a.udot9[c];
+    }
+    const int ph = a.phase[v];
+    const PhaseK<double>& P = a.mat.ph[ph - 1];
+    if (a.b6_32) {
+#pragma unroll
+        for (int c = 0; c < 6; c++) {
+            a.b6_32[(size_t)c * N + v] = (float)(a.epsp[(size_t)c * N + v] - a.dg64[(size_t)c * N + v]);
+            a.ddg32[(size_t)c * N + v] = 0.0f;
+        }
+#pragma unroll
+        for (int c = 6; c < 9; c++) a.ddg32[(size_t)c * N + v] = 0.0f;
+    }
+    if (!P.crystal) return;
+    double R[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) R[i][j] = a.tranmat[(size_t)(3 * i + j) * N + v];
+    for (int s = 0; s < P.n_sys; s++) {
+        double x5[6] = {P.schm_xt[s][0], P.schm_xt[s][1], P.schm_xt[s][2], P.schm_xt[s][3],
+                        P.schm_xt[s][4], 0.0};
+        double t[3][3], u[3][3], w[3][3];
+        b6_to_sym<double>(x5, t);
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = 0; j < 3; j++) u[i][j] = R[i][0] * t[0][j] + R[i][1] * t[1][j] + R[i][2] * t[2][j];
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = 0; j < 3; j++) w[i][j] = u[i][0] * R[j][0] + u[i][1] * R[j][1] + u[i][2] * R[j][2];
+        double o6[6];
+        sym_to_b6<double>(w, o6);
+#pragma unroll
+        for (int q = 0; q < 5; q++) {
+            a.schm64[(size_t)(s * 5 + q) * N + v] = o6[q];
+            if (a.schm32) a.schm32[(size_t)(s * 5 + q) * N + v] = (float)o6[q];
+        }
+    }
+    double rs[NS];
+#pragma unroll
+    for (int i = 0; i < NS; i++) rs[i] = (i < P.n_sys) ? a.rho_s[(size_t)i * N + v] : 0.0;
+    for (int i = 0; i < P.n_sys; i++) {
+        double rP = 0.0, rf = 0.0;
+#pragma unroll
+        for (int j = 0; j < NS; j++) {
+            rP += P.chi[i][j] * rs[j];
+            rf += P.chi1[i][j] * rs[j];
+        }
+        const double rm_stale = a.rho_m[(size_t)i * N + v];
+        const double rm = P.k_rhom[i] * sqrt(rP * rf);
+        const double tp = P.k_tpass[i] * sqrt(fabs(rP + rm)) + a.drx;
+        const double tps = P.k_tpass[i] * sqrt(fabs(rP + rm_stale)) + a.drx;
+        const double itc = 1.0 / (P.tau0 + P.k_tcut[i] * sqrt(rf));
+        const double go = P.k_gamo[i] * rm / sqrt(rf);
+        const double f4[4] = {tp, itc, go, tps};
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            a.fc64[(size_t)(12 * q + i) * N + v] = f4[q];
+            if (a.fc32) a.fc32[(size_t)(12 * q + i) * N + v] = (float)f4[q];
+        }
+    }
+}
+
+// FP32 bulk: fold the FP32 displacement-gradient increment into the FP64
+// field and seed the FP64 refinement with the FP32 stress.
+struct FoldArgs {
+    Grid g;
+    double* dg64;
+    const float* ddg32;
+    double* sig64;
+    const float* sig32;
+};
+
+__global__ void k_fold(const __grid_constant__ FoldArgs a) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    const int N = a.g.N;
+    if (v >= N) return;
+#pragma unroll
+    for (int c = 0; c < 9; c++) a.dg64[(size_t)c * N + v] += (double)a.ddg32[(size_t)c * N + v];
+#pragma unroll
+    for (int c = 0; c < 6; c++) a.sig64[(size_t)c * N + v] = (double)a.sig32[(size_t)c * N + v];
+}
+
+// ------------------------------------------------------ increment tail
+
+struct EndArgs {
+    Material<double> mat;
+    Grid g;
+    double udot_a[3][3];
+    int reorient;
+    double* dg_old;       // in: DisGrad at increment start; out: VelGrad
+    const double* dg64;
+    double* epsp;
+    const double* edot;
+    double* tranmat;
+    double* rho_s;
+    double* rho_m;
+    const double* gamdot;
+    double* gam_acum;
+    const double* sig64;
+    const double* schm64;
+    const int32_t* phase;
+    float* sig32;         // FP32 bulk: next increment starts from the refined stress
+    double* part;
+};
+
+// Orientation (constitutive.c:142-194): Rodrigues-type update of R by the
+// rotation increment rot (the reference drops rotations below 1e-6 by
+// rescaling with tan(|w|/2) before resetting |w| to 1).
+__device__ void reorient(double tran[3][3], const double rot[3][3]) {
+    double w[3] = {rot[2][1], rot[0][2], rot[1][0]};
+    double wn = sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+    double wt = tan(wn / 2.0);
+    if (fabs(wn) < 1E-6) wn = 1.0;
+    for (int i = 0; i < 3; i++) w[i] *= wt / wn;
+    const double om[3][3] = {{0., -w[2], w[1]}, {w[2], 0., -w[0]}, {-w[1], w[0], 0.}};
+    double om2[3][3], r[3][3], tn[3][3];
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) om2[i][j] = om[i][0] * om[0][j] + om[i][1] * om[1][j] + om[i][2] * om[2][j];
+    wt = wt * wt;
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) r[i][j] = (double)(i == j) + 2. * (om[i][j] + om2[i][j]) / (1. + wt);
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) tn[i][j] = r[i][0] * tran[0][j] + r[i][1] * tran[1][j] + r[i][2] * tran[2][j];
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) tran[i][j] = tn[i][j];
+}
+
+__global__ void __launch_bounds__(END_BLOCK) k_end(const __grid_constant__ EndArgs a) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    const int N = a.g.N;
+    const double dt = a.mat.dt;
+    double q[NPART_END];
+#pragma unroll
+    for (int i = 0; i < NPART_END; i++) q[i] = 0.0;
+    if (v < N) {
+        // VelGrad = (DisGrad - DisGrad_old)/dt (evolution.c:1268-1272)
+        double vg[9];
+#pragma unroll
+        for (int c = 0; c < 9; c++) {
+            vg[c] = (a.dg64[(size_t)c * N + v] - a.dg_old[(size_t)c * N + v]) / dt;
+            a.dg_old[(size_t)c * N + v] = vg[c];
+        }
+        // Eps += Edot dt (evolution.c:1297-1301)
+        double ep[6], ed[5];
+#pragma unroll
+        for (int c = 0; c < 5; c++) ed[c] = a.edot[(size_t)c * N + v];
+#pragma unroll
+        for (int c = 0; c < 6; c++) {
+            ep[c] = a.epsp[(size_t)c * N + v] + (c < 5 ? ed[c] * dt : 0.0);
+            a.epsp[(size_t)c * N + v] = ep[c];
+            q[7 + c] = ep[c];
+        }
+#pragma unroll
+        for (int c = 0; c < 5; c++) q[13 + c] = ed[c];
+        if (a.sig32)
+#pragma unroll
+            for (int c = 0; c < 6; c++) a.sig32[(size_t)c * N + v] = (float)a.sig64[(size_t)c * N + v];
+        const int ph = a.phase[v];
+        const PhaseK<double>& P = a.mat.ph[ph - 1];
+        if (P.crystal) {
+            double gd[NS];
+#pragma unroll
+            for (int i = 0; i < NS; i++) gd[i] = (i < P.n_sys) ? a.gamdot[(size_t)i * N + v] : 0.0;
+            if (a.reorient) {
+                // update_orient (constitutive.c:196-273)
+                double tr[3][3], Lp[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, rot[3][3];
+                for (int i = 0; i < 3; i++)
+                    for (int j = 0; j < 3; j++) tr[i][j] = a.tranmat[(size_t)(3 * i + j) * N + v];
+                for (int s = 0; s < P.n_sys; s++) {
+                    double bs[3], ns[3];
+                    for (int i = 0; i < 3; i++) {
+                        bs[i] = tr[i][0] * P.bb[s][0] + tr[i][1] * P.bb[s][1] + tr[i][2] * P.bb[s][2];
+                        ns[i] = tr[i][0] * P.bn[s][0] + tr[i][1] * P.bn[s][1] + tr[i][2] * P.bn[s][2];
+                    }
+                    for (int i = 0; i < 3; i++)
+                        for (int j = 0; j < 3; j++) Lp[i][j] += bs[i] * ns[j] * gd[s];
+                }
+                // antisymmetric VelGrad: A12 = vg[6], A13 = vg[7], A23 = vg[8]
+                const double rl[3][3] = {{0.0, vg[6], vg[7]}, {-vg[6], 0.0, vg[8]}, {-vg[7], -vg[8], 0.0}};
+                for (int i = 0; i < 3; i++)
+                    for (int j = 0; j < 3; j++)
+                        rot[i][j] = (a.udot_a[i][j] + rl[i][j] - (Lp[i][j] - Lp[j][i]) / 2.) * dt;
+                reorient(tr, rot);
+                for (int i = 0; i < 3; i++)
+                    for (int j = 0; j < 3; j++) a.tranmat[(size_t)(3 * i + j) * N + v] = tr[i][j];
+            }
+            // DislocationEvolution (constitutive.c:1373-1426), with rho_F and
+            // rho_m of the increment's flow-rule calls and the stored rho_m
+            // (the value before this increment) in rho_tot.
+            double rs[NS], rf[NS], rP[NS], rm[NS], rtot = 0.0;
+#pragma unroll
+            for (int i = 0; i < NS; i++) rs[i] = (i < P.n_sys) ? a.rho_s[(size_t)i * N + v] : 0.0;
+            for (int i = 0; i < P.n_sys; i++) {
+                double x = 0.0, y = 0.0;
+#pragma unroll
+                for (int j = 0; j < NS; j++) {
+                    x += P.chi[i][j] * rs[j];
+                    y += P.chi1[i][j] * rs[j];
+                }
+                rP[i] = x;
+                rf[i] = y;
+                rm[i] = P.k_rhom[i] * sqrt(x * y);
+                rtot += rs[i] + a.rho_m[(size_t)i * N + v];
+            }
+            double s6[6];
+#pragma unroll
+            for (int c = 0; c < 6; c++) s6[c] = a.sig64[(size_t)c * N + v];
+            const double G = P.shear_g, nu = a.mat.nu, T = a.mat.temperature, D0 = a.mat.d0;
+            const double eqb = exp(-1.0 * P.q_bulk);
+            for (int i = 0; i < P.n_sys; i++) {
+                const double* sc = a.schm64 + (size_t)(i * 5) * N + v;
+                const double rss = sc[0] * s6[0] + sc[(size_t)N] * s6[1] + sc[2 * (size_t)N] * s6[2] +
+                                   sc[3 * (size_t)N] * s6[3] + sc[4 * (size_t)N] * s6[4];
+                const double b = P.burgers[i];
+                const double ddip = sqrt(3.0) * G * b / 16.0 / 3.14159265359 / (1 - nu) / (fabs(rss) + 1.0E-4);
+                const double hyd = G * b / 3.14159265359 / (1 - nu) / ddip;
+                const double clim = 1E-17 * rtot * 0.5 * 1E24 * ddip * (D0 / b) * (rs[i] * rs[i]) *
+                                    (exp(fabs(hyd) * b * b * b * 100 / (1.38 * T)) - 1.0) * eqb;
+                const double ag = fabs(gd[i]);
+                const double sq = sqrt(rf[i]);
+                q[4] += clim * dt;
+                q[5] += ag * (P.c4 * sq) * dt;
+                q[6] += ag * (P.c5 * rs[i]) * dt;
+                const double dot = ag * (P.c4 * sq + P.c6 * ddip * rm[i] - P.c5 * rs[i]) - clim;
+                const double rn = rs[i] + dot * dt;
+                a.rho_s[(size_t)i * N + v] = rn;
+                a.rho_m[(size_t)i * N + v] = rm[i];
+                a.gam_acum[(size_t)i * N + v] += gd[i] * dt;
+                q[0] += rf[i];
+                q[1] += rP[i];
+                q[2] += rn;
+                q[3] += rm[i];
+            }
+        }
+    }
+    block_reduce_store<NPART_END>(q, a.part + (size_t)blockIdx.x * NPART_END);
+}
+
+struct EndReduceArgs {
+    Macro* macro;
+    const double* part;
+    int nblocks;
+    double wgt;
+};
+
+// AvgDislocation (constitutive.c:1681-1808) and <Eps>, <Edot>
+// (evolution.c:1307-1323), in the B basis.
+__global__ void __launch_bounds__(256) k_end_reduce(const __grid_constant__ EndReduceArgs a) {
+    double v[NPART_END];
+#pragma unroll
+    for (int q = 0; q < NPART_END; q++) v[q] = 0.0;
+    for (int b = threadIdx.x; b < a.nblocks; b += blockDim.x)
+#pragma unroll
+        for (int q = 0; q < NPART_END; q++) v[q] += a.part[(size_t)b * NPART_END + q];
+    __shared__ double tot[NPART_END];
+    double o[NPART_END];
+    block_reduce_store<NPART_END>(v, o);
+    if (threadIdx.x < NPART_END) tot[threadIdx.x] = o[threadIdx.x];
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    Macro* m = a.macro;
+    m->rho_dip_acc += tot[4];
+    m->rho_for_acc += tot[5];
+    m->rho_inp_acc += tot[6];
+    m->rho_avg[0] = tot[0] * a.wgt;
+    m->rho_avg[1] = tot[1] * a.wgt;
+    m->rho_avg[2] = tot[2] * a.wgt;
+    m->rho_avg[3] = tot[3] * a.wgt;
+    m->rho_avg[4] = 0.0;
+    m->rho_avg[5] = m->rho_dip_acc * a.wgt;
+    m->rho_avg[6] = m->rho_for_acc * a.wgt;
+    m->rho_avg[7] = m->rho_inp_acc * a.wgt;
+    for (int c = 0; c < 6; c++) m->eps_avg6[c] = tot[7 + c] * a.wgt;
+    for (int c = 0; c < 5; c++) m->edot_avg6[c] = tot[13 + c] * a.wgt;
+    m->edot_avg6[5] = 0.0;
+}
+
+// ------------------------------------------------------------- launchers
+
+template <typename T>
+static cudaError_t nr_t(Ctx& c, const Material<T>& mat, T* sig, const T* dg, const T* epsb,
+                        const T* schm, const T* fc, const T* sgr, T* edot, T* gamdot, T tol,
+                        int stale_mode, int check_done) {
+    NrArgs<T> a;
+    a.mat = mat;
+    a.g = c.g;
+    a.sig = sig; a.dg = dg; a.epsb = epsb; a.schm = schm; a.fc = fc;
+    a.orient = c.orient; a.phase = c.phase; a.sgr = sgr; a.edot = edot; a.gamdot = gamdot;
+    a.macro = c.macro; a.part = c.part_nr; a.tol = tol; a.itmax = c.nr_itmax;
+    a.nr_mode = c.nr_mode; a.stale_mode = stale_mode; a.check_done = check_done;
+    const int grp = check_done ? PG_NR : PG_REFINE;
+    prof_mark(c, grp, true);
+    k_nr<T><<<c.nb_nr, NR_BLOCK, 0, c.stream>>>(a);
+    prof_mark(c, grp, false);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_nr(Ctx& c, int refine) {
+    if (c.precision == 0)
+        return nr_t<double>(c, c.m64, c.sig64, c.dg64, c.epsp, c.schm64, c.fc64, c.sgr64, c.edot64,
+                            c.gamdot64, (double)c.nr_tol64, 1, 1);
+    if (refine)
+        return nr_t<double>(c, c.m64, c.sig64, c.dg64, c.epsp, c.schm64, c.fc64, c.sgr64, c.edot64,
+                            c.gamdot64, (double)c.nr_tol64, 0, 0);
+    return nr_t<float>(c, c.m32, c.sig32, c.ddg32, c.b6_32, c.schm32, c.fc32, c.sgr32, nullptr,
+                       nullptr, (float)c.nr_tol32, 1, 1);
+}
+
+cudaError_t launch_macro(Ctx& c) {
+    MacroArgs a;
+    a.cfg = c.cfg;
+    a.macro = c.macro;
+    a.part = c.part_nr;
+    a.nblocks = c.nb_nr;
+    prof_mark(c, PG_MACRO, true);
+    k_macro<<<1, 256, 0, c.stream>>>(a);
+    prof_mark(c, PG_MACRO, false);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_begin(Ctx& c, const double udot9[9], int creep, const double dgavg9[9],
+                         double drx) {
+    BeginArgs a;
+    a.mat = c.m64;
+    a.g = c.g;
+    for (int i = 0; i < 9; i++) {
+        a.udot9[i] = udot9[i];
+        a.dgavg9[i] = dgavg9[i];
+    }
+    a.creep = creep; a.drx = drx;
+    a.dg64 = c.dg64; a.dg_old = c.dg_old; a.tranmat = c.tranmat; a.rho_s = c.rho_s;
+    a.rho_m = c.rho_m; a.phase = c.phase; a.schm64 = c.schm64; a.fc64 = c.fc64;
+    a.schm32 = c.schm32; a.fc32 = c.fc32; a.b6_32 = c.b6_32; a.ddg32 = c.ddg32; a.epsp = c.epsp;
+    prof_mark(c, PG_BEGIN, true);
+    k_begin<<<(c.g.N + 127) / 128, 128, 0, c.stream>>>(a);
+    prof_mark(c, PG_BEGIN, false);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fold(Ctx& c) {
+    FoldArgs a;
+    a.g = c.g; a.dg64 = c.dg64; a.ddg32 = c.ddg32; a.sig64 = c.sig64; a.sig32 = c.sig32;
+    c.launches++;
+    k_fold<<<(c.g.N + 255) / 256, 256, 0, c.stream>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_end(Ctx& c, int reorient) {
+    EndArgs a;
+    a.mat = c.m64;
+    a.g = c.g;
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) a.udot_a[i][j] = c.udot_a[i][j];
+    a.reorient = reorient;
+    a.dg_old = c.dg_old; a.dg64 = c.dg64; a.epsp = c.epsp; a.edot = c.edot64;
+    a.tranmat = c.tranmat; a.rho_s = c.rho_s; a.rho_m = c.rho_m; a.gamdot = c.gamdot64;
+    a.gam_acum = c.gam_acum; a.sig64 = c.sig64; a.schm64 = c.schm64; a.phase = c.phase;
+    a.sig32 = c.sig32; a.part = c.part_end;
+    prof_mark(c, PG_END, true);
+    k_end<<<c.nb_end, END_BLOCK, 0, c.stream>>>(a);
+    prof_mark(c, PG_END, false);
+    EndReduceArgs r;
+    r.macro = c.macro; r.part = c.part_end; r.nblocks = c.nb_end; r.wgt = c.cfg.wgt;
+    c.launches++;
+    k_end_reduce<<<1, 256, 0, c.stream>>>(r);
+    return cudaGetLastError();
+}
+
+}  // namespace evpg

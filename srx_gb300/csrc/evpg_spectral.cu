@@ -1,0 +1,298 @@
+// Spectral-chain kernels (see evpg_spectral.cuh) and their launcher.
+#include "evpg_ctx.h"
+#include "evpg_spectral.cuh"
+
+namespace evpg {
+
+template <typename T> struct GreenK {
+    T c0[3][3][3][3];
+    T s0[3][3][3][3];
+    int elast_bc;
+};
+
+template <typename T> struct ZArgs {
+    Grid g;
+    FftPlan pl;
+    const int* done;
+    const T* sig;        // [6][N] real
+    T* dg;               // [9][N] real (inverse pass)
+    C2<T>* spec;         // [9][Nh]
+    const C2<T>* tw;
+    const double* dE9;   // macro correction added in the inverse pass
+    int P;
+    T invN;
+};
+
+template <typename T> struct YArgs {
+    Grid g;
+    FftPlan pl;
+    const int* done;
+    C2<T>* spec;
+    const C2<T>* tw;
+    int ncomp, P;
+};
+
+template <typename T> struct XArgs {
+    Grid g;
+    FftPlan pl;
+    const int* done;
+    C2<T>* spec;
+    const C2<T>* tw;
+    int P;
+    GreenK<T> gk;
+};
+
+template <typename T>
+__device__ __forceinline__ void load_tw(C2<T>* tw, const C2<T>* src, int n) {
+    for (int i = threadIdx.x; i < n; i += blockDim.x) tw[i] = src[i];
+}
+
+// Forward z: three complex FFTs of (sig[2p] + i sig[2p+1]) per column, split
+// into the two half spectra.
+template <typename T>
+__global__ void __launch_bounds__(256) k_fwd_z(const __grid_constant__ ZArgs<T> a) {
+    if (*a.done) return;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const Grid& g = a.g;
+    const int n = g.n2, nh = g.nh, P = a.P;
+    C2<T>* tw = reinterpret_cast<C2<T>*>(smem);
+    C2<T>* bA = tw + n;
+    C2<T>* bB = bA + P * n;
+    const int ncol = g.n0 * g.n1, c0 = blockIdx.x * P, np = min(P, ncol - c0);
+    load_tw<T>(tw, a.tw, n);
+    for (int pair = 0; pair < 3; pair++) {
+        const T* sa = a.sig + (size_t)(2 * pair) * g.N + (size_t)c0 * n;
+        const T* sb = a.sig + (size_t)(2 * pair + 1) * g.N + (size_t)c0 * n;
+        for (int i = threadIdx.x; i < np * n; i += blockDim.x) bA[i] = mk<T>(sa[i], sb[i]);
+        __syncthreads();
+        const C2<T>* r = fft_batch<T, -1>(bA, bB, np, n, a.pl, tw);
+        C2<T>* oa = a.spec + (size_t)(2 * pair) * g.Nh + (size_t)c0 * nh;
+        C2<T>* ob = a.spec + (size_t)(2 * pair + 1) * g.Nh + (size_t)c0 * nh;
+        for (int i = threadIdx.x; i < np * nh; i += blockDim.x) {
+            const int col = i / nh, k = i - col * nh;
+            const C2<T> z = r[col * n + k];
+            const C2<T> w = r[col * n + (k == 0 ? 0 : n - k)];
+            // A = (Z(k) + conj Z(n-k))/2, B = (Z(k) - conj Z(n-k))/(2i)
+            oa[i] = mk<T>((T)0.5 * (z.x + w.x), (T)0.5 * (z.y - w.y));
+            ob[i] = mk<T>((T)0.5 * (z.y + w.y), (T)-0.5 * (z.x - w.x));
+        }
+        __syncthreads();
+    }
+}
+
+// c2c along y on ncomp planes, pencils (x, kz..kz+P).
+template <typename T, int SIGN>
+__global__ void __launch_bounds__(256) k_y(const __grid_constant__ YArgs<T> a) {
+    if (*a.done) return;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const Grid& g = a.g;
+    const int n = g.n1, ps = n + 1, P = a.P, nh = g.nh;
+    C2<T>* tw = reinterpret_cast<C2<T>*>(smem);
+    C2<T>* bA = tw + n;
+    C2<T>* bB = bA + P * ps;
+    const int ntile = (nh + P - 1) / P;
+    const int x = blockIdx.x / ntile, kz0 = (blockIdx.x % ntile) * P, np = min(P, nh - kz0);
+    load_tw<T>(tw, a.tw, n);
+    for (int c = 0; c < a.ncomp; c++) {
+        C2<T>* base = a.spec + (size_t)c * g.Nh + (size_t)x * n * nh + kz0;
+        for (int i = threadIdx.x; i < n * np; i += blockDim.x) {
+            const int y = i / np, kk = i - y * np;
+            bA[kk * ps + y] = base[(size_t)y * nh + kk];
+        }
+        __syncthreads();
+        const C2<T>* r = fft_batch<T, SIGN>(bA, bB, np, ps, a.pl, tw);
+        for (int i = threadIdx.x; i < n * np; i += blockDim.x) {
+            const int y = i / np, kk = i - y * np;
+            base[(size_t)y * nh + kk] = r[kk * ps + y];
+        }
+        __syncthreads();
+    }
+}
+
+// Forward x, Green contraction, inverse x on pencils (y, kz..kz+P).
+template <typename T>
+__global__ void __launch_bounds__(256) k_x_green(const __grid_constant__ XArgs<T> a) {
+    if (*a.done) return;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const Grid& g = a.g;
+    const int n = g.n0, ps = n + 1, P = a.P, nh = g.nh;
+    C2<T>* tw = reinterpret_cast<C2<T>*>(smem);
+    C2<T>* bA = tw + n;
+    C2<T>* bB = bA + 9 * P * ps;
+    const int ntile = (nh + P - 1) / P;
+    const int y = blockIdx.x / ntile, kz0 = (blockIdx.x % ntile) * P, np = min(P, nh - kz0);
+    const size_t xs = (size_t)g.n1 * nh;
+    load_tw<T>(tw, a.tw, n);
+    for (int i = threadIdx.x; i < 6 * n * np; i += blockDim.x) {
+        const int c = i / (n * np), rem = i - c * n * np, x = rem / np, kk = rem - x * np;
+        bA[(c * np + kk) * ps + x] = a.spec[(size_t)c * g.Nh + x * xs + (size_t)y * nh + kz0 + kk];
+    }
+    __syncthreads();
+    C2<T>* R = fft_batch<T, -1>(bA, bB, 6 * np, ps, a.pl, tw);
+    C2<T>* W = (R == bA) ? bB : bA;
+    for (int i = threadIdx.x; i < n * np; i += blockDim.x) {
+        const int kk = i / n, kx = i - kk * n, kz = kz0 + kk, ky = y;
+        C2<T> sb[6], du[9];
+#pragma unroll
+        for (int c = 0; c < 6; c++) sb[c] = R[(c * np + kk) * ps + kx];
+        if ((kx | ky | kz) == 0) {
+            green_k0<T>(a.gk.s0, a.gk.elast_bc, sb, du);
+        } else {
+            T nv[3];
+            kvec<T>(kx, ky, kz, g, nv);
+            green_du<T>(a.gk.c0, nv, sb, du);
+            const bool nyq = ((g.n0 & 1) == 0 && 2 * kx == g.n0) ||
+                             ((g.n1 & 1) == 0 && 2 * ky == g.n1) ||
+                             ((g.n2 & 1) == 0 && 2 * kz == g.n2);
+            if (nyq) {
+                // Hermitian part: (du(k) + conj du(-k))/2 with sig_hat(-k) = conj sig_hat(k)
+                C2<T> sm[6], dm[9];
+#pragma unroll
+                for (int c = 0; c < 6; c++) sm[c] = cconj<T>(sb[c]);
+                const int mx = (g.n0 - kx) % g.n0, my = (g.n1 - ky) % g.n1, mz = (g.n2 - kz) % g.n2;
+                kvec<T>(mx, my, mz, g, nv);
+                green_du<T>(a.gk.c0, nv, sm, dm);
+#pragma unroll
+                for (int c = 0; c < 9; c++)
+                    du[c] = mk<T>((T)0.5 * (du[c].x + dm[c].x), (T)0.5 * (du[c].y - dm[c].y));
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < 9; c++) W[(c * np + kk) * ps + kx] = du[c];
+    }
+    __syncthreads();
+    const C2<T>* R2 = fft_batch<T, 1>(W, (W == bA) ? bB : bA, 9 * np, ps, a.pl, tw);
+    for (int i = threadIdx.x; i < 9 * n * np; i += blockDim.x) {
+        const int c = i / (n * np), rem = i - c * n * np, x = rem / np, kk = rem - x * np;
+        a.spec[(size_t)c * g.Nh + x * xs + (size_t)y * nh + kz0 + kk] = R2[(c * np + kk) * ps + x];
+    }
+}
+
+// Inverse z: pairs of Hermitian half spectra -> one complex IFFT -> two real
+// fields; DisGrad += dE + re/N (evolution.c:1197).
+template <typename T>
+__global__ void __launch_bounds__(256) k_inv_z(const __grid_constant__ ZArgs<T> a) {
+    if (*a.done) return;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const Grid& g = a.g;
+    const int n = g.n2, nh = g.nh, P = a.P;
+    C2<T>* tw = reinterpret_cast<C2<T>*>(smem);
+    C2<T>* bA = tw + n;
+    C2<T>* bB = bA + P * n;
+    const int ncol = g.n0 * g.n1, c0 = blockIdx.x * P, np = min(P, ncol - c0);
+    load_tw<T>(tw, a.tw, n);
+    for (int pair = 0; pair < 5; pair++) {
+        const int ca = 2 * pair, cb = 2 * pair + 1;
+        const bool hasb = cb < 9;
+        const C2<T>* sa = a.spec + (size_t)ca * g.Nh + (size_t)c0 * nh;
+        const C2<T>* sb = a.spec + (size_t)(hasb ? cb : ca) * g.Nh + (size_t)c0 * nh;
+        for (int i = threadIdx.x; i < np * n; i += blockDim.x) {
+            const int col = i / n, k = i - col * n;
+            C2<T> z;
+            if (k < nh) {
+                const C2<T> u = sa[col * nh + k];
+                const C2<T> v = hasb ? sb[col * nh + k] : mk<T>((T)0, (T)0);
+                z = mk<T>(u.x - v.y, u.y + v.x);  // u + i v
+            } else {
+                const C2<T> u = sa[col * nh + (n - k)];
+                const C2<T> v = hasb ? sb[col * nh + (n - k)] : mk<T>((T)0, (T)0);
+                z = mk<T>(u.x + v.y, -u.y + v.x);  // conj u + i conj v
+            }
+            bA[i] = z;
+        }
+        __syncthreads();
+        const C2<T>* r = fft_batch<T, 1>(bA, bB, np, n, a.pl, tw);
+        const T ea = (T)a.dE9[ca], eb = hasb ? (T)a.dE9[cb] : (T)0;
+        T* da = a.dg + (size_t)ca * g.N + (size_t)c0 * n;
+        T* db = a.dg + (size_t)(hasb ? cb : ca) * g.N + (size_t)c0 * n;
+        for (int i = threadIdx.x; i < np * n; i += blockDim.x) {
+            const C2<T> z = r[i];
+            da[i] += ea + z.x * a.invN;
+            if (hasb) db[i] += eb + z.y * a.invN;
+        }
+        __syncthreads();
+    }
+}
+
+template <typename T> static int pick_p(int n, int per_pencil_elems, size_t elem, size_t budget) {
+    const size_t per = (size_t)per_pencil_elems * elem;
+    int p = (int)(budget / per);
+    if (p < 1) p = 1;
+    if (p > 64) p = 64;
+    (void)n;
+    return p;
+}
+
+template <typename T>
+static cudaError_t spectral_t(Ctx& c, T* sig, T* dg, const C2<T>* const* tw) {
+    const Grid& g = c.g;
+    C2<T>* spec = reinterpret_cast<C2<T>*>(c.spec);
+    const int* done = macro_field<int>(c.macro, offsetof(Macro, done));
+    const size_t es = sizeof(C2<T>);
+    const size_t budget = 72 * 1024;
+    cudaError_t e;
+    // z passes
+    {
+        ZArgs<T> za;
+        za.g = g; za.pl = c.pl[2]; za.done = done; za.sig = sig; za.dg = dg; za.spec = spec;
+        za.tw = tw[2]; za.dE9 = macro_field<double>(c.macro, offsetof(Macro, dE9)); za.invN = (T)(1.0 / (double)g.N);
+        za.P = pick_p<T>(g.n2, 2 * g.n2, es, budget);
+        const int ncol = g.n0 * g.n1;
+        const size_t sm = (size_t)(g.n2 + 2 * za.P * g.n2) * es;
+        cudaFuncSetAttribute(k_fwd_z<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        cudaFuncSetAttribute(k_inv_z<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        prof_mark(c, PG_FWD_Z, true);
+        k_fwd_z<T><<<(ncol + za.P - 1) / za.P, 256, sm, c.stream>>>(za);
+        prof_mark(c, PG_FWD_Z, false);
+        // y forward
+        YArgs<T> ya;
+        ya.g = g; ya.pl = c.pl[1]; ya.done = done; ya.spec = spec; ya.tw = tw[1]; ya.ncomp = 6;
+        ya.P = pick_p<T>(g.n1, 2 * (g.n1 + 1), es, budget);
+        if (ya.P > g.nh) ya.P = g.nh;
+        const size_t smy = (size_t)(g.n1 + 2 * ya.P * (g.n1 + 1)) * es;
+        cudaFuncSetAttribute(k_y<T, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smy);
+        cudaFuncSetAttribute(k_y<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smy);
+        const int ntile_y = (g.nh + ya.P - 1) / ya.P;
+        prof_mark(c, PG_FWD_Y, true);
+        k_y<T, -1><<<g.n0 * ntile_y, 256, smy, c.stream>>>(ya);
+        prof_mark(c, PG_FWD_Y, false);
+        // x + Green
+        XArgs<T> xa;
+        xa.g = g; xa.pl = c.pl[0]; xa.done = done; xa.spec = spec; xa.tw = tw[0];
+        xa.P = pick_p<T>(g.n0, 18 * (g.n0 + 1), es, 150 * 1024);
+        if (xa.P > g.nh) xa.P = g.nh;
+        const Material<T>& m = material_of<T>(c);
+        for (int i = 0; i < 81; i++) {
+            (&xa.gk.c0[0][0][0][0])[i] = (&m.c0[0][0][0][0])[i];
+            (&xa.gk.s0[0][0][0][0])[i] = (&m.s0[0][0][0][0])[i];
+        }
+        xa.gk.elast_bc = m.elast_bc;
+        const size_t smx = (size_t)(g.n0 + 18 * xa.P * (g.n0 + 1)) * es;
+        cudaFuncSetAttribute(k_x_green<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smx);
+        const int ntile_x = (g.nh + xa.P - 1) / xa.P;
+        prof_mark(c, PG_X_GREEN, true);
+        k_x_green<T><<<g.n1 * ntile_x, 256, smx, c.stream>>>(xa);
+        prof_mark(c, PG_X_GREEN, false);
+        // y inverse
+        ya.ncomp = 9;
+        prof_mark(c, PG_INV_Y, true);
+        k_y<T, 1><<<g.n0 * ntile_y, 256, smy, c.stream>>>(ya);
+        prof_mark(c, PG_INV_Y, false);
+        prof_mark(c, PG_INV_Z, true);
+        k_inv_z<T><<<(ncol + za.P - 1) / za.P, 256, sm, c.stream>>>(za);
+        prof_mark(c, PG_INV_Z, false);
+    }
+    e = cudaGetLastError();
+    return e;
+}
+
+cudaError_t launch_spectral(Ctx& c) {
+    if (c.precision == 0) {
+        const double2* tw[3] = {c.tw64[0], c.tw64[1], c.tw64[2]};
+        return spectral_t<double>(c, c.sig64, c.dg64, tw);
+    }
+    const float2* tw[3] = {c.tw32[0], c.tw32[1], c.tw32[2]};
+    return spectral_t<float>(c, c.sig32, c.ddg32, tw);
+}
+
+}  // namespace evpg

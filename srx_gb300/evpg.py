@@ -1,0 +1,155 @@
+"""ctypes binding of the C ABI in ``include/evpg.h``.
+
+The CUDA library ``srx_gb300/_lib/libevpg.so`` is the only compute path;
+importing this module fails when it is missing (call
+``srx_gb300.build.build()`` first). There is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Optional
+
+import numpy as np
+
+from . import build as _build
+
+EVPG_OK = 0
+FP64, FP32_BULK = 0, 1
+NR_PLAIN, NR_LINESEARCH = 0, 1
+F_SIG, F_DISGRAD, F_EPS, F_EDOT, F_TRANMAT = 0, 1, 2, 3, 4
+F_RHO_S, F_RHO_M, F_GAMDOT, F_GAM_ACUM, F_VELGRAD, F_SIG6 = 5, 6, 7, 8, 9, 10
+FIELD_WIDTH = {F_SIG: 9, F_DISGRAD: 9, F_EPS: 9, F_EDOT: 9, F_TRANMAT: 9, F_RHO_S: 12,
+               F_RHO_M: 12, F_GAMDOT: 12, F_GAM_ACUM: 12, F_VELGRAD: 9, F_SIG6: 6}
+
+
+class EvpgError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__("evpg status %d: %s" % (status, msg))
+        self.status = status
+
+
+class IterOut(C.Structure):
+    _fields_ = [("err_e", C.c_double), ("err_s", C.c_double), ("err_e_sum", C.c_double),
+                ("err_s_sum", C.c_double), ("sig_avg", C.c_double * 9),
+                ("sig_avg_ph1", C.c_double * 9), ("ddisgrad", C.c_double * 9),
+                ("ddisgrad_acum", C.c_double * 9), ("s_vm", C.c_double), ("s_vm1", C.c_double),
+                ("iter", C.c_int32), ("converged", C.c_int32)]
+
+
+class IncrOut(C.Structure):
+    _fields_ = [("eps_avg", C.c_double * 9), ("edot_avg", C.c_double * 9),
+                ("rho_avg", C.c_double * 8), ("nr_iterations", C.c_int64)]
+
+
+_LIB = None
+
+
+def lib() -> C.CDLL:
+    """The loaded CUDA library (RuntimeError when it has not been built)."""
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(_build.LIB):
+            raise RuntimeError("libevpg.so is not built: run srx_gb300.build.build() (nvcc, sm_103a)")
+        L = C.CDLL(_build.LIB)
+        vp, i32, d, sz = C.c_void_p, C.c_int32, C.c_double, C.c_size_t
+        L.evpg_version.restype = C.c_char_p
+        L.evpg_last_error.restype = C.c_char_p
+        L.evpg_status_string.restype = C.c_char_p
+        L.evpg_status_string.argtypes = [C.c_int]
+        L.evpg_job_open.argtypes = [C.c_char_p, C.c_char_p, i32, i32, C.POINTER(vp)]
+        L.evpg_job_close.argtypes = [vp]
+        L.evpg_job_ctx.argtypes = [vp]
+        L.evpg_job_ctx.restype = vp
+        L.evpg_job_nvox.argtypes = [vp, C.POINTER(i32)]
+        L.evpg_job_nsteps.argtypes = [vp]
+        L.evpg_job_increment.argtypes = [vp, i32, C.POINTER(i32)]
+        L.evpg_job_scalars.argtypes = [vp, C.POINTER(d), i32]
+        L.evpg_job_run.argtypes = [vp, C.c_char_p, i32, i32]
+        L.evpg_download.argtypes = [vp, i32, C.POINTER(d), sz]
+        L.evpg_upload.argtypes = [vp, i32, C.POINTER(d), sz]
+        L.evpg_equilibrium_iteration.argtypes = [vp, d, C.POINTER(IterOut)]
+        L.evpg_equilibrium_solve.argtypes = [vp, d, C.POINTER(IterOut)]
+        L.evpg_increment_begin.argtypes = [vp, C.POINTER(d), i32, C.POINTER(d), d]
+        L.evpg_increment_end.argtypes = [vp, i32, C.POINTER(IncrOut)]
+        L.evpg_synchronize.argtypes = [vp]
+        L.evpg_device_bytes.argtypes = [vp, C.POINTER(C.c_int64)]
+        _LIB = L
+    return _LIB
+
+
+def check(st: int) -> None:
+    if st != EVPG_OK:
+        L = lib()
+        raise EvpgError(st, "%s: %s" % (L.evpg_status_string(st).decode(),
+                                        L.evpg_last_error().decode()))
+
+
+class Job:
+    """A job of the host driver: the reference's input files on the device."""
+
+    def __init__(self, input_path: str, rho0: Optional[str] = None, precision: int = FP64,
+                 nr_mode: int = NR_PLAIN):
+        L = lib()
+        h = C.c_void_p()
+        check(L.evpg_job_open(input_path.encode(), rho0.encode() if rho0 else None,
+                              precision, nr_mode, C.byref(h)))
+        self._h = h
+        n = (C.c_int32 * 3)()
+        check(L.evpg_job_nvox(h, n))
+        self.n = tuple(n)
+        self.N = n[0] * n[1] * n[2]
+        self.precision = precision
+
+    @property
+    def ctx(self) -> C.c_void_p:
+        return C.c_void_p(lib().evpg_job_ctx(self._h))
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().evpg_job_close(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def n_steps(self) -> int:
+        return lib().evpg_job_nsteps(self._h)
+
+    def increment(self, istep: int) -> int:
+        it = C.c_int32()
+        check(lib().evpg_job_increment(self._h, istep, C.byref(it)))
+        return it.value
+
+    def scalars(self) -> np.ndarray:
+        out = (C.c_double * 34)()
+        check(lib().evpg_job_scalars(self._h, out, 34))
+        return np.array(out[:])
+
+    def run(self, outdir: str, nsteps: int = -1, iout: bool = False) -> None:
+        check(lib().evpg_job_run(self._h, outdir.encode(), nsteps, 1 if iout else 0))
+
+    def download(self, field: int) -> np.ndarray:
+        w = FIELD_WIDTH[field]
+        out = np.empty(self.N * w, dtype=np.float64)
+        check(lib().evpg_download(self.ctx, field, out.ctypes.data_as(C.POINTER(C.c_double)),
+                                  out.size))
+        return out.reshape(self.N, w)
+
+    def upload(self, field: int, arr: np.ndarray) -> None:
+        a = np.ascontiguousarray(arr, dtype=np.float64).reshape(-1)
+        check(lib().evpg_upload(self.ctx, field, a.ctypes.data_as(C.POINTER(C.c_double)), a.size))
+
+    def device_bytes(self) -> int:
+        b = C.c_int64()
+        check(lib().evpg_device_bytes(self.ctx, C.byref(b)))
+        return b.value

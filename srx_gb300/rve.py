@@ -88,9 +88,17 @@ class Job:
     print_control: Sequence[int] = (0, 1)
     update_flag: int = 1
     hard_flag: int = 1
+    # explicit load (overrides `load`/`rate`): Voigt flags and values
+    velgrad_flag: Optional[Sequence[int]] = None
+    velgrad: Optional[Sequence[float]] = None
+    stress_flag: Optional[Sequence[int]] = None
+    time_step_override: Optional[float] = None
+    second_phase_gas: bool = False
 
     @property
     def time_step(self) -> float:
+        if self.time_step_override is not None:
+            return self.time_step_override
         return self.strain_per_step / self.rate
 
 
@@ -105,6 +113,15 @@ def voronoi(n: Sequence[int], n_grains: int, seed: int):
         [360.0 * u[:, 0], np.degrees(np.arccos(2.0 * u[:, 1] - 1.0)), 360.0 * u[:, 2]], axis=1
     )
     axes = [(np.arange(k) + 0.5) / k for k in n]
+    if int(np.prod(n)) > 64 ** 3:
+        # large grids: periodic k-d tree; exact distance ties are resolved to
+        # the lower seed index as below
+        from scipy.spatial import cKDTree
+        pts = np.stack(np.meshgrid(*axes, indexing="ij"), axis=-1).reshape(-1, 3)
+        d, i = cKDTree(seeds, boxsize=1.0).query(pts, k=2, workers=-1)
+        tie = d[:, 0] == d[:, 1]
+        best = np.where(tie, np.minimum(i[:, 0], i[:, 1]), i[:, 0])
+        return (best + 1).astype(np.int32).reshape(n), euler
     gid = np.zeros(n, dtype=np.int32)
     best = np.full(n, np.inf)
     cx, cy, cz = np.meshgrid(*axes, indexing="ij")
@@ -158,11 +175,13 @@ def write_namelist(path: str, job: Job, mat: Material, ms_name: str, sx_name: st
     """Namelist in the reference format (key table io.c:25-94)."""
     flag_v, direction, flag_s = LOADS[job.load]
     vel = [d * job.rate for d in direction]
+    if job.velgrad_flag is not None:
+        flag_v, vel, flag_s = job.velgrad_flag, list(job.velgrad), job.stress_flag
     n = [int(x) for x in job.n]
     m = mat
     kv = [
         ("N_phases", "2"), ("CellDim", "%d %d %d" % tuple(n)), ("initial_ms", ms_name),
-        ("Type_phases", "0 0"),
+        ("Type_phases", "0 1" if job.second_phase_gas else "0 0"),
         ("ElastConst_PhaseI", "%r %r %r %r" % (m.c11, m.c12, m.c44, m.nu)),
         ("Slip_PhaseI", sx_name),
         ("ElastConst_PhaseII", "%r %r %r %r" % (m.c11, m.c12, m.c44, m.nu)),
@@ -233,3 +252,51 @@ def make_case(dirpath: str, n: Sequence[int], n_grains: int, seed: int, job: Job
         r.tofile(p)
         out["rho0"] = p
     return out
+
+
+def write_case(dirpath: str, gid: np.ndarray, euler: np.ndarray, job: Job,
+               mat: Optional[Material] = None, phase: Optional[np.ndarray] = None,
+               rho0: Optional[np.ndarray] = None) -> dict:
+    """Case directory for an explicit grain map ``gid`` (1-based [n0,n1,n2]),
+    per-grain Bunge angles ``euler`` in degrees and optional per-voxel phase
+    ids and initial densities."""
+    mat = mat or Material()
+    os.makedirs(dirpath, exist_ok=True)
+    write_microstructure(os.path.join(dirpath, "ms.txt"), gid, np.asarray(euler, float), phase)
+    write_sx(os.path.join(dirpath, "cu.sx"), mat.tau0)
+    job = dataclasses.replace(job, n=tuple(int(x) for x in gid.shape))
+    write_namelist(os.path.join(dirpath, "input"), job, mat, "ms.txt", "cu.sx")
+    out = {"dir": dirpath, "input": os.path.join(dirpath, "input"), "rho0": None}
+    if rho0 is not None:
+        p = os.path.join(dirpath, "rho0.bin")
+        np.asarray(rho0, dtype=np.float64).reshape(-1).tofile(p)
+        out["rho0"] = p
+    return out
+
+
+def bicrystal8_case(dirpath: str, n_steps: int = 5, print_every: int = 1) -> dict:
+    """The reference's own 8^3 regression case, restated: planes i=1..4 with
+    Bunge (0,0,0), planes i=5..8 with (90,35,45), one grain id, phase 1; Cu
+    at c11/c12/c44 = 162700/119000/71150 MPa, tau0xf 0, interaction
+    coefficients 0.1/0.125/0.125/0.15/0.1/0.2; mixed-BC y tension
+    (VelGrad_BC -0.5e-3 1e-3 -0.5e-3, xx and zz stress free), TimeStep 0.1,
+    Err 5e-5, second phase gas, plain NR."""
+    gid = np.ones((8, 8, 8), dtype=np.int32)
+    gid[4:] = 2  # two orientation rows; the grain id written stays 1 below
+    euler = np.array([[0.0, 0.0, 0.0], [90.0, 35.0, 45.0]])
+    mat = Material(c11=162700.0, c12=119000.0, c44=71150.0, nu=0.35, tau0=0.0,
+                   self_inter=0.1, coplanar=0.125, cross_slip=0.125, glissile=0.15,
+                   hirth=0.1, lomer=0.2, rho_ssd_initial=1.0)
+    job = Job(n=(8, 8, 8), n_steps=n_steps, err=5e-5, iter_max=1000,
+              print_control=(1, print_every), velgrad_flag=(0, 1, 0, 1, 1, 1),
+              velgrad=(-0.5e-3, 1.0e-3, -0.5e-3, 0.0, 0.0, 0.0),
+              stress_flag=(1, 0, 1, 0, 0, 0), time_step_override=0.1, second_phase_gas=True)
+    os.makedirs(dirpath, exist_ok=True)
+    ang = euler[gid.reshape(-1) - 1]
+    with open(os.path.join(dirpath, "ms.txt"), "w") as f:
+        for v in range(512):
+            i, j, k = v // 64 + 1, (v // 8) % 8 + 1, v % 8 + 1
+            f.write("%g %g %g %d %d %d 1 1\n" % (ang[v, 0], ang[v, 1], ang[v, 2], i, j, k))
+    write_sx(os.path.join(dirpath, "cu.sx"), mat.tau0)
+    write_namelist(os.path.join(dirpath, "input"), job, mat, "ms.txt", "cu.sx")
+    return {"dir": dirpath, "input": os.path.join(dirpath, "input"), "rho0": None}

@@ -1,0 +1,42 @@
+"""The C-ABI library builds for sm_103a, loads, exports every entry point of
+include/evpg.h, and refuses to run without a GPU (no CPU fallback)."""
+import ctypes as C
+import os
+import re
+
+import pytest
+
+from conftest import ROOT
+
+
+def _declared():
+    src = open(os.path.join(ROOT, "include", "evpg.h")).read()
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?\w+\s*\*?\s*(evpg_\w+)\s*\(", src, re.M)))
+
+
+def test_header_declares_entry_points():
+    names = _declared()
+    for n in ("evpg_create", "evpg_destroy", "evpg_increment_begin", "evpg_equilibrium_iteration",
+              "evpg_equilibrium_solve", "evpg_increment_end", "evpg_download", "evpg_job_open",
+              "evpg_job_run"):
+        assert n in names
+
+
+def test_library_builds_and_exports_every_symbol():
+    from srx_gb300 import build
+    path = build.build()
+    lib = C.CDLL(path)
+    missing = [n for n in _declared() if not hasattr(lib, n)]
+    assert not missing, missing
+    assert os.path.exists(build.RUN)
+
+
+def test_no_cpu_fallback_without_device(tmp_path):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from srx_gb300 import evpg, rve
+    case = rve.make_case(str(tmp_path / "c"), (8, 8, 8), 3, 1, rve.Job(n=(8, 8, 8), n_steps=1))
+    with pytest.raises(evpg.EvpgError) as e:
+        evpg.Job(case["input"])
+    assert e.value.status == 9  # EVPG_ERR_NO_DEVICE

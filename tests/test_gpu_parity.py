@@ -1,0 +1,133 @@
+"""GPU path (C ABI, libevpg.so) against the reference's own outputs (golden
+fixtures) and against the oracle run on the same inputs.
+
+Tolerances (FP64 plain form): per-voxel fields within 1e-8 of the field's
+max magnitude, macroscopic stress within 1e-9 relative, identical equilibrium
+iteration counts. vm.out/dd.out are compared at their print precision (%e).
+FP32-bulk form: macroscopic stress within 1e-4 relative and field L2 within
+1e-3 of the FP64 result."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import (golden, read_iout_fields, read_iters, read_table, rel_err,
+                      write_spec_case)
+
+pytestmark = pytest.mark.gpu
+
+FIELD_TOL = 1e-8
+MACRO_TOL = 1e-9
+PRINT_TOL = 2e-6
+
+
+def _evpg():
+    from srx_gb300 import build, evpg
+    build.build()
+    return evpg
+
+
+def _run_gpu(case, out, steps, nr_mode, precision=0, iout=True):
+    evpg = _evpg()
+    os.makedirs(out, exist_ok=True)
+    with evpg.Job(case["input"], case.get("rho0"), precision=precision, nr_mode=nr_mode) as j:
+        j.run(str(out), steps, iout=iout)
+
+
+def test_bicrystal8_matches_reference(tmp_path):
+    z, spec = golden("bicrystal8")
+    case = write_spec_case(spec, tmp_path / "case")
+    _run_gpu(case, tmp_path / "out", spec["steps"], nr_mode=0)
+    assert read_iters(tmp_path / "out") == list(z["iters"])
+    assert rel_err(read_table(tmp_path / "out" / "vm.out"), z["vm"]) < PRINT_TOL
+    assert rel_err(read_table(tmp_path / "out" / "dd.out")[:, :2], z["dd"][:, :2]) < PRINT_TOL
+    for s in z["keep"]:
+        f = read_iout_fields(tmp_path / "out", int(s), 512)
+        for k in ("sig", "eps", "els", "rho_s", "gam_acum"):
+            assert rel_err(f[k], z["%s_%d" % (k, s)]) < FIELD_TOL, (k, int(s))
+
+
+@pytest.mark.parametrize("name", ["voronoi16_ls", "cfg0_32_ls"])
+def test_line_search_cases_match_reference(tmp_path, name):
+    z, spec = golden(name)
+    case = write_spec_case(spec, tmp_path / "case")
+    _run_gpu(case, tmp_path / "out", spec["steps"], nr_mode=1)
+    assert read_iters(tmp_path / "out") == list(z["iters"])
+    assert rel_err(read_table(tmp_path / "out" / "vm.out"), z["vm"]) < PRINT_TOL
+    N = int(np.prod(spec["n"]))
+    f = read_iout_fields(tmp_path / "out", spec["steps"] - 1, N)
+    idx = z["idx"]
+    for k in ("sig", "eps", "els", "rho_s", "gam_acum"):
+        assert rel_err(f[k][idx], z[k]) < FIELD_TOL, k
+
+
+def _oracle_case(tmp_path):
+    """Non-power-of-two grid (radix 3/5 and odd lengths), xy shear
+    and a gas second phase in part of the voxels."""
+    from srx_gb300 import rve
+    n = (12, 10, 9)
+    gid, euler = rve.voronoi(n, 6, seed=77)
+    phase = np.ones(n, dtype=np.int64)
+    phase[gid == 6] = 2
+    job = rve.Job(n=n, load="shear", rate=1e-3, strain_per_step=2e-4, n_steps=3, elast_bc=1,
+                  second_phase_gas=True, print_control=(1, 1))
+    return rve.write_case(str(tmp_path / "case"), gid, euler, job, phase=phase)
+
+
+@pytest.mark.parametrize("nr_mode", [0, 1])
+def test_against_oracle_on_mixed_radix_grid(tmp_path, oracle, nr_mode):
+    import ctypes as C
+    evpg = _evpg()
+    case = _oracle_case(tmp_path)
+    h = oracle.open(case["input"], nr_mode=nr_mode)
+    N = 12 * 10 * 9
+    try:
+        with evpg.Job(case["input"], nr_mode=nr_mode) as j:
+            for istep in range(3):
+                it_o = C.c_int()
+                assert oracle.L.evo_increment(h, istep, C.byref(it_o)) == 0
+                it_g = j.increment(istep)
+                assert it_g == it_o.value, istep
+                sc = j.scalars()
+                osc = oracle.field(h, "scalars", 32)
+                assert rel_err(sc[7:16], osc[0:9]) < MACRO_TOL, istep
+                sig_o = oracle.field(h, "Sig", 9 * N).reshape(N, 9)
+                assert rel_err(j.download(evpg.F_SIG), sig_o) < FIELD_TOL
+                rho_o = oracle.field(h, "rho_s", 12 * N).reshape(N, 12)
+                assert rel_err(j.download(evpg.F_RHO_S), rho_o) < FIELD_TOL
+                dg_o = oracle.field(h, "DisGrad", 9 * N).reshape(N, 9)
+                assert rel_err(j.download(evpg.F_DISGRAD), dg_o) < FIELD_TOL
+                tr_o = oracle.field(h, "TranMat", 9 * N).reshape(N, 9)
+                assert rel_err(j.download(evpg.F_TRANMAT), tr_o) < FIELD_TOL
+    finally:
+        oracle.L.evo_close(h)
+
+
+def test_solve_path_matches_iteration_path(tmp_path):
+    """evpg_equilibrium_solve (batched device loop) and the per-iteration call
+    give the same iterates."""
+    evpg = _evpg()
+    z, spec = golden("voronoi16_ls")
+    case = write_spec_case(spec, tmp_path / "case")
+    _run_gpu(case, tmp_path / "a", 1, nr_mode=1, iout=True)
+    with evpg.Job(case["input"], nr_mode=1) as j:
+        it = j.increment(0)
+        sig = j.download(evpg.F_SIG6)
+    assert it == read_iters(tmp_path / "a")[0]
+    f = read_iout_fields(tmp_path / "a", 0, 4096)
+    assert np.array_equal(sig, f["sig"])
+
+
+def test_fp32_bulk_within_stated_error(tmp_path):
+    """FP32 NR/FFT/Green with FP64 macro update, norms, state and a final FP64
+    NR refinement, against the FP64 reference result."""
+    z, spec = golden("voronoi16_ls")
+    case = write_spec_case(spec, tmp_path / "case")
+    _run_gpu(case, tmp_path / "out", spec["steps"], nr_mode=1, precision=1)
+    vm = read_table(tmp_path / "out" / "vm.out")
+    # s_vm (macroscopic von Mises stress) per increment
+    assert rel_err(vm[:, 5], z["vm"][:, 5]) < 1e-4
+    f = read_iout_fields(tmp_path / "out", spec["steps"] - 1, 4096)
+    for k in ("sig", "rho_s"):
+        l2 = np.linalg.norm(f[k] - z[k]) / np.linalg.norm(z[k])
+        assert l2 < 1e-3, (k, l2)
