@@ -211,7 +211,7 @@ static void free_ctx(Ctx* c) {
     void* ptrs[] = {c->sig64, c->dg64, c->dg_old, c->epsp, c->edot64, c->rho_s, c->rho_m,
                     c->gamdot64, c->gam_acum, c->tranmat, c->schm64, c->fc64, c->sgr64, c->orient,
                     c->phase, c->sig32, c->ddg32, c->b6_32, c->schm32, c->fc32, c->sgr32, c->spec,
-                    c->part_nr, c->part_end, c->macro, c->tw64[0], c->tw64[1], c->tw64[2],
+                    c->part_nr, c->part_nr2, c->ticket, c->part_end, c->macro, c->tw64[0], c->tw64[1], c->tw64[2],
                     c->tw32[0], c->tw32[1], c->tw32[2]};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -331,7 +331,9 @@ int evpg_create(const evpg_rve_desc* d, void** out) {
         AL(sp, 9 * (size_t)c->g.Nh);
         c->spec = sp;
     }
-    AL(c->part_nr, (size_t)c->nb_nr * NPART_NR);
+    AL(c->part_nr, (size_t)c->nb_nr * (NR_BLOCK / 32) * NPART_NR);
+    AL(c->part_nr2, (size_t)MACRO_BLOCKS * NPART_NR);
+    AL(c->ticket, 1);
     AL(c->part_end, (size_t)c->nb_end * NPART_END);
     AL(c->macro, 1);
     for (int a = 0; a < 3; a++) {

@@ -11,6 +11,7 @@ constexpr int NPART_NR = 15;   // err_e, err_s, sig6 sum, sig6 phase-1 sum, NR i
 constexpr int NPART_END = 18;  // rho_F, rho_P, rho_s, rho_m, d_dipole, d_forest, d_inplane,
                                // Eps (6), Edot (5)
 constexpr int NR_BLOCK = 128;
+constexpr int MACRO_BLOCKS = 64;
 constexpr int END_BLOCK = 128;
 
 // Kernel groups timed by the optional profiler (CUDA events on the context's
@@ -44,8 +45,10 @@ struct Ctx {
     // FP32 working set (FP32 bulk only)
     float *sig32, *ddg32, *b6_32, *schm32, *fc32, *sgr32;
     void* spec;  // 9 * Nh complex of the working precision
-    double* part_nr;
+    double* part_nr;   // [nb_nr * NR_BLOCK/32][NPART_NR] warp partials
     int nb_nr;
+    double* part_nr2;  // [MACRO_BLOCKS][NPART_NR]
+    unsigned int* ticket;
     double* part_end;
     int nb_end;
     Macro* macro;       // device

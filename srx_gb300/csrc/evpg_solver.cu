@@ -104,12 +104,6 @@ template <typename T> struct NrArgs {
     int check_done;
 };
 
-template <typename T> struct Eval {
-    T edot[5];
-    T d[15];   // upper triangle of d_edot (5x5)
-    T gam[NS];
-};
-
 __device__ __forceinline__ void sinh_cosh(double x, double& sh, double& ch) {
     if (x < 700.0) {
         const double e = exp(x), ei = 1.0 / e;
@@ -128,52 +122,58 @@ __device__ __forceinline__ void sinh_cosh(float x, float& sh, float& ch) {
     ch = 0.5f * (e + ei);
 }
 
-// StrainRate_Orowan at stress s (constitutive.c:585-725): per system the
-// resolved shear stress, sinh glide law and its derivative; returns edot,
-// d_edot and the shear rates. bad |= NaN seen.
+// StrainRate_Orowan at stress s (constitutive.c:585-725): per slip system the
+// resolved shear stress and the sinh glide law with its derivative; returns
+// edot (5), the upper triangle of d_edot (15) and the shear rates (shared
+// memory column of this thread). The system loop stays rolled to keep the
+// kernel small. bad |= NaN seen (the reference asserts).
+// Per-voxel constants of the slip systems staged in shared memory for the
+// sweep (column of this thread, stride NR_BLOCK): Schmid vectors at
+// [5i+q], tau_pass at [60+i], 1/(tau0+tau_cut) at [72+i], gam_o at [84+i].
+constexpr int NSTAGE = 96;
+
 template <typename T>
-__device__ __forceinline__ void flow_eval(const NrArgs<T>& a, const PhaseK<T>& P, int v,
-                                          const T* s, bool stale, Eval<T>& e, bool& bad) {
+__device__ __forceinline__ void flow_eval(const NrArgs<T>& a, int nsys, int v, const T* cs,
+                                          const T* s, bool stale, T* ed, T* dd, T* gam, bool& bad) {
     const size_t N = a.g.N;
 #pragma unroll
-    for (int q = 0; q < 5; q++) e.edot[q] = (T)0;
+    for (int q = 0; q < 5; q++) ed[q] = (T)0;
 #pragma unroll
-    for (int q = 0; q < 15; q++) e.d[q] = (T)0;
-#pragma unroll
-    for (int i = 0; i < NS; i++) {
-        e.gam[i] = (T)0;
-        if (i >= P.n_sys) continue;
+    for (int q = 0; q < 15; q++) dd[q] = (T)0;
+#pragma unroll 1
+    for (int i = 0; i < nsys; i++) {
         T sc[5];
 #pragma unroll
-        for (int q = 0; q < 5; q++) sc[q] = __ldg(a.schm + (size_t)(i * 5 + q) * N + v);
+        for (int q = 0; q < 5; q++) sc[q] = cs[(i * 5 + q) * NR_BLOCK];
         const T rss = sc[0] * s[0] + sc[1] * s[1] + sc[2] * s[2] + sc[3] * s[3] + sc[4] * s[4];
-        const T tp = __ldg(a.fc + (size_t)((stale ? 36 : 0) + i) * N + v);
+        const T tp = stale ? __ldg(a.fc + (size_t)(36 + i) * N + v) : cs[(60 + i) * NR_BLOCK];
         const T ar = fabs(rss);
+        T g = (T)0;
         if (ar > tp) {
-            const T itc = __ldg(a.fc + (size_t)(12 + i) * N + v);
-            const T go = __ldg(a.fc + (size_t)(24 + i) * N + v);
+            const T itc = cs[(72 + i) * NR_BLOCK];
+            const T go = cs[(84 + i) * NR_BLOCK];
             T sh, ch;
             sinh_cosh((ar - tp) * itc, sh, ch);
-            const T g = (rss > (T)0) ? go * sh : -(go * sh);
+            g = (rss > (T)0) ? go * sh : -(go * sh);
             const T g2 = go * ch * itc;
-            if (isnan(g) || isnan(g2)) bad = true;
-            e.gam[i] = g;
 #pragma unroll
-            for (int q = 0; q < 5; q++) e.edot[q] += sc[q] * g;
+            for (int q = 0; q < 5; q++) ed[q] += sc[q] * g;
             int k = 0;
 #pragma unroll
             for (int p = 0; p < 5; p++) {
                 const T w = sc[p] * g2;
 #pragma unroll
-                for (int q = p; q < 5; q++) e.d[k++] += w * sc[q];
+                for (int q = p; q < 5; q++) dd[k++] += w * sc[q];
             }
         }
+        gam[i * NR_BLOCK] = g;
     }
-    // constitutive.c:707,718 assert on NaN in edot and d_edot
+    bool nan = false;
 #pragma unroll
-    for (int q = 0; q < 5; q++) bad = bad || isnan(e.edot[q]);
+    for (int q = 0; q < 5; q++) nan = nan || isnan(ed[q]);
 #pragma unroll
-    for (int q = 0; q < 15; q++) bad = bad || isnan(e.d[q]);
+    for (int q = 0; q < 15; q++) nan = nan || isnan(dd[q]);
+    bad = bad || nan;
 }
 
 // Packed symmetric 6x6: index of (i,j), i <= j.
@@ -182,40 +182,40 @@ __host__ __device__ constexpr int sidx(int i, int j) { return i * 6 - i * (i - 1
 // Solve M x = b for symmetric positive definite M (packed upper, 21 entries)
 // by LDL^T without pivoting. Returns false when a pivot is not positive.
 template <typename T>
-__device__ __forceinline__ bool ldl_solve(const T (&m)[21], const T (&b)[6], T (&x)[6]) {
-    T L[6][6], d[6], id[6];
+__device__ __forceinline__ bool ldl_solve(T (&m)[21], const T (&b)[6], T (&x)[6]) {
+    // in place: m[sidx(k,i)] holds L(i,k) for i > k and d_k on the diagonal
+    T id[6];
+    bool ok = true;
 #pragma unroll
     for (int j = 0; j < 6; j++) {
-        T s = m[sidx(j, j)];
+        T dj = m[sidx(j, j)];
 #pragma unroll
-        for (int k = 0; k < j; k++) s -= L[j][k] * L[j][k] * d[k];
-        d[j] = s;
-        id[j] = (T)1 / s;
+        for (int k = 0; k < j; k++) dj -= m[sidx(k, j)] * m[sidx(k, j)] * m[sidx(k, k)];
+        m[sidx(j, j)] = dj;
+        ok = ok && (dj > (T)0);
+        id[j] = (T)1 / dj;
 #pragma unroll
         for (int i = j + 1; i < 6; i++) {
             T t = m[sidx(j, i)];
 #pragma unroll
-            for (int k = 0; k < j; k++) t -= L[i][k] * L[j][k] * d[k];
-            L[i][j] = t * id[j];
+            for (int k = 0; k < j; k++) t -= m[sidx(k, i)] * m[sidx(k, j)] * m[sidx(k, k)];
+            m[sidx(j, i)] = t * id[j];
         }
     }
-    bool ok = true;
-#pragma unroll
-    for (int j = 0; j < 6; j++) ok = ok && (d[j] > (T)0);
     T y[6];
 #pragma unroll
     for (int i = 0; i < 6; i++) {
-        T s = b[i];
+        T t = b[i];
 #pragma unroll
-        for (int k = 0; k < i; k++) s -= L[i][k] * y[k];
-        y[i] = s;
+        for (int k = 0; k < i; k++) t -= m[sidx(k, i)] * y[k];
+        y[i] = t;
     }
 #pragma unroll
     for (int i = 5; i >= 0; i--) {
-        T s = y[i] * id[i];
+        T t = y[i] * id[i];
 #pragma unroll
-        for (int k = i + 1; k < 6; k++) s -= L[k][i] * x[k];
-        x[i] = s;
+        for (int k = i + 1; k < 6; k++) t -= m[sidx(i, k)] * x[k];
+        x[i] = t;
     }
     return ok;
 }
@@ -231,108 +231,162 @@ __device__ __forceinline__ void mat6v(const T (&m)[6][6], const T* x, T* y) {
     }
 }
 
+// S x with S read from the per-orientation table (L1-resident: voxels of a
+// grain share it)
 template <typename T>
-__global__ void __launch_bounds__(NR_BLOCK) k_nr(const __grid_constant__ NrArgs<T> a) {
+__device__ __forceinline__ void sgr_v(const T* sg, const T* x, T* y) {
+#pragma unroll
+    for (int i = 0; i < 6; i++) {
+        T s = (T)0;
+#pragma unroll
+        for (int j = 0; j < 6; j++) s += __ldg(sg + i * 6 + j) * x[j];
+        y[i] = s;
+    }
+}
+
+// Warp-level partial sums without a block barrier: every warp writes its own
+// row of NPART_NR values (FP32: compensated within the warp).
+__device__ __forceinline__ void warp_store(double (&q)[NPART_NR], double* row) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int k = 0; k < NPART_NR; k++) {
+        double x = q[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+        if (lane == 0) row[k] = x;
+    }
+}
+__device__ __forceinline__ void warp_store(float (&q)[NPART_NR], double* row) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int k = 0; k < NPART_NR; k++) {
+        KSum ks{q[k], 0.0f};
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float s = __shfl_xor_sync(0xffffffffu, ks.s, o);
+            const float c = __shfl_xor_sync(0xffffffffu, ks.c, o);
+            ks.add(s);
+            ks.c += c;
+        }
+        if (lane == 0) row[k] = (double)ks.s + (double)ks.c;
+    }
+}
+
+template <typename T> struct NrMinBlocks { static constexpr int v = 2; };
+template <> struct NrMinBlocks<float> { static constexpr int v = 3; };
+
+// One UpdateStress sweep (evolution.c:181-423). The line search of the
+// NR_MODIFIED build runs as a small state machine so the flow rule has a
+// single call site: a MAIN step evaluates the flow rule at sigma, solves for
+// the Newton step and either applies it (plain) or proposes the first trial
+// point; a TRIAL step evaluates the flow rule there and accepts the point,
+// backtracks or gives up (evolution.c:337-370). An accepted trial's
+// evaluation is the next MAIN's evaluation.
+template <typename T, int LS>
+__global__ void __launch_bounds__(NR_BLOCK, NrMinBlocks<T>::v) k_nr(const __grid_constant__ NrArgs<T> a) {
+    extern __shared__ __align__(16) unsigned char nr_smem[];
+    T* s_stage = reinterpret_cast<T*>(nr_smem);
     if (a.check_done && a.macro->done) return;
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
     const int N = a.g.N;
-    const double dtd = (double)a.mat.dt;
     const T dt = a.mat.dt;
+    T* stg = s_stage + threadIdx.x;
+    T* gam = s_stage + NSTAGE * NR_BLOCK + threadIdx.x;
     T pe = 0, ps = 0, ss[6] = {0, 0, 0, 0, 0, 0}, s1[6] = {0, 0, 0, 0, 0, 0};
     int nr = 0;
     bool bad = false, sing = false, lsfail = false;
     const bool stale0 = a.stale_mode && a.macro->iter == 0;
-    if (v < N) {
-        const int ph = a.phase[v];
-        const PhaseK<T>& P = a.mat.ph[ph - 1];
-        if (!P.crystal) {
+    const int ph = (v < N) ? a.phase[v] : 1;
+    const PhaseK<T>& P = a.mat.ph[ph - 1];
+    if (v < N && !P.crystal) {
 #pragma unroll
-            for (int c = 0; c < 6; c++) a.sig[(size_t)c * N + v] = (T)0;
-            if (a.edot)
+        for (int c = 0; c < 6; c++) a.sig[(size_t)c * N + v] = (T)0;
+        if (a.edot)
 #pragma unroll
-                for (int c = 0; c < 5; c++) a.edot[(size_t)c * N + v] = (T)0;
-        } else {
-            const T* sg = a.sgr + (size_t)a.orient[v] * 36;
-            T S[6][6];
+            for (int c = 0; c < 5; c++) a.edot[(size_t)c * N + v] = (T)0;
+    } else if (v < N) {
+        const int nsys = P.n_sys;
+        const T* sg = a.sgr + (size_t)a.orient[v] * 36;
+        for (int i = 0; i < nsys; i++) {
 #pragma unroll
-            for (int i = 0; i < 6; i++)
+            for (int q = 0; q < 5; q++) stg[(i * 5 + q) * NR_BLOCK] = __ldg(a.schm + (size_t)(i * 5 + q) * N + v);
 #pragma unroll
-                for (int j = 0; j < 6; j++) S[i][j] = __ldg(sg + i * 6 + j);
-            T lam[6], sig[6], av[6], m0[21];
+            for (int q = 0; q < 3; q++) stg[(60 + 12 * q + i) * NR_BLOCK] = __ldg(a.fc + (size_t)(12 * q + i) * N + v);
+        }
+        T lam[6], sig[6], av[6], old[6], step[6], te[6];
 #pragma unroll
-            for (int c = 0; c < 6; c++) {
-                lam[c] = a.sig[(size_t)c * N + v];
-                sig[c] = lam[c];
-                av[c] = a.epsb[(size_t)c * N + v] - a.dg[(size_t)c * N + v];
-            }
+        for (int c = 0; c < 6; c++) {
+            lam[c] = a.sig[(size_t)c * N + v];
+            sig[c] = lam[c];
+            av[c] = a.epsb[(size_t)c * N + v] - a.dg[(size_t)c * N + v];
+        }
+        T signorm = 0;
 #pragma unroll
-            for (int i = 0; i < 6; i++)
-#pragma unroll
-                for (int j = i; j < 6; j++)
-                    m0[sidx(i, j)] = a.mat.s066[i][j] + (T)0.5 * (S[i][j] + S[j][i]);
-            T signorm = 0;
-#pragma unroll
-            for (int c = 0; c < 6; c++) signorm += lam[c] * lam[c];
-            signorm = sqrt(signorm);
-            T erral = (T)10 * a.tol, ce = 0, cs = 0;
-            Eval<T> ev, et;
-            bool have = false;
-            T edot_out[5] = {0, 0, 0, 0, 0};
-            T gl[NS];  // shear rates of the last flow-rule call (gamdot)
-#pragma unroll
-            for (int i = 0; i < NS; i++) gl[i] = (T)0;
-            int it = 0;
-            while (it < a.itmax && fabs(erral) > fabs(a.tol)) {
+        for (int c = 0; c < 6; c++) signorm += lam[c] * lam[c];
+        signorm = sqrt(signorm);
+        T ed[5], dd[15], edot_out[5] = {0, 0, 0, 0, 0};
+        T erral = (T)10 * a.tol, ce = 0, cs = 0;
+        T f_old = 0, slope = 0, alam = 1, alam2 = 0, alamin = 0;
+        bool have = false, trial = false;
+        int it = 0, guard = 0;
+        for (;;) {
+            if (!trial) {
+                if (!(it < a.itmax && fabs(erral) > fabs(a.tol))) break;
                 it++;
-                T old[6];
 #pragma unroll
                 for (int c = 0; c < 6; c++) old[c] = sig[c];
-                if (!have) flow_eval<T>(a, P, v, sig, stale0 && it == 1, ev, bad);
-                have = false;
+            }
+            if (!have) flow_eval<T>(a, nsys, v, stg, sig, !trial && stale0 && it == 1, ed, dd, gam, bad);
+            have = false;
+            if (bad) break;
+            bool finish = false;
+            if (!trial) {
 #pragma unroll
-                for (int i = 0; i < NS; i++) gl[i] = ev.gam[i];
-                if (bad) break;
-#pragma unroll
-                for (int q = 0; q < 5; q++) edot_out[q] = ev.edot[q];
+                for (int q = 0; q < 5; q++) edot_out[q] = ed[q];
                 // te = tot_eps - strain = (Eps - strain) + edot dt + S sig
-                T te[6], Ss[6];
-                mat6v<T>(S, sig, Ss);
+                T Ss[6];
+                sgr_v<T>(sg, sig, Ss);
 #pragma unroll
-                for (int c = 0; c < 6; c++) te[c] = av[c] + (c < 5 ? ev.edot[c] * dt : (T)0) + Ss[c];
+                for (int c = 0; c < 6; c++) te[c] = av[c] + (c < 5 ? ed[c] * dt : (T)0) + Ss[c];
+                // M = S066 + sym(S) + dt d_edot; rhs = S066 R = S066 (sig - lam) + te
                 T m[21];
 #pragma unroll
-                for (int k = 0; k < 21; k++) m[k] = m0[k];
+                for (int i = 0; i < 6; i++)
+#pragma unroll
+                    for (int j = i; j < 6; j++)
+                        m[sidx(i, j)] = a.mat.s066[i][j] + (T)0.5 * (__ldg(sg + i * 6 + j) + __ldg(sg + j * 6 + i));
                 {
                     int k = 0;
 #pragma unroll
                     for (int p = 0; p < 5; p++)
 #pragma unroll
-                        for (int q = p; q < 5; q++) m[sidx(p, q)] += dt * ev.d[k++];
+                        for (int q = p; q < 5; q++) m[sidx(p, q)] += dt * dd[k++];
                 }
-                // rhs = S066 R = S066 (sig - lam) + te
-                T dl[6], rhs[6], step[6];
+                T dl[6], rhs[6];
 #pragma unroll
                 for (int c = 0; c < 6; c++) dl[c] = sig[c] - lam[c];
                 mat6v<T>(a.mat.s066, dl, rhs);
 #pragma unroll
                 for (int c = 0; c < 6; c++) rhs[c] += te[c];
-                if (!ldl_solve<T>(m, rhs, step)) sing = true;
-                if (a.nr_mode == 0) {
+                if (!ldl_solve<T>(m, rhs, step)) { sing = true; break; }
+                if (!LS) {
 #pragma unroll
                     for (int c = 0; c < 6; c++) sig[c] -= step[c];
+                    finish = true;
                 } else {
-                    // NR_MODIFIED (evolution.c:280-371). The reference evaluates
-                    // slope = (J^T R).step with step = -J^-1 R (capped at length 10);
-                    // that product is -|R|^2 times the cap factor, used here directly:
-                    // through an ill-conditioned J its rounded value can change sign.
-                    T R[6], CR[6], f_old = 0;
+                    // NR_MODIFIED (evolution.c:284-336). slope = (J^T R).step with
+                    // step = -J^-1 R capped at length 10, i.e. -|R|^2 times the cap
+                    // factor; used directly because through an ill-conditioned J
+                    // the rounded product can change sign.
+                    T CR[6];
                     mat6v<T>(a.mat.c066, te, CR);
+                    f_old = 0;
 #pragma unroll
                     for (int c = 0; c < 6; c++) {
-                        R[c] = dl[c] + CR[c];
-                        f_old += R[c] * R[c];
+                        const T r = dl[c] + CR[c];
+                        f_old += r * r;
                     }
-                    T slope = -f_old;
+                    slope = -f_old;
                     f_old *= (T)0.5;
                     T nrm = 0;
 #pragma unroll
@@ -348,75 +402,75 @@ __global__ void __launch_bounds__(NR_BLOCK) k_nr(const __grid_constant__ NrArgs<
                         slope *= cap;
                     }
                     if (!(slope < (T)0)) {
-                        // R == 0: already at the root
-                        if (slope == (T)0) {
-#pragma unroll
-                            for (int c = 0; c < 6; c++) sig[c] = old[c];
-                        } else {
-                            lsfail = true;
-                            break;
-                        }
+                        if (slope != (T)0) { lsfail = true; break; }
+                        finish = true;  // R == 0: at the root already
                     } else {
                         T test = 0;
-    #pragma unroll
+#pragma unroll
                         for (int c = 0; c < 6; c++) {
                             const T tt = fabs(step[c]) / fmax(fabs(old[c]), (T)1);
                             if (tt > test) test = tt;
                         }
-                        const T alamin = (T)1e-7 / test;
-                        T alam = 1, alam2 = 0, tmplam = 0;
-                        const T f2 = 0;  // never updated in the reference
-                        for (int ls = 0; ls < 200; ls++) {
-    #pragma unroll
-                            for (int c = 0; c < 6; c++) sig[c] = old[c] + alam * step[c];
-                            flow_eval<T>(a, P, v, sig, false, et, bad);
-    #pragma unroll
-                            for (int i = 0; i < NS; i++) gl[i] = et.gam[i];
-                            if (bad) break;
-                            T Rt[6], tt6[6], fnew = 0;
-                            mat6v<T>(S, sig, Ss);
-    #pragma unroll
-                            for (int c = 0; c < 6; c++) tt6[c] = av[c] + (c < 5 ? et.edot[c] * dt : (T)0) + Ss[c];
-                            mat6v<T>(a.mat.c066, tt6, Rt);
-    #pragma unroll
-                            for (int c = 0; c < 6; c++) {
-                                const T r = sig[c] - lam[c] + Rt[c];
-                                fnew += r * r;
-                            }
-                            fnew *= (T)0.5;
-                            if (alam < alamin) {
-    #pragma unroll
-                                for (int c = 0; c < 6; c++) sig[c] = old[c];
-                                break;
-                            } else if (fnew <= f_old + (T)1e-4 * alam * slope) {
-                                ev = et;
-                                have = true;
-                                break;
-                            } else {
-                                if (fabs(alam - (T)1) < (T)1e-4) {
-                                    tmplam = -slope / ((T)2 * (fnew - f_old - slope));
-                                } else {
-                                    const T rhs1 = fnew - f_old - alam * slope;
-                                    const T rhs2 = f2 - f_old - alam2 * slope;
-                                    const T ac = (rhs1 / (alam * alam) - rhs2 / (alam2 * alam2)) / (alam - alam2);
-                                    const T bc = (-alam2 * rhs1 / (alam * alam) + alam * rhs2 / (alam2 * alam2)) /
-                                                 (alam - alam2);
-                                    if (fabs(ac) < (T)1e-4) {
-                                        tmplam = -slope / ((T)2 * bc);
-                                    } else {
-                                        const T disc = bc * bc - (T)3 * ac * slope;
-                                        if (disc < (T)0) tmplam = (T)0.5 * alam;
-                                        else if (bc <= (T)0) tmplam = (-bc + sqrt(disc)) / ((T)3 * ac);
-                                        else tmplam = -slope / (bc + sqrt(disc));
-                                    }
-                                    if (tmplam > (T)0.5 * alam) tmplam = (T)0.5 * alam;
-                                }
-                            }
-                            alam2 = alam;
-                            alam = fmax(tmplam, (T)0.1 * alam);
-                        }
+                        alamin = (T)1e-7 / test;
+                        alam = 1;
+                        alam2 = 0;
+#pragma unroll
+                        for (int c = 0; c < 6; c++) sig[c] = old[c] + step[c];
+                        trial = true;
+                        guard = 0;
                     }
                 }
+            } else {
+                // TRIAL: merit at sig = old + alam step (NR_quality, evolution.c:115-154)
+                T Ss[6], tt6[6], Rt[6], fnew = 0;
+                sgr_v<T>(sg, sig, Ss);
+#pragma unroll
+                for (int c = 0; c < 6; c++) tt6[c] = av[c] + (c < 5 ? ed[c] * dt : (T)0) + Ss[c];
+                mat6v<T>(a.mat.c066, tt6, Rt);
+#pragma unroll
+                for (int c = 0; c < 6; c++) {
+                    const T r = sig[c] - lam[c] + Rt[c];
+                    fnew += r * r;
+                }
+                fnew *= (T)0.5;
+                if (alam < alamin) {
+#pragma unroll
+                    for (int c = 0; c < 6; c++) sig[c] = old[c];
+                    trial = false;
+                    finish = true;
+                } else if (fnew <= f_old + (T)1e-4 * alam * slope) {
+                    have = true;  // this evaluation serves the next MAIN step
+                    trial = false;
+                    finish = true;
+                } else {
+                    T tmplam;
+                    if (fabs(alam - (T)1) < (T)1e-4) {
+                        tmplam = -slope / ((T)2 * (fnew - f_old - slope));
+                    } else {
+                        const T f2 = 0;  // never updated in the reference
+                        const T rhs1 = fnew - f_old - alam * slope;
+                        const T rhs2 = f2 - f_old - alam2 * slope;
+                        const T ac = (rhs1 / (alam * alam) - rhs2 / (alam2 * alam2)) / (alam - alam2);
+                        const T bc = (-alam2 * rhs1 / (alam * alam) + alam * rhs2 / (alam2 * alam2)) /
+                                     (alam - alam2);
+                        if (fabs(ac) < (T)1e-4) {
+                            tmplam = -slope / ((T)2 * bc);
+                        } else {
+                            const T disc = bc * bc - (T)3 * ac * slope;
+                            if (disc < (T)0) tmplam = (T)0.5 * alam;
+                            else if (bc <= (T)0) tmplam = (-bc + sqrt(disc)) / ((T)3 * ac);
+                            else tmplam = -slope / (bc + sqrt(disc));
+                        }
+                        if (tmplam > (T)0.5 * alam) tmplam = (T)0.5 * alam;
+                    }
+                    alam2 = alam;
+                    alam = fmax(tmplam, (T)0.1 * alam);
+#pragma unroll
+                    for (int c = 0; c < 6; c++) sig[c] = old[c] + alam * step[c];
+                    if (++guard > 200) { lsfail = true; break; }
+                }
+            }
+            if (finish) {
                 T cnr = 0;
                 ce = 0;
                 cs = 0;
@@ -427,49 +481,53 @@ __global__ void __launch_bounds__(NR_BLOCK) k_nr(const __grid_constant__ NrArgs<
                     cs += (sig[c] - lam[c]) * (sig[c] - lam[c]);
                 }
                 erral = sqrt(cnr) / signorm;
+                if (sizeof(T) == 4) {
+                    // FP32 form: at the NR solution tot_eps - eps = -S066 (sig - lambda);
+                    // evaluated at the final stress it carries no lag of the last
+                    // Newton step (the reference takes tot_eps before that step, which
+                    // at the FP32 NR tolerance would floor Err_e near 1e-5).
+                    T d6[6], q6[6];
+#pragma unroll
+                    for (int c = 0; c < 6; c++) d6[c] = sig[c] - lam[c];
+                    mat6v<T>(a.mat.s066, d6, q6);
+                    ce = 0;
+#pragma unroll
+                    for (int c = 0; c < 6; c++) ce += q6[c] * q6[c];
+                }
                 ce = sqrt(ce);
                 cs = sqrt(cs);
-                if (bad || sing) break;
-            }
-            nr = it;
-#pragma unroll
-            for (int c = 0; c < 6; c++) a.sig[(size_t)c * N + v] = sig[c];
-            if (a.edot)
-#pragma unroll
-                for (int c = 0; c < 5; c++) a.edot[(size_t)c * N + v] = edot_out[c];
-            if (a.gamdot)
-#pragma unroll
-                for (int i = 0; i < NS; i++)
-                    if (i < P.n_sys) a.gamdot[(size_t)i * N + v] = gl[i];
-            pe = ce;
-            ps = cs;
-#pragma unroll
-            for (int c = 0; c < 6; c++) {
-                ss[c] = sig[c];
-                s1[c] = (ph == 1) ? sig[c] : (T)0;
             }
         }
+        nr = it;
+#pragma unroll
+        for (int c = 0; c < 6; c++) a.sig[(size_t)c * N + v] = sig[c];
+        if (a.edot)
+#pragma unroll
+            for (int c = 0; c < 5; c++) a.edot[(size_t)c * N + v] = edot_out[c];
+        if (a.gamdot)
+            for (int i = 0; i < nsys; i++) a.gamdot[(size_t)i * N + v] = gam[i * NR_BLOCK];
+        pe = ce;
+        ps = cs;
+#pragma unroll
+        for (int c = 0; c < 6; c++) {
+            ss[c] = sig[c];
+            s1[c] = (ph == 1) ? sig[c] : (T)0;
+        }
     }
-    (void)dtd;
     if (bad) set_status(a.macro, 4);
     if (sing) set_status(a.macro, 5);
     if (lsfail) set_status(a.macro, 6);
-    double* out = a.part + (size_t)blockIdx.x * NPART_NR;
-    if (sizeof(T) == 8) {
-        double q[NPART_NR];
-        q[0] = (double)pe; q[1] = (double)ps;
+    T q[NPART_NR];
+    q[0] = pe;
+    q[1] = ps;
 #pragma unroll
-        for (int c = 0; c < 6; c++) { q[2 + c] = (double)ss[c]; q[8 + c] = (double)s1[c]; }
-        q[14] = (double)nr;
-        block_reduce_store<NPART_NR>(q, out);
-    } else {
-        float q[NPART_NR];
-        q[0] = (float)pe; q[1] = (float)ps;
-#pragma unroll
-        for (int c = 0; c < 6; c++) { q[2 + c] = (float)ss[c]; q[8 + c] = (float)s1[c]; }
-        q[14] = (float)nr;
-        block_reduce_store_f<NPART_NR>(q, out);
+    for (int c = 0; c < 6; c++) {
+        q[2 + c] = ss[c];
+        q[8 + c] = s1[c];
     }
+    q[14] = (T)nr;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    warp_store(q, a.part + (size_t)warp * NPART_NR);
 }
 
 // ---------------------------------------------------------------- macro
@@ -477,30 +535,15 @@ __global__ void __launch_bounds__(NR_BLOCK) k_nr(const __grid_constant__ NrArgs<
 struct MacroArgs {
     LoopCfg cfg;
     Macro* macro;
-    const double* part;
-    int nblocks;
+    const double* part;   // [nrows][NPART_NR] warp partials of the NR sweep
+    int nrows;
+    double* part2;        // [gridDim][NPART_NR]
+    unsigned int* ticket; // last-block detection, reset by the last block
 };
 
-// Sum of the NR partials, then get_smacro (evolution.c:590-664), the error
-// normalisation (evolution.c:1233-1252) and the loop test (evolution.c:1150).
-__global__ void __launch_bounds__(256) k_macro(const __grid_constant__ MacroArgs a) {
-    Macro* m = a.macro;
-    if (m->done) return;
-    __shared__ double tot[NPART_NR];
-    {
-        double v[NPART_NR];
-#pragma unroll
-        for (int q = 0; q < NPART_NR; q++) v[q] = 0.0;
-        for (int b = threadIdx.x; b < a.nblocks; b += blockDim.x)
-#pragma unroll
-            for (int q = 0; q < NPART_NR; q++) v[q] += a.part[(size_t)b * NPART_NR + q];
-        double o[NPART_NR];
-        block_reduce_store<NPART_NR>(v, o);
-        if (threadIdx.x < NPART_NR) tot[threadIdx.x] = o[threadIdx.x];
-    }
-    __syncthreads();
-    if (threadIdx.x != 0) return;
-    const LoopCfg& c = a.cfg;
+// get_smacro and the loop test (evolution.c:590-664, 1227-1252, 1150) on the
+// FP64 totals; thread 0 of the last block.
+__device__ void macro_update(const LoopCfg& c, Macro* m, const double* tot) {
     double s6[6], s16[6], sa[3][3], s1a[3][3];
     for (int q = 0; q < 6; q++) {
         s6[q] = tot[2 + q];
@@ -513,7 +556,7 @@ __global__ void __launch_bounds__(256) k_macro(const __grid_constant__ MacroArgs
             m->sig_avg[i][j] = sa[i][j] * c.wgt;
             m->sig_avg1[i][j] = s1a[i][j] * (c.wgt / c.wgt_ph1);
         }
-    static const int IJV[2][6] = {{0, 1, 2, 1, 0, 0}, {0, 1, 2, 2, 2, 1}};
+    const int IJV[2][6] = {{0, 1, 2, 1, 0, 0}, {0, 1, 2, 2, 2, 1}};
     for (int i = 0; i < 6; i++) {
         const int ii = IJV[0][i], jj = IJV[1][i];
         double d = 0.0;
@@ -573,6 +616,56 @@ __global__ void __launch_bounds__(256) k_macro(const __grid_constant__ MacroArgs
     const double mx = (fabs(es) > fabs(ee)) ? fabs(es) : fabs(ee);
     m->converged = !(mx > c.err_tol);
     m->done = m->converged || m->iter >= c.iter_max || m->status != 0;
+}
+
+// Deterministic two-level sum of the NR warp partials: each block sums a
+// contiguous range of rows in a fixed order; the last block to finish sums
+// the block rows in order and runs the macro update.
+__global__ void __launch_bounds__(256) k_macro(const __grid_constant__ MacroArgs a) {
+    Macro* m = a.macro;
+    if (m->done) return;
+    __shared__ double red[NPART_NR][8];
+    __shared__ bool last;
+    const int per = (a.nrows + gridDim.x - 1) / gridDim.x;
+    const int r0 = blockIdx.x * per, r1 = min(a.nrows, r0 + per);
+    double v[NPART_NR];
+#pragma unroll
+    for (int q = 0; q < NPART_NR; q++) v[q] = 0.0;
+    for (int r = r0 + (int)threadIdx.x; r < r1; r += blockDim.x)
+#pragma unroll
+        for (int q = 0; q < NPART_NR; q++) v[q] += a.part[(size_t)r * NPART_NR + q];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < NPART_NR; q++) {
+        double x = v[q];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+        if (lane == 0) red[q][wid] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < NPART_NR) {
+        double s = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) s += red[threadIdx.x][w];
+        a.part2[(size_t)blockIdx.x * NPART_NR + threadIdx.x] = s;
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = (atomicAdd(a.ticket, 1u) == gridDim.x - 1);
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    // last block: sum the block rows in a fixed order, then the macro update
+    __shared__ double tot[NPART_NR];
+    if (threadIdx.x < NPART_NR) {
+        double s = 0.0;
+        for (int b = 0; b < (int)gridDim.x; b++) s += __ldcg(a.part2 + (size_t)b * NPART_NR + threadIdx.x);
+        tot[threadIdx.x] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        *a.ticket = 0;
+        macro_update(a.cfg, m, tot);
+    }
 }
 
 // ------------------------------------------------------ increment head
@@ -905,7 +998,14 @@ static cudaError_t nr_t(Ctx& c, const Material<T>& mat, T* sig, const T* dg, con
     a.nr_mode = c.nr_mode; a.stale_mode = stale_mode; a.check_done = check_done;
     const int grp = check_done ? PG_NR : PG_REFINE;
     prof_mark(c, grp, true);
-    k_nr<T><<<c.nb_nr, NR_BLOCK, 0, c.stream>>>(a);
+    const size_t sm = (size_t)(NSTAGE + NS) * NR_BLOCK * sizeof(T);
+    if (c.nr_mode) {
+        cudaFuncSetAttribute(k_nr<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        k_nr<T, 1><<<c.nb_nr, NR_BLOCK, sm, c.stream>>>(a);
+    } else {
+        cudaFuncSetAttribute(k_nr<T, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        k_nr<T, 0><<<c.nb_nr, NR_BLOCK, sm, c.stream>>>(a);
+    }
     prof_mark(c, grp, false);
     return cudaGetLastError();
 }
@@ -926,9 +1026,11 @@ cudaError_t launch_macro(Ctx& c) {
     a.cfg = c.cfg;
     a.macro = c.macro;
     a.part = c.part_nr;
-    a.nblocks = c.nb_nr;
+    a.nrows = c.nb_nr * (NR_BLOCK / 32);
+    a.part2 = c.part_nr2;
+    a.ticket = c.ticket;
     prof_mark(c, PG_MACRO, true);
-    k_macro<<<1, 256, 0, c.stream>>>(a);
+    k_macro<<<MACRO_BLOCKS, 256, 0, c.stream>>>(a);
     prof_mark(c, PG_MACRO, false);
     return cudaGetLastError();
 }

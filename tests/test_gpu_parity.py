@@ -61,29 +61,31 @@ def test_line_search_cases_match_reference(tmp_path, name):
         assert rel_err(f[k][idx], z[k]) < FIELD_TOL, k
 
 
-def _oracle_case(tmp_path):
-    """Non-power-of-two grid (radix 3/5 and odd lengths), xy shear
-    and a gas second phase in part of the voxels."""
+def _oracle_case(tmp_path, gas=False, iter_max=1000, steps=3):
+    """Non-power-of-two grid (radix 3 and 5 stages, odd length, Nyquist planes
+    on two axes), z tension; with gas=True the sixth grain is a gas phase.
+    The reference's own NR fails on xy shear with this material (the elastic
+    predictor overshoots the passing stress by ~60 cutting stresses), so
+    tension is the load that can be pinned."""
     from srx_gb300 import rve
     n = (12, 10, 9)
     gid, euler = rve.voronoi(n, 6, seed=77)
     phase = np.ones(n, dtype=np.int64)
-    phase[gid == 6] = 2
-    job = rve.Job(n=n, load="shear", rate=1e-3, strain_per_step=2e-4, n_steps=3, elast_bc=1,
-                  second_phase_gas=True, print_control=(1, 1))
+    if gas:
+        phase[gid == 6] = 2
+    job = rve.Job(n=n, load="tension", rate=1e-3, strain_per_step=2e-4, n_steps=steps,
+                  iter_max=iter_max, second_phase_gas=gas, print_control=(1, 1))
     return rve.write_case(str(tmp_path / "case"), gid, euler, job, phase=phase)
 
 
-@pytest.mark.parametrize("nr_mode", [0, 1])
-def test_against_oracle_on_mixed_radix_grid(tmp_path, oracle, nr_mode):
+def _compare_with_oracle(oracle, case, nr_mode, steps):
     import ctypes as C
     evpg = _evpg()
-    case = _oracle_case(tmp_path)
     h = oracle.open(case["input"], nr_mode=nr_mode)
     N = 12 * 10 * 9
     try:
         with evpg.Job(case["input"], nr_mode=nr_mode) as j:
-            for istep in range(3):
+            for istep in range(steps):
                 it_o = C.c_int()
                 assert oracle.L.evo_increment(h, istep, C.byref(it_o)) == 0
                 it_g = j.increment(istep)
@@ -91,16 +93,25 @@ def test_against_oracle_on_mixed_radix_grid(tmp_path, oracle, nr_mode):
                 sc = j.scalars()
                 osc = oracle.field(h, "scalars", 32)
                 assert rel_err(sc[7:16], osc[0:9]) < MACRO_TOL, istep
-                sig_o = oracle.field(h, "Sig", 9 * N).reshape(N, 9)
-                assert rel_err(j.download(evpg.F_SIG), sig_o) < FIELD_TOL
-                rho_o = oracle.field(h, "rho_s", 12 * N).reshape(N, 12)
-                assert rel_err(j.download(evpg.F_RHO_S), rho_o) < FIELD_TOL
-                dg_o = oracle.field(h, "DisGrad", 9 * N).reshape(N, 9)
-                assert rel_err(j.download(evpg.F_DISGRAD), dg_o) < FIELD_TOL
-                tr_o = oracle.field(h, "TranMat", 9 * N).reshape(N, 9)
-                assert rel_err(j.download(evpg.F_TRANMAT), tr_o) < FIELD_TOL
+                for f, name, w in ((evpg.F_SIG, "Sig", 9), (evpg.F_RHO_S, "rho_s", 12),
+                                   (evpg.F_DISGRAD, "DisGrad", 9), (evpg.F_TRANMAT, "TranMat", 9),
+                                   (evpg.F_EPS, "Eps", 9), (evpg.F_GAM_ACUM, "gam_acum", 12)):
+                    ref = oracle.field(h, name, w * N).reshape(N, w)
+                    assert rel_err(j.download(f), ref) < FIELD_TOL, (istep, name)
     finally:
         oracle.L.evo_close(h)
+
+
+@pytest.mark.parametrize("nr_mode,steps", [(0, 1), (1, 3)])
+def test_against_oracle_on_mixed_radix_grid(tmp_path, oracle, nr_mode, steps):
+    _compare_with_oracle(oracle, _oracle_case(tmp_path, steps=steps), nr_mode, steps)
+
+
+def test_against_oracle_with_gas_phase(tmp_path, oracle):
+    """Gas voxels (zero stress, excluded from the NR and the dislocation
+    update); the loop stalls with the infinite stiffness contrast, so it is
+    compared after IterMax = 60 iterations."""
+    _compare_with_oracle(oracle, _oracle_case(tmp_path, gas=True, iter_max=60, steps=1), 1, 1)
 
 
 def test_solve_path_matches_iteration_path(tmp_path):
