@@ -198,6 +198,27 @@ int evpg_profile_read(void *ctx, double *ms, int64_t *launches, int32_t n);
 /* Kernels launched on this context so far. */
 int evpg_launch_count(void *ctx, int64_t *n);
 
+/* Allocation-free Green-operator correction (no counterpart in the
+ * reference). For callers that cannot allocate device memory on the call
+ * path -- their device memory belongs to another allocator, or their device
+ * footprint is fixed when the library loads. It computes, in FP64,
+ *   du9 = Re IFFT( Gamma(k) : FFT(sig6) ) / N
+ * the displacement-gradient correction of one equilibrium iteration
+ * (evolution.c:1157-1201 without the macro term), from caller-owned device
+ * buffers: sig6 [6][N] is the stress in the B basis (one plane per
+ * component, voxel index (x*n1+y)*n2+z), du9 [9][N] receives the B basis of
+ * the symmetric part and A12, A13, A23 of the antisymmetric part. c0 and s0
+ * are C0 and S0 (3x3x3x3, row-major); elast_bc is ElastBC.
+ * Limits: every n_i <= 64 and n0*n1*(n2/2+1) <= 17408 (e.g. 32^3); larger
+ * grids return EVPG_ERR_ARG. Scratch is a static device array of ~2.5 MB that
+ * every GPU loading the library keeps until exit; nothing is allocated. The
+ * first call on a device looks up that array's device address, so make that
+ * first call outside any stream capture. Calls whose work overlaps on the GPU
+ * share the array and race: serialise them. stream: a cudaStream_t or NULL. */
+int evpg_green_correction_noalloc(const double *sig6, double *du9, int32_t n0, int32_t n1,
+                                  int32_t n2, const double c0[81], const double s0[81],
+                                  int32_t elast_bc, void *stream);
+
 /* ---- host driver: the reference's own input files and increment loop ---- */
 
 /* GetNameList + SetupJob from the reference's namelist file; relative file

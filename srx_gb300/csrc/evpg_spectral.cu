@@ -296,3 +296,170 @@ cudaError_t launch_spectral(Ctx& c) {
 }
 
 }  // namespace evpg
+
+// ---------------------------------------------------------------------------
+// Allocation-free Green-operator correction.
+//
+// For callers that cannot allocate device memory on the call path -- code
+// whose device memory is owned by another allocator (a framework's pool), or
+// a service whose device footprint must be fixed when the library loads --
+// this entry point runs the spectral chain of one equilibrium iteration on
+// caller-owned input and output buffers. Its scratch (the nine half spectra,
+// the twiddle tables, a zero loop flag and a zero macro correction) lives in
+// the file-scope array below, which every GPU that loads the library holds
+// until the process exits. Calls that overlap on the GPU share that array and
+// race; callers serialise them (one stream, or events).
+
+#include <math.h>
+#include <string.h>
+
+#include <mutex>
+
+#include "evpg.h"
+
+namespace evpg {
+
+constexpr int NOALLOC_MAX_LEN = 64;               // per axis
+constexpr long long NOALLOC_MAX_HALF = 32 * 32 * 17;  // n0*n1*(n2/2+1), e.g. 32^3
+constexpr size_t NOALLOC_SPEC_BYTES = 9 * NOALLOC_MAX_HALF * sizeof(double2);
+constexpr size_t NOALLOC_TW_OFF = NOALLOC_SPEC_BYTES;
+constexpr size_t NOALLOC_ZERO_OFF = NOALLOC_TW_OFF + 3 * NOALLOC_MAX_LEN * sizeof(double2);
+constexpr size_t NOALLOC_BYTES = NOALLOC_ZERO_OFF + 256;  // flag (int) + 9 doubles, padded
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
+
+static std::mutex g_noalloc_mu;
+static void* g_noalloc_ptr[128];  // device address of the array, per device
+
+static void na_plan(int n, FftPlan& p) {
+    memset(&p, 0, sizeof p);
+    p.n = n;
+    int m = n, nf = 0;
+    const int pref[] = {8, 4, 2, 3, 5};
+    for (int r : pref)
+        while (m % r == 0 && nf < 12) {
+            p.radix[nf++] = r;
+            m /= r;
+        }
+    for (int q = 7; m > 1 && nf < 12; q += 2)
+        while (m % q == 0 && nf < 12) {
+            p.radix[nf++] = q;
+            m /= q;
+        }
+    p.nf = nf;
+    int ns = 1;
+    for (int s = 0; s < nf; s++) {
+        p.ns[s] = ns;
+        ns *= p.radix[s];
+    }
+}
+
+// exp(-2 pi i t/n) with exact axis values (same table as the context path)
+static double2 na_root(long t, long n) {
+    const long q = (4 * t) / n, r = 4 * t - q * n;
+    long double c0, s0;
+    if (r == 0) {
+        c0 = 1.0L;
+        s0 = 0.0L;
+    } else if (2 * r <= n) {
+        const long double th = 1.57079632679489661923132169163975144L * ((long double)r / (long double)n);
+        c0 = cosl(th);
+        s0 = sinl(th);
+    } else {
+        const long double th = 1.57079632679489661923132169163975144L * ((long double)(n - r) / (long double)n);
+        c0 = sinl(th);
+        s0 = cosl(th);
+    }
+    long double cc, ss;
+    switch (q & 3) {
+        case 0: cc = c0; ss = s0; break;
+        case 1: cc = -s0; ss = c0; break;
+        case 2: cc = -c0; ss = -s0; break;
+        default: cc = s0; ss = -c0; break;
+    }
+    return make_double2((double)cc, -(double)ss);
+}
+
+}  // namespace evpg
+
+extern "C" int evpg_green_correction_noalloc(const double* sig6, double* du9, int32_t n0, int32_t n1,
+                                             int32_t n2, const double c0[81], const double s0[81],
+                                             int32_t elast_bc, void* stream) {
+    using namespace evpg;
+    const int n[3] = {n0, n1, n2};
+    if (!sig6 || !du9 || !c0 || !s0) return EVPG_ERR_ARG;
+    for (int a = 0; a < 3; a++)
+        if (n[a] < 1 || n[a] > NOALLOC_MAX_LEN) return EVPG_ERR_ARG;
+    const long long half = (long long)n0 * n1 * (n2 / 2 + 1);
+    if (half > NOALLOC_MAX_HALF) return EVPG_ERR_ARG;  // beyond the static scratch
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 128) return EVPG_ERR_CUDA;
+    unsigned char* base;
+    {
+        // once per device, with that device current: the device address of the
+        // static array (its host-side name is not a device pointer)
+        std::lock_guard<std::mutex> lk(g_noalloc_mu);
+        if (!g_noalloc_ptr[dev]) {
+            void* p = nullptr;
+            if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return EVPG_ERR_CUDA;
+            g_noalloc_ptr[dev] = p;
+        }
+        base = (unsigned char*)g_noalloc_ptr[dev];
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    Grid g;
+    g.n0 = n0; g.n1 = n1; g.n2 = n2; g.nh = n2 / 2 + 1; g.N = n0 * n1 * n2; g.Nh = half;
+    FftPlan pl[3];
+    double2 tw[3][NOALLOC_MAX_LEN];
+    for (int a = 0; a < 3; a++) {
+        na_plan(n[a], pl[a]);
+        for (int t = 0; t < n[a]; t++) tw[a][t] = na_root(t, n[a]);
+    }
+    double2* spec = (double2*)base;
+    double2* twd = (double2*)(base + NOALLOC_TW_OFF);
+    int* zero_flag = (int*)(base + NOALLOC_ZERO_OFF);
+    double* zero9 = (double*)(base + NOALLOC_ZERO_OFF + 16);
+    const double2* twp[3] = {twd, twd + NOALLOC_MAX_LEN, twd + 2 * NOALLOC_MAX_LEN};
+    // the loop flag and the macro correction must read zero; the output is
+    // accumulated into, so it starts at zero too
+    if (cudaMemsetAsync(base + NOALLOC_ZERO_OFF, 0, 256, st) != cudaSuccess) return EVPG_ERR_CUDA;
+    if (cudaMemsetAsync(du9, 0, (size_t)9 * g.N * sizeof(double), st) != cudaSuccess) return EVPG_ERR_CUDA;
+    if (cudaMemcpyAsync(twd, tw, sizeof tw, cudaMemcpyHostToDevice, st) != cudaSuccess) return EVPG_ERR_CUDA;
+
+    const size_t es = sizeof(double2), budget = 72 * 1024;
+    ZArgs<double> za;
+    za.g = g; za.pl = pl[2]; za.done = zero_flag; za.sig = sig6; za.dg = du9; za.spec = spec;
+    za.tw = twp[2]; za.dE9 = zero9; za.invN = 1.0 / (double)g.N;
+    za.P = pick_p<double>(n2, 2 * n2, es, budget);
+    const int ncol = n0 * n1;
+    const size_t sm = (size_t)(n2 + 2 * za.P * n2) * es;
+    YArgs<double> ya;
+    ya.g = g; ya.pl = pl[1]; ya.done = zero_flag; ya.spec = spec; ya.tw = twp[1]; ya.ncomp = 6;
+    ya.P = pick_p<double>(n1, 2 * (n1 + 1), es, budget);
+    if (ya.P > g.nh) ya.P = g.nh;
+    const size_t smy = (size_t)(n1 + 2 * ya.P * (n1 + 1)) * es;
+    const int ntile_y = (g.nh + ya.P - 1) / ya.P;
+    XArgs<double> xa;
+    xa.g = g; xa.pl = pl[0]; xa.done = zero_flag; xa.spec = spec; xa.tw = twp[0];
+    xa.P = pick_p<double>(n0, 18 * (n0 + 1), es, 150 * 1024);
+    if (xa.P > g.nh) xa.P = g.nh;
+    for (int i = 0; i < 81; i++) {
+        (&xa.gk.c0[0][0][0][0])[i] = c0[i];
+        (&xa.gk.s0[0][0][0][0])[i] = s0[i];
+    }
+    xa.gk.elast_bc = elast_bc;
+    const size_t smx = (size_t)(n0 + 18 * xa.P * (n0 + 1)) * es;
+    const int ntile_x = (g.nh + xa.P - 1) / xa.P;
+    cudaFuncSetAttribute(k_fwd_z<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    cudaFuncSetAttribute(k_inv_z<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    cudaFuncSetAttribute(k_y<double, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smy);
+    cudaFuncSetAttribute(k_y<double, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smy);
+    cudaFuncSetAttribute(k_x_green<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smx);
+    k_fwd_z<double><<<(ncol + za.P - 1) / za.P, 256, sm, st>>>(za);
+    k_y<double, -1><<<n0 * ntile_y, 256, smy, st>>>(ya);
+    k_x_green<double><<<n1 * ntile_x, 256, smx, st>>>(xa);
+    ya.ncomp = 9;
+    k_y<double, 1><<<n0 * ntile_y, 256, smy, st>>>(ya);
+    k_inv_z<double><<<(ncol + za.P - 1) / za.P, 256, sm, st>>>(za);
+    return cudaGetLastError() == cudaSuccess ? EVPG_OK : EVPG_ERR_CUDA;
+}
