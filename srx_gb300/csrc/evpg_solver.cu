@@ -273,7 +273,7 @@ __device__ __forceinline__ void warp_store(float (&q)[NPART_NR], double* row) {
 }
 
 template <typename T> struct NrMinBlocks { static constexpr int v = 2; };
-template <> struct NrMinBlocks<float> { static constexpr int v = 3; };
+template <> struct NrMinBlocks<float> { static constexpr int v = 4; };
 
 // One UpdateStress sweep (evolution.c:181-423). The line search of the
 // NR_MODIFIED build runs as a small state machine so the flow rule has a

@@ -169,7 +169,11 @@ __global__ void __launch_bounds__(256) k_x_green(const __grid_constant__ XArgs<T
 }
 
 // Inverse z: pairs of Hermitian half spectra -> one complex IFFT -> two real
-// fields; DisGrad += dE + re/N (evolution.c:1197).
+// fields; DisGrad += dE + re/N (evolution.c:1197). The DisGrad values of a
+// pair are loaded into registers before its transform, so their latency
+// overlaps the FFT stages (at most INVZ_EPT elements per thread).
+constexpr int INVZ_EPT = 16;
+
 template <typename T>
 __global__ void __launch_bounds__(256) k_inv_z(const __grid_constant__ ZArgs<T> a) {
     if (*a.done) return;
@@ -180,13 +184,23 @@ __global__ void __launch_bounds__(256) k_inv_z(const __grid_constant__ ZArgs<T> 
     C2<T>* bA = tw + n;
     C2<T>* bB = bA + P * n;
     const int ncol = g.n0 * g.n1, c0 = blockIdx.x * P, np = min(P, ncol - c0);
+    const int tot = np * n;
     load_tw<T>(tw, a.tw, n);
     for (int pair = 0; pair < 5; pair++) {
         const int ca = 2 * pair, cb = 2 * pair + 1;
         const bool hasb = cb < 9;
+        T* da = a.dg + (size_t)ca * g.N + (size_t)c0 * n;
+        T* db = a.dg + (size_t)(hasb ? cb : ca) * g.N + (size_t)c0 * n;
+        T pa[INVZ_EPT], pb[INVZ_EPT];
+#pragma unroll
+        for (int e = 0; e < INVZ_EPT; e++) {
+            const int i = threadIdx.x + e * blockDim.x;
+            pa[e] = (i < tot) ? da[i] : (T)0;
+            pb[e] = (i < tot && hasb) ? db[i] : (T)0;
+        }
         const C2<T>* sa = a.spec + (size_t)ca * g.Nh + (size_t)c0 * nh;
         const C2<T>* sb = a.spec + (size_t)(hasb ? cb : ca) * g.Nh + (size_t)c0 * nh;
-        for (int i = threadIdx.x; i < np * n; i += blockDim.x) {
+        for (int i = threadIdx.x; i < tot; i += blockDim.x) {
             const int col = i / n, k = i - col * n;
             C2<T> z;
             if (k < nh) {
@@ -203,12 +217,14 @@ __global__ void __launch_bounds__(256) k_inv_z(const __grid_constant__ ZArgs<T> 
         __syncthreads();
         const C2<T>* r = fft_batch<T, 1>(bA, bB, np, n, a.pl, tw);
         const T ea = (T)a.dE9[ca], eb = hasb ? (T)a.dE9[cb] : (T)0;
-        T* da = a.dg + (size_t)ca * g.N + (size_t)c0 * n;
-        T* db = a.dg + (size_t)(hasb ? cb : ca) * g.N + (size_t)c0 * n;
-        for (int i = threadIdx.x; i < np * n; i += blockDim.x) {
-            const C2<T> z = r[i];
-            da[i] += ea + z.x * a.invN;
-            if (hasb) db[i] += eb + z.y * a.invN;
+#pragma unroll
+        for (int e = 0; e < INVZ_EPT; e++) {
+            const int i = threadIdx.x + e * blockDim.x;
+            if (i < tot) {
+                const C2<T> z = r[i];
+                da[i] = pa[e] + (ea + z.x * a.invN);
+                if (hasb) db[i] = pb[e] + (eb + z.y * a.invN);
+            }
         }
         __syncthreads();
     }
@@ -223,6 +239,15 @@ template <typename T> static int pick_p(int n, int per_pencil_elems, size_t elem
     return p;
 }
 
+// Pencils per CTA: as many as the shared-memory budget allows, but few enough
+// that the grid has at least `want` CTAs (a few per SM) to hide latency.
+static int pencils(long long total_pencils, int pmax, long long want) {
+    long long p = total_pencils / want;
+    if (p > pmax) p = pmax;
+    if (p < 1) p = 1;
+    return (int)p;
+}
+
 template <typename T>
 static cudaError_t spectral_t(Ctx& c, T* sig, T* dg, const C2<T>* const* tw) {
     const Grid& g = c.g;
@@ -230,14 +255,23 @@ static cudaError_t spectral_t(Ctx& c, T* sig, T* dg, const C2<T>* const* tw) {
     const int* done = macro_field<int>(c.macro, offsetof(Macro, done));
     const size_t es = sizeof(C2<T>);
     const size_t budget = 72 * 1024;
+    int nsm = 152;
+    {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    }
+    const long long want = 4LL * nsm;
     cudaError_t e;
-    // z passes
     {
         ZArgs<T> za;
         za.g = g; za.pl = c.pl[2]; za.done = done; za.sig = sig; za.dg = dg; za.spec = spec;
-        za.tw = tw[2]; za.dE9 = macro_field<double>(c.macro, offsetof(Macro, dE9)); za.invN = (T)(1.0 / (double)g.N);
-        za.P = pick_p<T>(g.n2, 2 * g.n2, es, budget);
+        za.tw = tw[2]; za.dE9 = macro_field<double>(c.macro, offsetof(Macro, dE9));
+        za.invN = (T)(1.0 / (double)g.N);
         const int ncol = g.n0 * g.n1;
+        za.P = pencils(ncol, pick_p<T>(g.n2, 2 * g.n2, es, budget), want);
+        if (za.P * g.n2 > 256 * INVZ_EPT) za.P = (256 * INVZ_EPT) / g.n2;
+        if (za.P < 1) za.P = 1;
         const size_t sm = (size_t)(g.n2 + 2 * za.P * g.n2) * es;
         cudaFuncSetAttribute(k_fwd_z<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         cudaFuncSetAttribute(k_inv_z<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
@@ -247,7 +281,7 @@ static cudaError_t spectral_t(Ctx& c, T* sig, T* dg, const C2<T>* const* tw) {
         // y forward
         YArgs<T> ya;
         ya.g = g; ya.pl = c.pl[1]; ya.done = done; ya.spec = spec; ya.tw = tw[1]; ya.ncomp = 6;
-        ya.P = pick_p<T>(g.n1, 2 * (g.n1 + 1), es, budget);
+        ya.P = pencils((long long)g.n0 * g.nh, pick_p<T>(g.n1, 2 * (g.n1 + 1), es, budget), want);
         if (ya.P > g.nh) ya.P = g.nh;
         const size_t smy = (size_t)(g.n1 + 2 * ya.P * (g.n1 + 1)) * es;
         cudaFuncSetAttribute(k_y<T, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smy);
@@ -259,7 +293,7 @@ static cudaError_t spectral_t(Ctx& c, T* sig, T* dg, const C2<T>* const* tw) {
         // x + Green
         XArgs<T> xa;
         xa.g = g; xa.pl = c.pl[0]; xa.done = done; xa.spec = spec; xa.tw = tw[0];
-        xa.P = pick_p<T>(g.n0, 18 * (g.n0 + 1), es, 150 * 1024);
+        xa.P = pencils((long long)g.n1 * g.nh, pick_p<T>(g.n0, 18 * (g.n0 + 1), es, 75 * 1024), want);
         if (xa.P > g.nh) xa.P = g.nh;
         const Material<T>& m = material_of<T>(c);
         for (int i = 0; i < 81; i++) {
@@ -431,6 +465,7 @@ extern "C" int evpg_green_correction_noalloc(const double* sig6, double* du9, in
     za.g = g; za.pl = pl[2]; za.done = zero_flag; za.sig = sig6; za.dg = du9; za.spec = spec;
     za.tw = twp[2]; za.dE9 = zero9; za.invN = 1.0 / (double)g.N;
     za.P = pick_p<double>(n2, 2 * n2, es, budget);
+    if (za.P * n2 > 256 * INVZ_EPT) za.P = (256 * INVZ_EPT) / n2;
     const int ncol = n0 * n1;
     const size_t sm = (size_t)(n2 + 2 * za.P * n2) * es;
     YArgs<double> ya;
