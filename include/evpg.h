@@ -182,6 +182,30 @@ int evpg_equilibrium_solve(void *ctx, double e_vm, evpg_iter_out *out);
  * Update_Flag == 1 && istep > 1). out may be NULL. */
 int evpg_increment_end(void *ctx, int32_t reorient, evpg_incr_out *out);
 
+/* The whole increment -- head, equilibrium loop, tail -- as one CUDA graph
+ * launch on the context's stream (captured on the first call, replayed
+ * after): the loop is a conditional WHILE node whose condition the device
+ * sets after every iteration, so no host round trip happens inside the
+ * increment. Same results as evpg_increment_begin + evpg_equilibrium_solve +
+ * evpg_increment_end (with the increment tail skipped when the loop stops on
+ * an error). e_vm: strain-error normaliser; reorient as in
+ * evpg_increment_end. it/inc may be NULL. No counterpart in the reference,
+ * whose loop is host-driven (evolution.c:1150). */
+int evpg_increment(void *ctx, const double udot_dt[3][3], int32_t creep,
+                   const double disgrad_avg_actual[3][3], double time_tot, double e_vm,
+                   int32_t reorient, evpg_iter_out *it, evpg_incr_out *inc);
+
+/* Change the loading between increments (a mid-run BC switch, e.g.
+ * tension then shear; the reference reads one BC set per run, init.c:865-901):
+ * the Voigt flags, the applied Cauchy stress and the antisymmetric part of
+ * the applied velocity gradient. The host passes the new Udot*dt to the next
+ * increment head. No counterpart in the reference. */
+int evpg_set_load(void *ctx, const int32_t velgrad_bc_flag[6], const int32_t stress_bc_flag[6],
+                  const double scauchy[3][3], const double udot_a[3][3]);
+/* Device bytes evpg_create allocates for an n[0] x n[1] x n[2] RVE with
+ * n_orient distinct orientations (for admission by HBM footprint). */
+int evpg_estimate_bytes(const int32_t n[3], int32_t precision, int32_t n_orient, int64_t *bytes);
+
 int evpg_download(void *ctx, int32_t field, double *host, size_t count);
 int evpg_upload(void *ctx, int32_t field, const double *host, size_t count);
 int evpg_synchronize(void *ctx);
@@ -219,6 +243,38 @@ int evpg_green_correction_noalloc(const double *sig6, double *du9, int32_t n0, i
                                   int32_t n2, const double c0[81], const double s0[81],
                                   int32_t elast_bc, void *stream);
 
+/* ---- batches: many RVE contexts advanced by the same launches ----
+ * (no counterpart in the reference, which runs one RVE per MPI job)
+ *
+ * A batch holds up to any number of contexts of one precision and NR mode
+ * ("slots"). evpg_batch_round runs one round on the batch's own stream: the
+ * increment heads of the slots staged with evpg_batch_stage, then
+ * equilibrium iterations -- each kernel launched once over all slots whose
+ * loop is running -- with every slot's increment tail in the iteration where
+ * its loop ends, until no slot is running or max_ticks iterations ran. A
+ * slot that finished its increment in the round reads phase 3 (ended) from
+ * evpg_batch_slot; one still iterating reads 2 and continues in the next
+ * round. The round is one CUDA graph launch (conditional WHILE node),
+ * re-captured when the slots change. A context belongs to at most one batch
+ * at a time and issues no work of its own while the batch runs; results are
+ * identical to the context's own evpg_increment. */
+int evpg_batch_create(int32_t precision, int32_t nr_mode, void **batch_out);
+int evpg_batch_destroy(void *batch);
+/* Replace the slots (contexts stay owned by the caller). */
+int evpg_batch_set(void *batch, void *const *ctxs, int32_t n);
+/* Controls of slot's next increment (as evpg_increment). */
+int evpg_batch_stage(void *batch, int32_t slot, const double udot_dt[3][3], int32_t creep,
+                     const double disgrad_avg_actual[3][3], double time_tot, double e_vm,
+                     int32_t reorient);
+int evpg_batch_round(void *batch, int32_t max_ticks, int32_t *ticks);
+/* After a round: phase (0 idle, 1 staged, 2 running, 3 ended), sticky
+ * status (evpg_status of the slot's last error) and the macro outputs of
+ * the slot's current increment. Any out pointer may be NULL. */
+int evpg_batch_slot(void *batch, int32_t slot, int32_t *phase, int32_t *status,
+                    evpg_iter_out *it, evpg_incr_out *inc);
+int evpg_batch_launch_count(void *batch, int64_t *n);
+const char *evpg_batch_last_error(void);
+
 /* ---- host driver: the reference's own input files and increment loop ---- */
 
 /* GetNameList + SetupJob from the reference's namelist file; relative file
@@ -236,6 +292,28 @@ int evpg_job_nsteps(void *job);
  * iters: equilibrium iterations taken. */
 int evpg_job_increment(void *job, int32_t istep, int32_t *iters);
 
+/* Batched increments of jobs (one precision and NR mode per batch):
+ * evpg_job_stage puts increment istep of a job into a batch slot holding the
+ * job's context; after evpg_batch_round, evpg_job_collect finishes the
+ * job's increment if its slot ended (*ended = 1, iters = its equilibrium
+ * iterations). evpg_jobs_run_batched runs nsteps[i] increments of every job
+ * in one batch, rounds of at most max_ticks iterations, iters[i*stride+k]
+ * = iterations of job i's increment k; results equal evpg_job_increment's. */
+int evpg_job_stage(void *job, void *batch, int32_t slot, int32_t istep);
+int evpg_job_collect(void *job, void *batch, int32_t slot, int32_t *ended, int32_t *iters);
+int evpg_jobs_run_batched(void *const *jobs, int32_t n, const int32_t *nsteps, int32_t max_ticks,
+                          int32_t *iters, int32_t stride, int64_t *rounds);
+
+/* Mid-run load switch of a job (tension then shear, ...): the Voigt flags
+ * and values of the velocity-gradient and stress boundary conditions
+ * (VelGrad_BC_Flag, VelGrad_BC, Stress_BC_Flag, Stress_BC, init.c:865-901)
+ * for the increments that follow; _from reads them from another namelist. */
+int evpg_job_set_load(void *job, const int32_t velgrad_flag[6], const double velgrad[6],
+                      const int32_t stress_flag[6], const double stress[6]);
+int evpg_job_set_load_from(void *job, const char *input_path);
+/* CellDim of a namelist file, without opening the job. */
+int evpg_job_grid(const char *input_path, int32_t n[3]);
+
 /* Scalars after the last increment: [0] TimeTot, [1] e_vm, [2] evmp,
  * [3] d_vm, [4] dvmp, [5] s_vm, [6] s_vm1, [7..15] SigAvg, [16..24] SigAvg1,
  * [25..32] rho averages as evpg_incr_out, [33] NR iterations of the
@@ -246,6 +324,53 @@ int evpg_job_scalars(void *job, double *out, int32_t count);
  * write_iout the reference's .iout dumps at PrintControl steps. nsteps < 0:
  * N_steps from the namelist. */
 int evpg_job_run(void *job, const char *outdir, int32_t nsteps, int32_t write_iout);
+
+/* ---- serving: continuous batching of solve requests ----
+ * (no counterpart in the reference)
+ *
+ * Requests arrive at any time (evpg_server_submit: a namelist file, optional
+ * per-voxel initial density, the number of increments and an optional load
+ * switch to another namelist's boundary conditions after switch_step
+ * increments). Loader threads open them in arrival order as soon as their
+ * device footprint fits hbm_budget; the GPU thread admits opened requests
+ * into free slots of one batch at every round boundary and advances all
+ * slots together, round_ticks equilibrium iterations per round. Finished
+ * solves release their device memory. Times are seconds since the server
+ * was created. */
+typedef struct evpg_server_cfg {
+    int32_t precision, nr_mode;
+    int64_t hbm_budget;    /* bytes of contexts the server may hold */
+    int32_t max_slots;     /* RVEs advanced together */
+    int32_t round_ticks;   /* equilibrium iterations per round */
+    int32_t loaders;       /* host threads opening requests */
+} evpg_server_cfg;
+
+typedef struct evpg_request_info {
+    int32_t state;         /* 0 queued, 1 loading, 2 ready, 3 running, 4 done, 5 failed */
+    int32_t status;        /* evpg_status of a failed request */
+    int32_t increments;    /* increments finished */
+    int64_t iterations;    /* equilibrium iterations, summed over increments */
+    double t_submit, t_admit, t_done;
+    int64_t device_bytes;  /* footprint reserved while loaded */
+} evpg_request_info;
+
+typedef struct evpg_server_stats {
+    int32_t completed, failed;
+    int64_t increments, iterations, rounds, ticks;
+    double solve_p50, solve_p99;   /* submit -> done [s] */
+    double incr_p50, incr_p99;     /* increment staged -> increment ended [s] */
+    double span;                   /* first submit -> last completion [s] */
+    double solves_per_s;
+} evpg_serve_stats;
+
+int evpg_server_create(const evpg_server_cfg *cfg, void **server_out);
+int evpg_server_submit(void *server, const char *input_path, const char *rho0_path, int32_t nsteps,
+                       int32_t switch_step, const char *switch_input_path, int64_t *id);
+/* Wait until every submitted request finished (EVPG_ERR_ITERMAX on timeout). */
+int evpg_server_wait(void *server, double timeout_s);
+int evpg_server_request(void *server, int64_t id, evpg_request_info *info);
+int evpg_server_stats(void *server, evpg_serve_stats *stats);
+int evpg_server_destroy(void *server);
 
 #ifdef __cplusplus
 }

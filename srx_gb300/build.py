@@ -21,8 +21,8 @@ LIB = os.path.join(LIBDIR, "libevpg.so")
 RUN = os.path.join(LIBDIR, "evpg_run")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["evpg_api.cu", "evpg_spectral.cu", "evpg_solver.cu"]
-C_SOURCES = ["host/evpg_job.c"]
+CU_SOURCES = ["evpg_api.cu", "evpg_spectral.cu", "evpg_solver.cu", "evpg_batch.cu"]
+C_SOURCES = ["host/evpg_job.c", "host/evpg_serve.c"]
 
 
 def _nvcc() -> str:
@@ -71,7 +71,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     with cf.ThreadPoolExecutor(max_workers=min(8, len(jobs))) as ex:
         list(ex.map(_run, jobs))
     objs = [os.path.join(obj, os.path.basename(s) + ".o") for s in CU_SOURCES + C_SOURCES]
-    _run([nvcc, *ARCH, "-shared", "-o", LIB, *objs, "-lm"])
+    _run([nvcc, *ARCH, "-shared", "-o", LIB, *objs, "-lm", "-lpthread"])
     _run([nvcc, *ARCH, "-o", RUN, os.path.join(obj, "evpg_run.c.o"), "-L", LIBDIR, "-levpg",
           "-Xlinker", "-rpath,$ORIGIN", "-lm"])
     if verbose:

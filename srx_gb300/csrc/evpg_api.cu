@@ -9,6 +9,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <mutex>
 #include <vector>
 
 namespace evpg {
@@ -20,6 +21,11 @@ static int fail(int st, const char* fmt, ...) {
     va_start(ap, fmt);
     vsnprintf(g_err, sizeof g_err, fmt, ap);
     va_end(ap);
+    return st;
+}
+
+int record_error(int st, const char* msg) {
+    snprintf(g_err, sizeof g_err, "%s", msg);
     return st;
 }
 
@@ -207,6 +213,7 @@ static void prof_free(Ctx& c) {
 
 static void free_ctx(Ctx* c) {
     if (!c) return;
+    free_solo(*c);
     prof_free(*c);
     void* ptrs[] = {c->sig64, c->dg64, c->dg_old, c->epsp, c->edot64, c->rho_s, c->rho_m,
                     c->gamdot64, c->gam_acum, c->tranmat, c->schm64, c->fc64, c->sgr64, c->orient,
@@ -216,8 +223,27 @@ static void free_ctx(Ctx* c) {
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (c->macro_host) cudaFreeHost(c->macro_host);
+    if (c->ctl_host) cudaFreeHost(c->ctl_host);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+    delete c->ks;
     delete c;
+}
+
+void set_kernel_attributes() {
+    static std::mutex mu;
+    static unsigned long long done_mask = 0;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lk(mu);
+    if (dev >= 0 && dev < 64 && (done_mask >> dev) & 1ULL) return;
+    spectral_attributes();
+    solver_attributes();
+    if (dev >= 0 && dev < 64) done_mask |= 1ULL << dev;
+}
+
+void build_sets(Ctx& c) {
+    build_spectral_sets(c);
+    build_solver_sets(c);
 }
 
 }  // namespace evpg
@@ -342,6 +368,7 @@ int evpg_create(const evpg_rve_desc* d, void** out) {
     }
 #undef AL
     if (e == cudaSuccess) e = cudaMallocHost((void**)&c->macro_host, sizeof(Macro));
+    if (e == cudaSuccess) e = cudaMallocHost((void**)&c->ctl_host, sizeof(IncrCtl));
     if (e != cudaSuccess) {
         free_ctx(c);
         cudaGetLastError();
@@ -349,6 +376,7 @@ int evpg_create(const evpg_rve_desc* d, void** out) {
                     "allocation: %s", cudaGetErrorString(e));
     }
     memset(c->macro_host, 0, sizeof(Macro));
+    memset(c->ctl_host, 0, sizeof(IncrCtl));
 
     // host-side layout changes: AoS tensors -> SoA planes in the B basis
     std::vector<double> h(60 * n);
@@ -398,10 +426,25 @@ int evpg_create(const evpg_rve_desc* d, void** out) {
         e = put(c->tw64[a], t64.data(), na * sizeof(double2));
         if (e == cudaSuccess) e = put(c->tw32[a], t32.data(), na * sizeof(float2));
     }
+    // an idle context: no increment requested, loop finished
+    if (e == cudaSuccess) {
+        c->macro_host->done = 1;
+        c->macro_host->ctl.phase = PH_IDLE;
+        e = put(c->macro, c->macro_host, sizeof(Macro));
+    }
     if (e != cudaSuccess) {
         free_ctx(c);
         return fail(EVPG_ERR_CUDA, "upload: %s", cudaGetErrorString(e));
     }
+    {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, dev);
+    }
+    set_kernel_attributes();
+    c->ks = new KernelSets();
+    memset((void*)c->ks, 0, sizeof(KernelSets));
+    build_sets(*c);
     *out = c;
     return EVPG_OK;
 }
@@ -485,24 +528,12 @@ int evpg_synchronize(void* ctx) {
 
 namespace evpg {
 
-__global__ void k_macro_begin(Macro* m, double drx, double err0) {
-    for (int i = 0; i < 3; i++)
-        for (int j = 0; j < 3; j++) {
-            m->dE[i][j] = 0.0;
-            m->dE_acum[i][j] = 0.0;
-        }
-    for (int q = 0; q < 9; q++) m->dE9[q] = 0.0;
-    m->err_e = err0;
-    m->err_s = err0;
-    m->iter = 0;
-    m->done = 0;
-    m->converged = 0;
-    m->status = 0;
-    m->nr_iters = 0;
-    m->tpass_drx = drx;
+__global__ void k_set_evm(Macro* m, double e_vm) {
+    m->e_vm = e_vm;
+    m->ctl.e_vm = e_vm;
 }
 
-__global__ void k_set_evm(Macro* m, double e_vm) { m->e_vm = e_vm; }
+__global__ void k_set_reorient(Macro* m, int r) { m->ctl.reorient = r; }
 
 static int read_macro(Ctx* c) {
     CK(cudaMemcpyAsync(c->macro_host, c->macro, sizeof(Macro), cudaMemcpyDeviceToHost, c->stream));
@@ -526,10 +557,31 @@ static void fill_iter_out(const Macro& m, evpg_iter_out* o) {
 }
 
 static int launch_iteration(Ctx* c) {
-    CK(launch_spectral(*c));
-    CK(launch_nr(*c, 0));
+    CK(launch_spectral(*c, GATE_RUNNING));
+    CK(launch_nr(*c, 0, GATE_RUNNING));
     CK(launch_macro(*c));
     return EVPG_OK;
+}
+
+// Controls of one increment into the context's pinned staging area.
+static void stage_ctl(Ctx* c, const double udot_dt[3][3], int creep, const double dgavg[3][3],
+                      double time_tot, double e_vm, int reorient) {
+    IncrCtl& k = *c->ctl_host;
+    double u9[9], g9[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    tensor_to_9(udot_dt, u9);
+    if (creep) tensor_to_9(dgavg, g9);
+    memcpy(k.udot9, u9, sizeof u9);
+    memcpy(k.dgavg9, g9, sizeof g9);
+    // DeltaTau_DRX*exp((t_last-TimeTot)/TimeStep/tau_DRX), t_last = -1E3*tau_DRX*TimeStep
+    const double dt = c->m64.dt;
+    const double t_last = -1E3 * c->tau_drx * dt;
+    k.drx = c->delta_tau_drx * exp((t_last - time_tot) / dt / c->tau_drx);
+    k.e_vm = e_vm;
+    k.err0 = 2. * c->cfg.err_tol;
+    k.creep = creep ? 1 : 0;
+    k.reorient = reorient ? 1 : 0;
+    k.phase = PH_BEGIN;
+    k.pad = 0;
 }
 
 }  // namespace evpg
@@ -540,20 +592,14 @@ int evpg_increment_begin(void* ctx, const double udot_dt[3][3], int32_t creep,
                          const double dgavg[3][3], double time_tot) {
     Ctx* c = (Ctx*)ctx;
     if (!c || !udot_dt) return fail(EVPG_ERR_ARG, "null argument");
-    double u9[9], g9[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-    tensor_to_9(udot_dt, u9);
-    if (creep) {
-        if (!dgavg) return fail(EVPG_ERR_ARG, "creep needs disgrad_avg_actual");
-        tensor_to_9(dgavg, g9);
-    }
-    // DeltaTau_DRX*exp((t_last-TimeTot)/TimeStep/tau_DRX), t_last = -1E3*tau_DRX*TimeStep
-    const double dt = c->m64.dt;
-    const double t_last = -1E3 * c->tau_drx * dt;
-    const double drx = c->delta_tau_drx * exp((t_last - time_tot) / dt / c->tau_drx);
-    k_macro_begin<<<1, 1, 0, c->stream>>>(c->macro, drx, 2. * c->cfg.err_tol);
-    c->launches++;
-    CK(cudaGetLastError());
-    CK(launch_begin(*c, u9, creep ? 1 : 0, g9, drx));
+    if (creep && !dgavg) return fail(EVPG_ERR_ARG, "creep needs disgrad_avg_actual");
+    // the staging area may still feed an earlier copy
+    CK(cudaStreamSynchronize(c->stream));
+    stage_ctl(c, udot_dt, creep, dgavg, time_tot, 0.0, 0);
+    CK(cudaMemcpyAsync(c->macro, c->ctl_host, sizeof(IncrCtl), cudaMemcpyHostToDevice, c->stream));
+    CK(launch_macro_begin(*c, GATE_BEGIN));
+    CK(launch_begin(*c, GATE_BEGIN));
+    CK(launch_phase(*c, PH_BEGIN, PH_RUNNING));
     return EVPG_OK;
 }
 
@@ -597,11 +643,14 @@ int evpg_equilibrium_solve(void* ctx, double e_vm, evpg_iter_out* out) {
 int evpg_increment_end(void* ctx, int32_t reorient, evpg_incr_out* out) {
     Ctx* c = (Ctx*)ctx;
     if (!c) return fail(EVPG_ERR_ARG, "null context");
+    k_set_reorient<<<1, 1, 0, c->stream>>>(c->macro, reorient ? 1 : 0);
+    c->launches++;
     if (c->precision == EVPG_FP32_BULK) {
-        CK(launch_fold(*c));
-        CK(launch_nr(*c, 1));
+        CK(launch_fold(*c, GATE_ALWAYS));
+        CK(launch_nr(*c, 1, GATE_ALWAYS));
     }
-    CK(launch_end(*c, reorient ? 1 : 0));
+    CK(launch_end(*c, GATE_ALWAYS));
+    CK(launch_phase(*c, PH_RUNNING, PH_ENDED));
     int st = read_macro(c);
     if (st) return st;
     const Macro& m = *c->macro_host;
@@ -615,6 +664,41 @@ int evpg_increment_end(void* ctx, int32_t reorient, evpg_incr_out* out) {
         out->nr_iterations = m.nr_iters;
     }
     if (m.status) return fail(m.status, "%s", evpg_status_string(m.status));
+    return EVPG_OK;
+}
+
+int evpg_set_load(void* ctx, const int32_t velgrad_bc_flag[6], const int32_t stress_bc_flag[6],
+                  const double scauchy[3][3], const double udot_a[3][3]) {
+    Ctx* c = (Ctx*)ctx;
+    if (!c || !velgrad_bc_flag || !stress_bc_flag || !scauchy || !udot_a)
+        return fail(EVPG_ERR_ARG, "null argument");
+    for (int i = 0; i < 6; i++)
+        if (velgrad_bc_flag[i] * stress_bc_flag[i] != 0 || velgrad_bc_flag[i] + stress_bc_flag[i] != 1)
+            return fail(EVPG_ERR_ARG, "component %d: exactly one of velocity gradient and stress is prescribed", i);
+    CK(cudaStreamSynchronize(c->stream));
+    for (int i = 0; i < 6; i++) {
+        c->cfg.vflag[i] = velgrad_bc_flag[i];
+        c->cfg.sflag[i] = stress_bc_flag[i];
+    }
+    memcpy(c->cfg.scauchy, scauchy, sizeof c->cfg.scauchy);
+    memcpy(c->udot_a, udot_a, sizeof c->udot_a);
+    build_sets(*c);
+    c->version++;
+    return EVPG_OK;
+}
+
+int evpg_estimate_bytes(const int32_t n[3], int32_t precision, int32_t n_orient, int64_t* bytes) {
+    if (!n || !bytes || n[0] < 1 || n[1] < 1 || n[2] < 1) return fail(EVPG_ERR_ARG, "bad argument");
+    const long long N = (long long)n[0] * n[1] * n[2];
+    const long long Nh = (long long)n[0] * n[1] * (n[2] / 2 + 1);
+    const long long no = n_orient > 0 ? n_orient : 1;
+    const long long nb_nr = (N + NR_BLOCK - 1) / NR_BLOCK, nb_end = (N + END_BLOCK - 1) / END_BLOCK;
+    long long b = 8 * N * (6 + 9 + 9 + 6 + 5 + 12 + 12 + 12 + 12 + 9 + 60 + 48) + 8 * 36 * no + 4 * 2 * N;
+    if (precision == EVPG_FP32_BULK) b += 4 * N * (6 + 9 + 6 + 60 + 48) + 4 * 36 * no + 8 * 9 * Nh;
+    else b += 16 * 9 * Nh;
+    b += 8 * nb_nr * (NR_BLOCK / 32) * NPART_NR + 8 * MACRO_BLOCKS * NPART_NR + 4 + 8 * nb_end * NPART_END;
+    b += (long long)sizeof(Macro) + 24LL * (n[0] + n[1] + n[2]);
+    *bytes = b;
     return EVPG_OK;
 }
 

@@ -1,0 +1,197 @@
+// Launch arguments of every kernel of the equilibrium iteration and of the
+// increment head and tail. One set per RVE context is built when the context
+// is created; a single-RVE launch passes it by value (__grid_constant__), a
+// batched launch reads the set of each RVE from a device table.
+#pragma once
+#include "evpg_common.cuh"
+
+namespace evpg {
+
+constexpr int NPART_NR = 15;   // err_e, err_s, sig6 sum, sig6 phase-1 sum, NR iterations
+constexpr int NPART_END = 18;  // rho_F, rho_P, rho_s, rho_m, d_dipole, d_forest, d_inplane,
+                               // Eps (6), Edot (5)
+constexpr int NR_BLOCK = 128;
+constexpr int MACRO_BLOCKS = 64;
+constexpr int END_BLOCK = 128;
+constexpr int SPEC_THREADS = 256;
+
+// Which RVEs a launch works on, decided on the device from the RVE's Macro:
+//   GATE_ALWAYS   every launch
+//   GATE_RUNNING  the equilibrium loop of the increment is running and not done
+//   GATE_ENDING   the loop finished without error and the tail has not run yet
+//   GATE_BEGIN    a new increment was requested (IncrCtl.phase == 1)
+enum Gate { GATE_ALWAYS = 0, GATE_RUNNING = 1, GATE_ENDING = 2, GATE_BEGIN = 3 };
+
+// IncrCtl.phase
+enum SlotPhase { PH_IDLE = 0, PH_BEGIN = 1, PH_RUNNING = 2, PH_ENDED = 3 };
+
+__device__ __forceinline__ bool gate_open(const Macro* m, int gate) {
+    switch (gate) {
+        case GATE_RUNNING: return m->ctl.phase == PH_RUNNING && !m->done;
+        case GATE_ENDING: return m->ctl.phase == PH_RUNNING && m->done && m->status == 0;
+        case GATE_BEGIN: return m->ctl.phase == PH_BEGIN;
+        default: return true;
+    }
+}
+
+template <typename T> struct GreenK {
+    T c0[3][3][3][3];
+    T s0[3][3][3][3];
+    int elast_bc;
+};
+
+template <typename T> struct ZArgs {
+    Grid g;
+    FftPlan pl;
+    const Macro* macro;
+    int gate;
+    const T* sig;        // [6][N] real
+    T* dg;               // [9][N] real (inverse pass)
+    C2<T>* spec;         // [9][Nh]
+    const C2<T>* tw;
+    const double* dE9;   // macro correction added in the inverse pass
+    int P;
+    T invN;
+};
+
+template <typename T> struct YArgs {
+    Grid g;
+    FftPlan pl;
+    const Macro* macro;
+    int gate;
+    C2<T>* spec;
+    const C2<T>* tw;
+    int ncomp, P;
+};
+
+template <typename T> struct XArgs {
+    Grid g;
+    FftPlan pl;
+    const Macro* macro;
+    int gate;
+    C2<T>* spec;
+    const C2<T>* tw;
+    int P;
+    GreenK<T> gk;
+};
+
+template <typename T> struct NrArgs {
+    Material<T> mat;
+    Grid g;
+    T* sig;               // [6][N] lambda in, sigma out
+    const T* dg;          // [9][N] strain source ([0..5] used)
+    const T* epsb;        // [6][N] a = epsb - dg: Eps (FP64) or Eps - eps_begin (FP32)
+    const T* schm;        // [60][N]
+    const T* fc;          // [48][N]
+    const int32_t* orient;
+    const int32_t* phase;
+    const T* sgr;         // [n_orient][36]
+    T* edot;              // [5][N] or null
+    T* gamdot;            // [12][N] or null
+    Macro* macro;
+    double* part;         // [warps][NPART_NR]
+    T tol;
+    int itmax, nr_mode;
+    int stale_mode;       // 1: the first flow-rule call of the increment uses the stored rho_m
+    int gate;
+};
+
+struct MacroArgs {
+    LoopCfg cfg;
+    Macro* macro;
+    const double* part;   // [nrows][NPART_NR] warp partials of the NR sweep
+    int nrows;
+    double* part2;        // [MACRO_BLOCKS][NPART_NR]
+    unsigned int* ticket; // last-block detection, reset by the last block
+};
+
+struct BeginArgs {
+    Material<double> mat;
+    Grid g;
+    Macro* macro;        // increment controls (udot, creep, drx) in macro->ctl
+    int gate;
+    double* dg64;        // [9][N]
+    double* dg_old;      // [9][N]
+    const double* tranmat;
+    const double* rho_s;
+    const double* rho_m;
+    const int32_t* phase;
+    double* schm64;      // [60][N]
+    double* fc64;        // [48][N]
+    // FP32 bulk
+    float* schm32;
+    float* fc32;
+    float* b6_32;
+    float* ddg32;
+    const double* epsp;
+};
+
+struct FoldArgs {
+    Grid g;
+    const Macro* macro;
+    int gate;
+    double* dg64;
+    const float* ddg32;
+    double* sig64;
+    const float* sig32;
+};
+
+struct EndArgs {
+    Material<double> mat;
+    Grid g;
+    const Macro* macro;   // reorient flag in macro->ctl
+    int gate;
+    double udot_a[3][3];
+    double* dg_old;       // in: DisGrad at increment start; out: VelGrad
+    const double* dg64;
+    double* epsp;
+    const double* edot;
+    double* tranmat;
+    double* rho_s;
+    double* rho_m;
+    const double* gamdot;
+    double* gam_acum;
+    const double* sig64;
+    const double* schm64;
+    const int32_t* phase;
+    float* sig32;         // FP32 bulk: next increment starts from the refined stress
+    double* part;
+};
+
+struct EndReduceArgs {
+    Macro* macro;
+    int gate;
+    const double* part;
+    int nblocks;
+    double wgt;
+};
+
+// Everything one RVE context launches, with grid sizes and dynamic shared
+// memory, in the context's working precision T.
+template <typename T> struct SpecSet {
+    ZArgs<T> z;
+    YArgs<T> yf, yi;
+    XArgs<T> x;
+    int grid_z, grid_y, grid_x;
+    size_t sm_z, sm_y, sm_x;
+};
+
+template <typename T> struct NrSet {
+    NrArgs<T> a;
+    int grid;
+};
+
+struct KernelSets {
+    SpecSet<double> s64;
+    SpecSet<float> s32;
+    NrSet<double> nr64;   // loop sweep (FP64 form) or refinement (FP32 bulk)
+    NrSet<float> nr32;    // loop sweep (FP32 bulk)
+    MacroArgs mac;
+    BeginArgs beg;
+    FoldArgs fold;
+    EndArgs end;
+    EndReduceArgs endr;
+    int grid_begin, grid_fold, grid_end;
+};
+
+}  // namespace evpg

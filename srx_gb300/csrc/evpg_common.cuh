@@ -85,8 +85,23 @@ template <typename T> struct Material {
     int elast_bc;
 };
 
+// Controls of the next increment, written by the host (one stream-ordered
+// copy) before the increment head runs.
+struct IncrCtl {
+    double udot9[9];    // applied Udot*dt in the field representation
+    double dgavg9[9];   // uniform DisGrad for creep
+    double drx;         // DeltaTau_DRX*exp(...) of this increment
+    double e_vm;        // strain-error normaliser of this increment
+    double err0;        // initial error value (2*Err)
+    int creep;
+    int reorient;       // update_orient in the increment tail
+    int phase;          // 0 idle, 1 begin requested, 2 running, 3 ended
+    int pad;
+};
+
 // Device-resident macro state of the equilibrium loop (always FP64).
 struct Macro {
+    IncrCtl ctl;
     double dE[3][3];        // dDisGradAvg of the last iteration (upper triangle)
     double dE9[9];          // the same in the field representation (B basis + A12,A13,A23)
     double dE_acum[3][3];   // dDisGradAvg_acum

@@ -3,16 +3,9 @@
 #include <cuda_runtime.h>
 #include <stddef.h>
 #include <stdint.h>
-#include "evpg_common.cuh"
+#include "evpg_args.h"
 
 namespace evpg {
-
-constexpr int NPART_NR = 15;   // err_e, err_s, sig6 sum, sig6 phase-1 sum, NR iterations
-constexpr int NPART_END = 18;  // rho_F, rho_P, rho_s, rho_m, d_dipole, d_forest, d_inplane,
-                               // Eps (6), Edot (5)
-constexpr int NR_BLOCK = 128;
-constexpr int MACRO_BLOCKS = 64;
-constexpr int END_BLOCK = 128;
 
 // Kernel groups timed by the optional profiler (CUDA events on the context's
 // stream around each launch).
@@ -53,6 +46,12 @@ struct Ctx {
     int nb_end;
     Macro* macro;       // device
     Macro* macro_host;  // pinned mirror
+    IncrCtl* ctl_host;  // pinned staging of the next increment's controls
+    KernelSets* ks;     // launch arguments of every kernel (built at creation)
+    int sched_p[3];     // pencils per CTA of the z, y, x passes (0: default)
+    int nsm;            // SM count of the device
+    long long version;  // bumped whenever ks changes (batches refresh their tables)
+    void* solo;         // batch of this context alone (evpg_increment's round graph)
     LoopCfg cfg;
     Material<double> m64;
     Material<float> m32;
@@ -77,15 +76,56 @@ template <typename T> inline const Material<T>& material_of(const Ctx& c);
 template <> inline const Material<double>& material_of<double>(const Ctx& c) { return c.m64; }
 template <> inline const Material<float>& material_of<float>(const Ctx& c) { return c.m32; }
 
+// Fill c.ks from the allocated context (pencils per CTA, grids, shared memory).
+void build_sets(Ctx& c);
+void build_spectral_sets(Ctx& c);
+void build_solver_sets(Ctx& c);
+// Largest and default pencils per CTA of the z, y, x passes.
+void spec_pmax(const Grid& g, size_t elem_bytes, int pmax[3]);
+void spec_default_p(const Grid& g, size_t elem_bytes, int nsm, int P[3]);
+// Message of the last error on this host thread (evpg_last_error); returns st.
+int record_error(int st, const char* msg);
+// Release the context's own round graph.
+void free_solo(Ctx& c);
+// Set the kernels' dynamic shared-memory limits (once per device).
+void set_kernel_attributes();
+void spectral_attributes();
+void solver_attributes();
+
+// One batched launch: the per-RVE argument table (device), the CTA map
+// (device, map[b] = (slot, CTA index within the slot)), the CTA count and the
+// dynamic shared memory (maximum over the slots).
+struct BatchLaunch {
+    const void* tab;
+    const int2* map;
+    int nblk;
+    size_t smem;
+};
+enum BatchKind { BL_Z, BL_YF, BL_X, BL_YI, BL_NR, BL_MACRO, BL_MBEGIN, BL_BEGIN, BL_FOLD,
+                 BL_REFINE, BL_END, BL_ENDR, BL_COUNT };
+cudaError_t launch_spectral_batch(int precision, const BatchLaunch* L, cudaStream_t st);
+// NR sweep, macro update for every slot
+cudaError_t launch_nr_batch(int precision, int nr_mode, const BatchLaunch& L, cudaStream_t st);
+cudaError_t launch_macro_batch(const BatchLaunch& L, cudaStream_t st);
+// increment head (macro reset + k_begin), gated per slot
+cudaError_t launch_begin_batch(const BatchLaunch* L, cudaStream_t st);
+// increment tail (fold + FP64 refinement for FP32 bulk, k_end, k_end_reduce)
+cudaError_t launch_end_batch(int precision, int nr_mode, const BatchLaunch* L, cudaStream_t st);
+
+// Launchers of one RVE's kernels on its stream; `gate` selects when a launch
+// does work (Gate).
 // spectral chain of one iteration in the working precision
-cudaError_t launch_spectral(Ctx& c);
+cudaError_t launch_spectral(Ctx& c, int gate);
 // NR sweep: refine = 0 inside the loop (working precision), 1 the FP64
 // refinement of the FP32-bulk form at the end of the loop
-cudaError_t launch_nr(Ctx& c, int refine);
+cudaError_t launch_nr(Ctx& c, int refine, int gate);
 cudaError_t launch_macro(Ctx& c);
-cudaError_t launch_begin(Ctx& c, const double udot9[9], int creep, const double dgavg9[9],
-                         double drx);
-cudaError_t launch_fold(Ctx& c);
-cudaError_t launch_end(Ctx& c, int reorient);
+// reset of the macro state at the increment head (controls from macro->ctl)
+cudaError_t launch_macro_begin(Ctx& c, int gate);
+cudaError_t launch_begin(Ctx& c, int gate);
+cudaError_t launch_fold(Ctx& c, int gate);
+cudaError_t launch_end(Ctx& c, int gate);
+// macro->ctl.phase: from -> to (single thread)
+cudaError_t launch_phase(Ctx& c, int from, int to);
 
 }  // namespace evpg

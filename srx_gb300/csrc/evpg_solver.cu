@@ -83,26 +83,6 @@ __device__ __forceinline__ void set_status(Macro* m, int st) { atomicCAS(&m->sta
 
 // ------------------------------------------------------------------- NR
 
-template <typename T> struct NrArgs {
-    Material<T> mat;
-    Grid g;
-    T* sig;               // [6][N] lambda in, sigma out
-    const T* dg;          // [9][N] strain source ([0..5] used)
-    const T* epsb;        // [6][N] a = epsb - dg: Eps (FP64) or Eps - eps_begin (FP32)
-    const T* schm;        // [60][N]
-    const T* fc;          // [48][N]
-    const int32_t* orient;
-    const int32_t* phase;
-    const T* sgr;         // [n_orient][36]
-    T* edot;              // [5][N] or null
-    T* gamdot;            // [12][N] or null
-    Macro* macro;
-    double* part;         // [gridDim][NPART_NR]
-    T tol;
-    int itmax, nr_mode;
-    int stale_mode;       // 1: the first flow-rule call of the increment uses the stored rho_m
-    int check_done;
-};
 
 __device__ __forceinline__ void sinh_cosh(double x, double& sh, double& ch) {
     if (x < 700.0) {
@@ -282,12 +262,15 @@ template <> struct NrMinBlocks<float> { static constexpr int v = 4; };
 // point; a TRIAL step evaluates the flow rule there and accepts the point,
 // backtracks or gives up (evolution.c:337-370). An accepted trial's
 // evaluation is the next MAIN's evaluation.
-template <typename T, int LS>
-__global__ void __launch_bounds__(NR_BLOCK, NrMinBlocks<T>::v) k_nr(const __grid_constant__ NrArgs<T> a) {
-    extern __shared__ __align__(16) unsigned char nr_smem[];
+// B: batched launch (C066/S066 staged in shared memory at sS/sC); otherwise
+// they are read from the kernel's constant bank.
+template <typename T, int LS, bool B>
+__device__ __forceinline__ void nr_body(const NrArgs<T>& a, int bid, unsigned char* nr_smem,
+                                        const T* sS, const T* sC) {
     T* s_stage = reinterpret_cast<T*>(nr_smem);
-    if (a.check_done && a.macro->done) return;
-    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    const T(&S66)[6][6] = B ? *reinterpret_cast<const T(*)[6][6]>(sS) : a.mat.s066;
+    const T(&C66)[6][6] = B ? *reinterpret_cast<const T(*)[6][6]>(sC) : a.mat.c066;
+    const int v = bid * NR_BLOCK + threadIdx.x;
     const int N = a.g.N;
     const T dt = a.mat.dt;
     T* stg = s_stage + threadIdx.x;
@@ -354,7 +337,7 @@ __global__ void __launch_bounds__(NR_BLOCK, NrMinBlocks<T>::v) k_nr(const __grid
                 for (int i = 0; i < 6; i++)
 #pragma unroll
                     for (int j = i; j < 6; j++)
-                        m[sidx(i, j)] = a.mat.s066[i][j] + (T)0.5 * (__ldg(sg + i * 6 + j) + __ldg(sg + j * 6 + i));
+                        m[sidx(i, j)] = S66[i][j] + (T)0.5 * (__ldg(sg + i * 6 + j) + __ldg(sg + j * 6 + i));
                 {
                     int k = 0;
 #pragma unroll
@@ -365,7 +348,7 @@ __global__ void __launch_bounds__(NR_BLOCK, NrMinBlocks<T>::v) k_nr(const __grid
                 T dl[6], rhs[6];
 #pragma unroll
                 for (int c = 0; c < 6; c++) dl[c] = sig[c] - lam[c];
-                mat6v<T>(a.mat.s066, dl, rhs);
+                mat6v<T>(S66, dl, rhs);
 #pragma unroll
                 for (int c = 0; c < 6; c++) rhs[c] += te[c];
                 if (!ldl_solve<T>(m, rhs, step)) { sing = true; break; }
@@ -379,7 +362,7 @@ __global__ void __launch_bounds__(NR_BLOCK, NrMinBlocks<T>::v) k_nr(const __grid
                     // factor; used directly because through an ill-conditioned J
                     // the rounded product can change sign.
                     T CR[6];
-                    mat6v<T>(a.mat.c066, te, CR);
+                    mat6v<T>(C66, te, CR);
                     f_old = 0;
 #pragma unroll
                     for (int c = 0; c < 6; c++) {
@@ -426,7 +409,7 @@ __global__ void __launch_bounds__(NR_BLOCK, NrMinBlocks<T>::v) k_nr(const __grid
                 sgr_v<T>(sg, sig, Ss);
 #pragma unroll
                 for (int c = 0; c < 6; c++) tt6[c] = av[c] + (c < 5 ? ed[c] * dt : (T)0) + Ss[c];
-                mat6v<T>(a.mat.c066, tt6, Rt);
+                mat6v<T>(C66, tt6, Rt);
 #pragma unroll
                 for (int c = 0; c < 6; c++) {
                     const T r = sig[c] - lam[c] + Rt[c];
@@ -489,7 +472,7 @@ __global__ void __launch_bounds__(NR_BLOCK, NrMinBlocks<T>::v) k_nr(const __grid
                     T d6[6], q6[6];
 #pragma unroll
                     for (int c = 0; c < 6; c++) d6[c] = sig[c] - lam[c];
-                    mat6v<T>(a.mat.s066, d6, q6);
+                    mat6v<T>(S66, d6, q6);
                     ce = 0;
 #pragma unroll
                     for (int c = 0; c < 6; c++) ce += q6[c] * q6[c];
@@ -526,20 +509,35 @@ __global__ void __launch_bounds__(NR_BLOCK, NrMinBlocks<T>::v) k_nr(const __grid
         q[8 + c] = s1[c];
     }
     q[14] = (T)nr;
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int warp = (bid * NR_BLOCK + threadIdx.x) >> 5;
     warp_store(q, a.part + (size_t)warp * NPART_NR);
+}
+
+template <typename T, int LS>
+__global__ void __launch_bounds__(NR_BLOCK, NrMinBlocks<T>::v) k_nr(const __grid_constant__ NrArgs<T> a) {
+    extern __shared__ __align__(16) unsigned char nr_smem[];
+    if (!gate_open(a.macro, a.gate)) return;
+    nr_body<T, LS, false>(a, blockIdx.x, nr_smem, nullptr, nullptr);
+}
+
+template <typename T, int LS>
+__global__ void __launch_bounds__(NR_BLOCK, NrMinBlocks<T>::v) kb_nr(const NrArgs<T>* __restrict__ tab,
+                                                                     const int2* __restrict__ map) {
+    extern __shared__ __align__(16) unsigned char nr_smem[];
+    const int2 m = map[blockIdx.x];
+    const NrArgs<T>& a = tab[m.x];
+    if (!gate_open(a.macro, a.gate)) return;
+    T* sm = reinterpret_cast<T*>(nr_smem) + (NSTAGE + NS) * NR_BLOCK;
+    for (int i = threadIdx.x; i < 36; i += NR_BLOCK) {
+        sm[i] = (&a.mat.s066[0][0])[i];
+        sm[36 + i] = (&a.mat.c066[0][0])[i];
+    }
+    __syncthreads();
+    nr_body<T, LS, true>(a, m.y, nr_smem, sm, sm + 36);
 }
 
 // ---------------------------------------------------------------- macro
 
-struct MacroArgs {
-    LoopCfg cfg;
-    Macro* macro;
-    const double* part;   // [nrows][NPART_NR] warp partials of the NR sweep
-    int nrows;
-    double* part2;        // [gridDim][NPART_NR]
-    unsigned int* ticket; // last-block detection, reset by the last block
-};
 
 // get_smacro and the loop test (evolution.c:590-664, 1227-1252, 1150) on the
 // FP64 totals; thread 0 of the last block.
@@ -621,13 +619,14 @@ __device__ void macro_update(const LoopCfg& c, Macro* m, const double* tot) {
 // Deterministic two-level sum of the NR warp partials: each block sums a
 // contiguous range of rows in a fixed order; the last block to finish sums
 // the block rows in order and runs the macro update.
-__global__ void __launch_bounds__(256) k_macro(const __grid_constant__ MacroArgs a) {
+// bid: block index within the RVE's MACRO_BLOCKS blocks.
+__device__ __forceinline__ void macro_body(const MacroArgs& a, int bid) {
     Macro* m = a.macro;
-    if (m->done) return;
     __shared__ double red[NPART_NR][8];
     __shared__ bool last;
-    const int per = (a.nrows + gridDim.x - 1) / gridDim.x;
-    const int r0 = blockIdx.x * per, r1 = min(a.nrows, r0 + per);
+    const int nb = MACRO_BLOCKS;
+    const int per = (a.nrows + nb - 1) / nb;
+    const int r0 = bid * per, r1 = min(a.nrows, r0 + per);
     double v[NPART_NR];
 #pragma unroll
     for (int q = 0; q < NPART_NR; q++) v[q] = 0.0;
@@ -646,11 +645,11 @@ __global__ void __launch_bounds__(256) k_macro(const __grid_constant__ MacroArgs
     if (threadIdx.x < NPART_NR) {
         double s = 0.0;
         for (int w = 0; w < (int)(blockDim.x >> 5); w++) s += red[threadIdx.x][w];
-        a.part2[(size_t)blockIdx.x * NPART_NR + threadIdx.x] = s;
+        a.part2[(size_t)bid * NPART_NR + threadIdx.x] = s;
     }
     __threadfence();
     __syncthreads();
-    if (threadIdx.x == 0) last = (atomicAdd(a.ticket, 1u) == gridDim.x - 1);
+    if (threadIdx.x == 0) last = (atomicAdd(a.ticket, 1u) == (unsigned)nb - 1);
     __syncthreads();
     if (!last) return;
     __threadfence();
@@ -658,7 +657,7 @@ __global__ void __launch_bounds__(256) k_macro(const __grid_constant__ MacroArgs
     __shared__ double tot[NPART_NR];
     if (threadIdx.x < NPART_NR) {
         double s = 0.0;
-        for (int b = 0; b < (int)gridDim.x; b++) s += __ldcg(a.part2 + (size_t)b * NPART_NR + threadIdx.x);
+        for (int b = 0; b < nb; b++) s += __ldcg(a.part2 + (size_t)b * NPART_NR + threadIdx.x);
         tot[threadIdx.x] = s;
     }
     __syncthreads();
@@ -668,42 +667,69 @@ __global__ void __launch_bounds__(256) k_macro(const __grid_constant__ MacroArgs
     }
 }
 
+__global__ void __launch_bounds__(256) k_macro(const __grid_constant__ MacroArgs a) {
+    if (a.macro->done) return;
+    macro_body(a, blockIdx.x);
+}
+
+__global__ void __launch_bounds__(256) kb_macro(const MacroArgs* __restrict__ tab, const int2* __restrict__ map) {
+    const int2 m = map[blockIdx.x];
+    const MacroArgs& a = tab[m.x];
+    if (a.macro->done) return;
+    macro_body(a, m.y);
+}
+
+// Increment head, first step: reset the macro state from the controls the
+// host wrote into macro->ctl (one thread per RVE).
+__device__ __forceinline__ void macro_begin(Macro* m) {
+    const IncrCtl& c = m->ctl;
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) {
+            m->dE[i][j] = 0.0;
+            m->dE_acum[i][j] = 0.0;
+        }
+    for (int q = 0; q < 9; q++) m->dE9[q] = 0.0;
+    m->err_e = c.err0;
+    m->err_s = c.err0;
+    m->iter = 0;
+    m->done = 0;
+    m->converged = 0;
+    m->status = 0;
+    m->nr_iters = 0;
+    m->tpass_drx = c.drx;
+    m->e_vm = c.e_vm;
+}
+
+__global__ void k_macro_begin(Macro* m, int gate) {
+    if (threadIdx.x == 0 && gate_open(m, gate)) macro_begin(m);
+}
+
+__global__ void kb_macro_begin(Macro* const* __restrict__ ms, int n, int gate) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && gate_open(ms[i], gate)) macro_begin(ms[i]);
+}
+
+__global__ void k_phase(Macro* m, int from, int to) {
+    if (threadIdx.x == 0 && m->ctl.phase == from) m->ctl.phase = to;
+}
+
 // ------------------------------------------------------ increment head
 
-struct BeginArgs {
-    Material<double> mat;
-    Grid g;
-    double udot9[9];     // applied Udot*dt in the field representation
-    double dgavg9[9];    // uniform DisGrad for creep
-    int creep;
-    double drx;          // DeltaTau_DRX*exp(...) of this increment
-    double* dg64;        // [9][N]
-    double* dg_old;      // [9][N]
-    const double* tranmat;
-    const double* rho_s;
-    const double* rho_m;
-    const int32_t* phase;
-    double* schm64;      // [60][N]
-    double* fc64;        // [48][N]
-    // FP32 bulk
-    float* schm32;
-    float* fc32;
-    float* b6_32;
-    float* ddg32;
-    const double* epsp;
-};
 
 // update_schmid (kinematics.c:430-463) and the rho-dependent products of the
 // flow rule that stay fixed during an increment (constitutive.c:559-633).
-__global__ void __launch_bounds__(128) k_begin(const __grid_constant__ BeginArgs a) {
-    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void begin_body(const BeginArgs& a, int bid) {
+    const int v = bid * 128 + threadIdx.x;
     const int N = a.g.N;
     if (v >= N) return;
+    const IncrCtl& ctl = a.macro->ctl;
+    const int creep = ctl.creep;
+    const double drx = ctl.drx;
 #pragma unroll
     for (int c = 0; c < 9; c++) {
         const double d = a.dg64[(size_t)c * N + v];
         a.dg_old[(size_t)c * N + v] = d;
-        a.dg64[(size_t)c * N + v] = a.creep ? a.dgavg9[c] : d + a.udot9[c];
+        a.dg64[(size_t)c * N + v] = creep ? ctl.dgavg9[c] : d + ctl.udot9[c];
     }
     const int ph = a.phase[v];
     const PhaseK<double>& P = a.mat.ph[ph - 1];
@@ -755,8 +781,8 @@ __global__ void __launch_bounds__(128) k_begin(const __grid_constant__ BeginArgs
         }
         const double rm_stale = a.rho_m[(size_t)i * N + v];
         const double rm = P.k_rhom[i] * sqrt(rP * rf);
-        const double tp = P.k_tpass[i] * sqrt(fabs(rP + rm)) + a.drx;
-        const double tps = P.k_tpass[i] * sqrt(fabs(rP + rm_stale)) + a.drx;
+        const double tp = P.k_tpass[i] * sqrt(fabs(rP + rm)) + drx;
+        const double tps = P.k_tpass[i] * sqrt(fabs(rP + rm_stale)) + drx;
         const double itc = 1.0 / (P.tau0 + P.k_tcut[i] * sqrt(rf));
         const double go = P.k_gamo[i] * rm / sqrt(rf);
         const double f4[4] = {tp, itc, go, tps};
@@ -768,18 +794,23 @@ __global__ void __launch_bounds__(128) k_begin(const __grid_constant__ BeginArgs
     }
 }
 
+__global__ void __launch_bounds__(128) k_begin(const __grid_constant__ BeginArgs a) {
+    if (!gate_open(a.macro, a.gate)) return;
+    begin_body(a, blockIdx.x);
+}
+
+__global__ void __launch_bounds__(128) kb_begin(const BeginArgs* __restrict__ tab, const int2* __restrict__ map) {
+    const int2 m = map[blockIdx.x];
+    const BeginArgs& a = tab[m.x];
+    if (!gate_open(a.macro, a.gate)) return;
+    begin_body(a, m.y);
+}
+
 // FP32 bulk: fold the FP32 displacement-gradient increment into the FP64
 // field and seed the FP64 refinement with the FP32 stress.
-struct FoldArgs {
-    Grid g;
-    double* dg64;
-    const float* ddg32;
-    double* sig64;
-    const float* sig32;
-};
 
-__global__ void k_fold(const __grid_constant__ FoldArgs a) {
-    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void fold_body(const FoldArgs& a, int bid) {
+    const int v = bid * 256 + threadIdx.x;
     const int N = a.g.N;
     if (v >= N) return;
 #pragma unroll
@@ -788,28 +819,20 @@ __global__ void k_fold(const __grid_constant__ FoldArgs a) {
     for (int c = 0; c < 6; c++) a.sig64[(size_t)c * N + v] = (double)a.sig32[(size_t)c * N + v];
 }
 
+__global__ void __launch_bounds__(256) k_fold(const __grid_constant__ FoldArgs a) {
+    if (!gate_open(a.macro, a.gate)) return;
+    fold_body(a, blockIdx.x);
+}
+
+__global__ void __launch_bounds__(256) kb_fold(const FoldArgs* __restrict__ tab, const int2* __restrict__ map) {
+    const int2 m = map[blockIdx.x];
+    const FoldArgs& a = tab[m.x];
+    if (!gate_open(a.macro, a.gate)) return;
+    fold_body(a, m.y);
+}
+
 // ------------------------------------------------------ increment tail
 
-struct EndArgs {
-    Material<double> mat;
-    Grid g;
-    double udot_a[3][3];
-    int reorient;
-    double* dg_old;       // in: DisGrad at increment start; out: VelGrad
-    const double* dg64;
-    double* epsp;
-    const double* edot;
-    double* tranmat;
-    double* rho_s;
-    double* rho_m;
-    const double* gamdot;
-    double* gam_acum;
-    const double* sig64;
-    const double* schm64;
-    const int32_t* phase;
-    float* sig32;         // FP32 bulk: next increment starts from the refined stress
-    double* part;
-};
 
 // Orientation (constitutive.c:142-194): Rodrigues-type update of R by the
 // rotation increment rot (the reference drops rotations below 1e-6 by
@@ -833,8 +856,9 @@ __device__ void reorient(double tran[3][3], const double rot[3][3]) {
         for (int j = 0; j < 3; j++) tran[i][j] = tn[i][j];
 }
 
-__global__ void __launch_bounds__(END_BLOCK) k_end(const __grid_constant__ EndArgs a) {
-    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void end_body(const EndArgs& a, int bid) {
+    const int v = bid * END_BLOCK + threadIdx.x;
+    const int reorient_on = a.macro->ctl.reorient;
     const int N = a.g.N;
     const double dt = a.mat.dt;
     double q[NPART_END];
@@ -869,7 +893,7 @@ __global__ void __launch_bounds__(END_BLOCK) k_end(const __grid_constant__ EndAr
             double gd[NS];
 #pragma unroll
             for (int i = 0; i < NS; i++) gd[i] = (i < P.n_sys) ? a.gamdot[(size_t)i * N + v] : 0.0;
-            if (a.reorient) {
+            if (reorient_on) {
                 // update_orient (constitutive.c:196-273)
                 double tr[3][3], Lp[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, rot[3][3];
                 for (int i = 0; i < 3; i++)
@@ -941,19 +965,25 @@ __global__ void __launch_bounds__(END_BLOCK) k_end(const __grid_constant__ EndAr
             }
         }
     }
-    block_reduce_store<NPART_END>(q, a.part + (size_t)blockIdx.x * NPART_END);
+    block_reduce_store<NPART_END>(q, a.part + (size_t)bid * NPART_END);
 }
 
-struct EndReduceArgs {
-    Macro* macro;
-    const double* part;
-    int nblocks;
-    double wgt;
-};
+__global__ void __launch_bounds__(END_BLOCK) k_end(const __grid_constant__ EndArgs a) {
+    if (!gate_open(a.macro, a.gate)) return;
+    end_body(a, blockIdx.x);
+}
+
+__global__ void __launch_bounds__(END_BLOCK) kb_end(const EndArgs* __restrict__ tab, const int2* __restrict__ map) {
+    const int2 m = map[blockIdx.x];
+    const EndArgs& a = tab[m.x];
+    if (!gate_open(a.macro, a.gate)) return;
+    end_body(a, m.y);
+}
+
 
 // AvgDislocation (constitutive.c:1681-1808) and <Eps>, <Edot>
 // (evolution.c:1307-1323), in the B basis.
-__global__ void __launch_bounds__(256) k_end_reduce(const __grid_constant__ EndReduceArgs a) {
+__device__ __forceinline__ void end_reduce_body(const EndReduceArgs& a) {
     double v[NPART_END];
 #pragma unroll
     for (int q = 0; q < NPART_END; q++) v[q] = 0.0;
@@ -983,103 +1013,192 @@ __global__ void __launch_bounds__(256) k_end_reduce(const __grid_constant__ EndR
     m->edot_avg6[5] = 0.0;
 }
 
+__global__ void __launch_bounds__(256) k_end_reduce(const __grid_constant__ EndReduceArgs a) {
+    if (!gate_open(a.macro, a.gate)) return;
+    end_reduce_body(a);
+}
+
+// one block per RVE
+__global__ void __launch_bounds__(256) kb_end_reduce(const EndReduceArgs* __restrict__ tab) {
+    const EndReduceArgs& a = tab[blockIdx.x];
+    if (!gate_open(a.macro, a.gate)) return;
+    end_reduce_body(a);
+}
+
 // ------------------------------------------------------------- launchers
 
 template <typename T>
-static cudaError_t nr_t(Ctx& c, const Material<T>& mat, T* sig, const T* dg, const T* epsb,
-                        const T* schm, const T* fc, const T* sgr, T* edot, T* gamdot, T tol,
-                        int stale_mode, int check_done) {
-    NrArgs<T> a;
+static void nr_set(Ctx& c, NrSet<T>& S, const Material<T>& mat, T* sig, const T* dg, const T* epsb,
+                   const T* schm, const T* fc, const T* sgr, T* edot, T* gamdot, T tol, int stale_mode,
+                   int gate) {
+    NrArgs<T>& a = S.a;
     a.mat = mat;
     a.g = c.g;
     a.sig = sig; a.dg = dg; a.epsb = epsb; a.schm = schm; a.fc = fc;
     a.orient = c.orient; a.phase = c.phase; a.sgr = sgr; a.edot = edot; a.gamdot = gamdot;
     a.macro = c.macro; a.part = c.part_nr; a.tol = tol; a.itmax = c.nr_itmax;
-    a.nr_mode = c.nr_mode; a.stale_mode = stale_mode; a.check_done = check_done;
-    const int grp = check_done ? PG_NR : PG_REFINE;
-    prof_mark(c, grp, true);
-    const size_t sm = (size_t)(NSTAGE + NS) * NR_BLOCK * sizeof(T);
-    if (c.nr_mode) {
-        cudaFuncSetAttribute(k_nr<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        k_nr<T, 1><<<c.nb_nr, NR_BLOCK, sm, c.stream>>>(a);
+    a.nr_mode = c.nr_mode; a.stale_mode = stale_mode; a.gate = gate;
+    S.grid = c.nb_nr;
+}
+
+void build_solver_sets(Ctx& c) {
+    KernelSets& k = *c.ks;
+    if (c.precision == 0) {
+        nr_set<double>(c, k.nr64, c.m64, c.sig64, c.dg64, c.epsp, c.schm64, c.fc64, c.sgr64, c.edot64,
+                       c.gamdot64, (double)c.nr_tol64, 1, GATE_RUNNING);
     } else {
-        cudaFuncSetAttribute(k_nr<T, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        k_nr<T, 0><<<c.nb_nr, NR_BLOCK, sm, c.stream>>>(a);
+        // FP64 refinement at the end of the loop: no stale rho_m, runs once
+        nr_set<double>(c, k.nr64, c.m64, c.sig64, c.dg64, c.epsp, c.schm64, c.fc64, c.sgr64, c.edot64,
+                       c.gamdot64, (double)c.nr_tol64, 0, GATE_ENDING);
+        nr_set<float>(c, k.nr32, c.m32, c.sig32, c.ddg32, c.b6_32, c.schm32, c.fc32, c.sgr32, nullptr,
+                      nullptr, (float)c.nr_tol32, 1, GATE_RUNNING);
     }
+    MacroArgs& m = k.mac;
+    m.cfg = c.cfg; m.macro = c.macro; m.part = c.part_nr; m.nrows = c.nb_nr * (NR_BLOCK / 32);
+    m.part2 = c.part_nr2; m.ticket = c.ticket;
+    BeginArgs& b = k.beg;
+    b.mat = c.m64; b.g = c.g; b.macro = c.macro; b.gate = GATE_BEGIN;
+    b.dg64 = c.dg64; b.dg_old = c.dg_old; b.tranmat = c.tranmat; b.rho_s = c.rho_s;
+    b.rho_m = c.rho_m; b.phase = c.phase; b.schm64 = c.schm64; b.fc64 = c.fc64;
+    b.schm32 = c.schm32; b.fc32 = c.fc32; b.b6_32 = c.b6_32; b.ddg32 = c.ddg32; b.epsp = c.epsp;
+    k.grid_begin = (c.g.N + 127) / 128;
+    FoldArgs& f = k.fold;
+    f.g = c.g; f.macro = c.macro; f.gate = GATE_ENDING; f.dg64 = c.dg64; f.ddg32 = c.ddg32;
+    f.sig64 = c.sig64; f.sig32 = c.sig32;
+    k.grid_fold = (c.g.N + 255) / 256;
+    EndArgs& e = k.end;
+    e.mat = c.m64; e.g = c.g; e.macro = c.macro; e.gate = GATE_ENDING;
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) e.udot_a[i][j] = c.udot_a[i][j];
+    e.dg_old = c.dg_old; e.dg64 = c.dg64; e.epsp = c.epsp; e.edot = c.edot64;
+    e.tranmat = c.tranmat; e.rho_s = c.rho_s; e.rho_m = c.rho_m; e.gamdot = c.gamdot64;
+    e.gam_acum = c.gam_acum; e.sig64 = c.sig64; e.schm64 = c.schm64; e.phase = c.phase;
+    e.sig32 = c.sig32; e.part = c.part_end;
+    k.grid_end = c.nb_end;
+    EndReduceArgs& r = k.endr;
+    r.macro = c.macro; r.gate = GATE_ENDING; r.part = c.part_end; r.nblocks = c.nb_end; r.wgt = c.cfg.wgt;
+}
+
+template <typename T> static constexpr size_t nr_smem() { return (size_t)(NSTAGE + NS) * NR_BLOCK * sizeof(T); }
+template <typename T> static constexpr size_t nrb_smem() { return nr_smem<T>() + 72 * sizeof(T); }
+
+template <typename T> static void nr_attributes() {
+    cudaFuncSetAttribute(k_nr<T, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)nr_smem<T>());
+    cudaFuncSetAttribute(k_nr<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)nr_smem<T>());
+    cudaFuncSetAttribute(kb_nr<T, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)nrb_smem<T>());
+    cudaFuncSetAttribute(kb_nr<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)nrb_smem<T>());
+}
+
+void solver_attributes() {
+    nr_attributes<double>();
+    nr_attributes<float>();
+}
+
+template <typename T>
+static cudaError_t nr_launch(Ctx& c, const NrSet<T>& S, int gate, int grp) {
+    NrArgs<T> a = S.a;
+    a.gate = gate;
+    prof_mark(c, grp, true);
+    if (c.nr_mode) k_nr<T, 1><<<S.grid, NR_BLOCK, nr_smem<T>(), c.stream>>>(a);
+    else k_nr<T, 0><<<S.grid, NR_BLOCK, nr_smem<T>(), c.stream>>>(a);
     prof_mark(c, grp, false);
     return cudaGetLastError();
 }
 
-cudaError_t launch_nr(Ctx& c, int refine) {
-    if (c.precision == 0)
-        return nr_t<double>(c, c.m64, c.sig64, c.dg64, c.epsp, c.schm64, c.fc64, c.sgr64, c.edot64,
-                            c.gamdot64, (double)c.nr_tol64, 1, 1);
-    if (refine)
-        return nr_t<double>(c, c.m64, c.sig64, c.dg64, c.epsp, c.schm64, c.fc64, c.sgr64, c.edot64,
-                            c.gamdot64, (double)c.nr_tol64, 0, 0);
-    return nr_t<float>(c, c.m32, c.sig32, c.ddg32, c.b6_32, c.schm32, c.fc32, c.sgr32, nullptr,
-                       nullptr, (float)c.nr_tol32, 1, 1);
+cudaError_t launch_nr(Ctx& c, int refine, int gate) {
+    const KernelSets& k = *c.ks;
+    if (c.precision == 0) return nr_launch<double>(c, k.nr64, gate, PG_NR);
+    if (refine) return nr_launch<double>(c, k.nr64, gate, PG_REFINE);
+    return nr_launch<float>(c, k.nr32, gate, PG_NR);
 }
 
 cudaError_t launch_macro(Ctx& c) {
-    MacroArgs a;
-    a.cfg = c.cfg;
-    a.macro = c.macro;
-    a.part = c.part_nr;
-    a.nrows = c.nb_nr * (NR_BLOCK / 32);
-    a.part2 = c.part_nr2;
-    a.ticket = c.ticket;
     prof_mark(c, PG_MACRO, true);
-    k_macro<<<MACRO_BLOCKS, 256, 0, c.stream>>>(a);
+    k_macro<<<MACRO_BLOCKS, 256, 0, c.stream>>>(c.ks->mac);
     prof_mark(c, PG_MACRO, false);
     return cudaGetLastError();
 }
 
-cudaError_t launch_begin(Ctx& c, const double udot9[9], int creep, const double dgavg9[9],
-                         double drx) {
-    BeginArgs a;
-    a.mat = c.m64;
-    a.g = c.g;
-    for (int i = 0; i < 9; i++) {
-        a.udot9[i] = udot9[i];
-        a.dgavg9[i] = dgavg9[i];
-    }
-    a.creep = creep; a.drx = drx;
-    a.dg64 = c.dg64; a.dg_old = c.dg_old; a.tranmat = c.tranmat; a.rho_s = c.rho_s;
-    a.rho_m = c.rho_m; a.phase = c.phase; a.schm64 = c.schm64; a.fc64 = c.fc64;
-    a.schm32 = c.schm32; a.fc32 = c.fc32; a.b6_32 = c.b6_32; a.ddg32 = c.ddg32; a.epsp = c.epsp;
+cudaError_t launch_macro_begin(Ctx& c, int gate) {
+    c.launches++;
+    k_macro_begin<<<1, 32, 0, c.stream>>>(c.macro, gate);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_phase(Ctx& c, int from, int to) {
+    c.launches++;
+    k_phase<<<1, 32, 0, c.stream>>>(c.macro, from, to);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_begin(Ctx& c, int gate) {
+    BeginArgs a = c.ks->beg;
+    a.gate = gate;
     prof_mark(c, PG_BEGIN, true);
-    k_begin<<<(c.g.N + 127) / 128, 128, 0, c.stream>>>(a);
+    k_begin<<<c.ks->grid_begin, 128, 0, c.stream>>>(a);
     prof_mark(c, PG_BEGIN, false);
     return cudaGetLastError();
 }
 
-cudaError_t launch_fold(Ctx& c) {
-    FoldArgs a;
-    a.g = c.g; a.dg64 = c.dg64; a.ddg32 = c.ddg32; a.sig64 = c.sig64; a.sig32 = c.sig32;
+cudaError_t launch_fold(Ctx& c, int gate) {
+    FoldArgs a = c.ks->fold;
+    a.gate = gate;
     c.launches++;
-    k_fold<<<(c.g.N + 255) / 256, 256, 0, c.stream>>>(a);
+    k_fold<<<c.ks->grid_fold, 256, 0, c.stream>>>(a);
     return cudaGetLastError();
 }
 
-cudaError_t launch_end(Ctx& c, int reorient) {
-    EndArgs a;
-    a.mat = c.m64;
-    a.g = c.g;
-    for (int i = 0; i < 3; i++)
-        for (int j = 0; j < 3; j++) a.udot_a[i][j] = c.udot_a[i][j];
-    a.reorient = reorient;
-    a.dg_old = c.dg_old; a.dg64 = c.dg64; a.epsp = c.epsp; a.edot = c.edot64;
-    a.tranmat = c.tranmat; a.rho_s = c.rho_s; a.rho_m = c.rho_m; a.gamdot = c.gamdot64;
-    a.gam_acum = c.gam_acum; a.sig64 = c.sig64; a.schm64 = c.schm64; a.phase = c.phase;
-    a.sig32 = c.sig32; a.part = c.part_end;
+cudaError_t launch_end(Ctx& c, int gate) {
+    EndArgs a = c.ks->end;
+    a.gate = gate;
     prof_mark(c, PG_END, true);
-    k_end<<<c.nb_end, END_BLOCK, 0, c.stream>>>(a);
+    k_end<<<c.ks->grid_end, END_BLOCK, 0, c.stream>>>(a);
     prof_mark(c, PG_END, false);
-    EndReduceArgs r;
-    r.macro = c.macro; r.part = c.part_end; r.nblocks = c.nb_end; r.wgt = c.cfg.wgt;
+    EndReduceArgs r = c.ks->endr;
+    r.gate = gate;
     c.launches++;
     k_end_reduce<<<1, 256, 0, c.stream>>>(r);
+    return cudaGetLastError();
+}
+
+// ---- batched launchers (tables built by the batch; gates inside the tables)
+
+cudaError_t launch_nr_batch(int precision, int nr_mode, const BatchLaunch& L, cudaStream_t st) {
+    if (precision == 0) {
+        if (nr_mode) kb_nr<double, 1><<<L.nblk, NR_BLOCK, nrb_smem<double>(), st>>>((const NrArgs<double>*)L.tab, L.map);
+        else kb_nr<double, 0><<<L.nblk, NR_BLOCK, nrb_smem<double>(), st>>>((const NrArgs<double>*)L.tab, L.map);
+    } else {
+        if (nr_mode) kb_nr<float, 1><<<L.nblk, NR_BLOCK, nrb_smem<float>(), st>>>((const NrArgs<float>*)L.tab, L.map);
+        else kb_nr<float, 0><<<L.nblk, NR_BLOCK, nrb_smem<float>(), st>>>((const NrArgs<float>*)L.tab, L.map);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_macro_batch(const BatchLaunch& L, cudaStream_t st) {
+    kb_macro<<<L.nblk, 256, 0, st>>>((const MacroArgs*)L.tab, L.map);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_begin_batch(const BatchLaunch* L, cudaStream_t st) {
+    const BatchLaunch& mb = L[BL_MBEGIN];
+    kb_macro_begin<<<(mb.nblk + 127) / 128, 128, 0, st>>>((Macro* const*)mb.tab, mb.nblk, GATE_BEGIN);
+    const BatchLaunch& b = L[BL_BEGIN];
+    kb_begin<<<b.nblk, 128, 0, st>>>((const BeginArgs*)b.tab, b.map);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_end_batch(int precision, int nr_mode, const BatchLaunch* L, cudaStream_t st) {
+    if (precision != 0) {
+        const BatchLaunch& f = L[BL_FOLD];
+        kb_fold<<<f.nblk, 256, 0, st>>>((const FoldArgs*)f.tab, f.map);
+        const BatchLaunch& r = L[BL_REFINE];
+        if (nr_mode) kb_nr<double, 1><<<r.nblk, NR_BLOCK, nrb_smem<double>(), st>>>((const NrArgs<double>*)r.tab, r.map);
+        else kb_nr<double, 0><<<r.nblk, NR_BLOCK, nrb_smem<double>(), st>>>((const NrArgs<double>*)r.tab, r.map);
+    }
+    const BatchLaunch& e = L[BL_END];
+    kb_end<<<e.nblk, END_BLOCK, 0, st>>>((const EndArgs*)e.tab, e.map);
+    const BatchLaunch& er = L[BL_ENDR];
+    kb_end_reduce<<<er.nblk, 256, 0, st>>>((const EndReduceArgs*)er.tab);
     return cudaGetLastError();
 }
 

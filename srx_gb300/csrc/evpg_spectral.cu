@@ -4,61 +4,21 @@
 
 namespace evpg {
 
-template <typename T> struct GreenK {
-    T c0[3][3][3][3];
-    T s0[3][3][3][3];
-    int elast_bc;
-};
-
-template <typename T> struct ZArgs {
-    Grid g;
-    FftPlan pl;
-    const int* done;
-    const T* sig;        // [6][N] real
-    T* dg;               // [9][N] real (inverse pass)
-    C2<T>* spec;         // [9][Nh]
-    const C2<T>* tw;
-    const double* dE9;   // macro correction added in the inverse pass
-    int P;
-    T invN;
-};
-
-template <typename T> struct YArgs {
-    Grid g;
-    FftPlan pl;
-    const int* done;
-    C2<T>* spec;
-    const C2<T>* tw;
-    int ncomp, P;
-};
-
-template <typename T> struct XArgs {
-    Grid g;
-    FftPlan pl;
-    const int* done;
-    C2<T>* spec;
-    const C2<T>* tw;
-    int P;
-    GreenK<T> gk;
-};
-
 template <typename T>
 __device__ __forceinline__ void load_tw(C2<T>* tw, const C2<T>* src, int n) {
     for (int i = threadIdx.x; i < n; i += blockDim.x) tw[i] = src[i];
 }
 
 // Forward z: three complex FFTs of (sig[2p] + i sig[2p+1]) per column, split
-// into the two half spectra.
+// into the two half spectra. bid: CTA index within this RVE's grid.
 template <typename T>
-__global__ void __launch_bounds__(256) k_fwd_z(const __grid_constant__ ZArgs<T> a) {
-    if (*a.done) return;
-    extern __shared__ __align__(16) unsigned char smem[];
+__device__ __forceinline__ void fwd_z_body(const ZArgs<T>& a, int bid, unsigned char* smem) {
     const Grid& g = a.g;
     const int n = g.n2, nh = g.nh, P = a.P;
     C2<T>* tw = reinterpret_cast<C2<T>*>(smem);
     C2<T>* bA = tw + n;
     C2<T>* bB = bA + P * n;
-    const int ncol = g.n0 * g.n1, c0 = blockIdx.x * P, np = min(P, ncol - c0);
+    const int ncol = g.n0 * g.n1, c0 = bid * P, np = min(P, ncol - c0);
     load_tw<T>(tw, a.tw, n);
     for (int pair = 0; pair < 3; pair++) {
         const T* sa = a.sig + (size_t)(2 * pair) * g.N + (size_t)c0 * n;
@@ -82,16 +42,14 @@ __global__ void __launch_bounds__(256) k_fwd_z(const __grid_constant__ ZArgs<T> 
 
 // c2c along y on ncomp planes, pencils (x, kz..kz+P).
 template <typename T, int SIGN>
-__global__ void __launch_bounds__(256) k_y(const __grid_constant__ YArgs<T> a) {
-    if (*a.done) return;
-    extern __shared__ __align__(16) unsigned char smem[];
+__device__ __forceinline__ void y_body(const YArgs<T>& a, int bid, unsigned char* smem) {
     const Grid& g = a.g;
     const int n = g.n1, ps = n + 1, P = a.P, nh = g.nh;
     C2<T>* tw = reinterpret_cast<C2<T>*>(smem);
     C2<T>* bA = tw + n;
     C2<T>* bB = bA + P * ps;
     const int ntile = (nh + P - 1) / P;
-    const int x = blockIdx.x / ntile, kz0 = (blockIdx.x % ntile) * P, np = min(P, nh - kz0);
+    const int x = bid / ntile, kz0 = (bid % ntile) * P, np = min(P, nh - kz0);
     load_tw<T>(tw, a.tw, n);
     for (int c = 0; c < a.ncomp; c++) {
         C2<T>* base = a.spec + (size_t)c * g.Nh + (size_t)x * n * nh + kz0;
@@ -111,16 +69,15 @@ __global__ void __launch_bounds__(256) k_y(const __grid_constant__ YArgs<T> a) {
 
 // Forward x, Green contraction, inverse x on pencils (y, kz..kz+P).
 template <typename T>
-__global__ void __launch_bounds__(256) k_x_green(const __grid_constant__ XArgs<T> a) {
-    if (*a.done) return;
-    extern __shared__ __align__(16) unsigned char smem[];
+__device__ __forceinline__ void x_green_body(const XArgs<T>& a, const GreenK<T>& gk, int bid,
+                                             unsigned char* smem) {
     const Grid& g = a.g;
     const int n = g.n0, ps = n + 1, P = a.P, nh = g.nh;
     C2<T>* tw = reinterpret_cast<C2<T>*>(smem);
     C2<T>* bA = tw + n;
     C2<T>* bB = bA + 9 * P * ps;
     const int ntile = (nh + P - 1) / P;
-    const int y = blockIdx.x / ntile, kz0 = (blockIdx.x % ntile) * P, np = min(P, nh - kz0);
+    const int y = bid / ntile, kz0 = (bid % ntile) * P, np = min(P, nh - kz0);
     const size_t xs = (size_t)g.n1 * nh;
     load_tw<T>(tw, a.tw, n);
     for (int i = threadIdx.x; i < 6 * n * np; i += blockDim.x) {
@@ -136,11 +93,11 @@ __global__ void __launch_bounds__(256) k_x_green(const __grid_constant__ XArgs<T
 #pragma unroll
         for (int c = 0; c < 6; c++) sb[c] = R[(c * np + kk) * ps + kx];
         if ((kx | ky | kz) == 0) {
-            green_k0<T>(a.gk.s0, a.gk.elast_bc, sb, du);
+            green_k0<T>(gk.s0, gk.elast_bc, sb, du);
         } else {
             T nv[3];
             kvec<T>(kx, ky, kz, g, nv);
-            green_du<T>(a.gk.c0, nv, sb, du);
+            green_du<T>(gk.c0, nv, sb, du);
             const bool nyq = ((g.n0 & 1) == 0 && 2 * kx == g.n0) ||
                              ((g.n1 & 1) == 0 && 2 * ky == g.n1) ||
                              ((g.n2 & 1) == 0 && 2 * kz == g.n2);
@@ -151,7 +108,7 @@ __global__ void __launch_bounds__(256) k_x_green(const __grid_constant__ XArgs<T
                 for (int c = 0; c < 6; c++) sm[c] = cconj<T>(sb[c]);
                 const int mx = (g.n0 - kx) % g.n0, my = (g.n1 - ky) % g.n1, mz = (g.n2 - kz) % g.n2;
                 kvec<T>(mx, my, mz, g, nv);
-                green_du<T>(a.gk.c0, nv, sm, dm);
+                green_du<T>(gk.c0, nv, sm, dm);
 #pragma unroll
                 for (int c = 0; c < 9; c++)
                     du[c] = mk<T>((T)0.5 * (du[c].x + dm[c].x), (T)0.5 * (du[c].y - dm[c].y));
@@ -175,15 +132,13 @@ __global__ void __launch_bounds__(256) k_x_green(const __grid_constant__ XArgs<T
 constexpr int INVZ_EPT = 16;
 
 template <typename T>
-__global__ void __launch_bounds__(256) k_inv_z(const __grid_constant__ ZArgs<T> a) {
-    if (*a.done) return;
-    extern __shared__ __align__(16) unsigned char smem[];
+__device__ __forceinline__ void inv_z_body(const ZArgs<T>& a, int bid, unsigned char* smem) {
     const Grid& g = a.g;
     const int n = g.n2, nh = g.nh, P = a.P;
     C2<T>* tw = reinterpret_cast<C2<T>*>(smem);
     C2<T>* bA = tw + n;
     C2<T>* bB = bA + P * n;
-    const int ncol = g.n0 * g.n1, c0 = blockIdx.x * P, np = min(P, ncol - c0);
+    const int ncol = g.n0 * g.n1, c0 = bid * P, np = min(P, ncol - c0);
     const int tot = np * n;
     load_tw<T>(tw, a.tw, n);
     for (int pair = 0; pair < 5; pair++) {
@@ -230,12 +185,94 @@ __global__ void __launch_bounds__(256) k_inv_z(const __grid_constant__ ZArgs<T> 
     }
 }
 
-template <typename T> static int pick_p(int n, int per_pencil_elems, size_t elem, size_t budget) {
+// ---- single-RVE kernels: arguments in the constant bank
+
+template <typename T>
+__global__ void __launch_bounds__(SPEC_THREADS) k_fwd_z(const __grid_constant__ ZArgs<T> a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    if (!gate_open(a.macro, a.gate)) return;
+    fwd_z_body<T>(a, blockIdx.x, smem);
+}
+
+template <typename T, int SIGN>
+__global__ void __launch_bounds__(SPEC_THREADS) k_y(const __grid_constant__ YArgs<T> a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    if (!gate_open(a.macro, a.gate)) return;
+    y_body<T, SIGN>(a, blockIdx.x, smem);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(SPEC_THREADS) k_x_green(const __grid_constant__ XArgs<T> a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    if (!gate_open(a.macro, a.gate)) return;
+    x_green_body<T>(a, a.gk, blockIdx.x, smem);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(SPEC_THREADS) k_inv_z(const __grid_constant__ ZArgs<T> a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    if (!gate_open(a.macro, a.gate)) return;
+    inv_z_body<T>(a, blockIdx.x, smem);
+}
+
+// ---- batched kernels: one launch over many RVEs; map[b] = (RVE slot, CTA
+// index within that RVE's grid), arguments of each RVE in a device table
+
+template <typename T>
+__global__ void __launch_bounds__(SPEC_THREADS) kb_fwd_z(const ZArgs<T>* __restrict__ tab,
+                                                         const int2* __restrict__ map) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int2 m = map[blockIdx.x];
+    const ZArgs<T>& a = tab[m.x];
+    if (!gate_open(a.macro, a.gate)) return;
+    fwd_z_body<T>(a, m.y, smem);
+}
+
+template <typename T, int SIGN>
+__global__ void __launch_bounds__(SPEC_THREADS) kb_y(const YArgs<T>* __restrict__ tab,
+                                                     const int2* __restrict__ map) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int2 m = map[blockIdx.x];
+    const YArgs<T>& a = tab[m.x];
+    if (!gate_open(a.macro, a.gate)) return;
+    y_body<T, SIGN>(a, m.y, smem);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(SPEC_THREADS) kb_x_green(const XArgs<T>* __restrict__ tab,
+                                                           const int2* __restrict__ map) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ GreenK<T> gks;
+    const int2 m = map[blockIdx.x];
+    const XArgs<T>& a = tab[m.x];
+    if (!gate_open(a.macro, a.gate)) return;
+    // C0 and S0 are contiguous (2 x 81 values)
+    const T* src = &a.gk.c0[0][0][0][0];
+    T* dst = &gks.c0[0][0][0][0];
+    for (int i = threadIdx.x; i < 162; i += blockDim.x) dst[i] = src[i];
+    if (threadIdx.x == 0) gks.elast_bc = a.gk.elast_bc;
+    __syncthreads();
+    x_green_body<T>(a, gks, m.y, smem);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(SPEC_THREADS) kb_inv_z(const ZArgs<T>* __restrict__ tab,
+                                                         const int2* __restrict__ map) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int2 m = map[blockIdx.x];
+    const ZArgs<T>& a = tab[m.x];
+    if (!gate_open(a.macro, a.gate)) return;
+    inv_z_body<T>(a, m.y, smem);
+}
+
+// ------------------------------------------------------------ schedules
+
+// Pencils per CTA that fit a shared-memory budget (at most 64).
+static int pick_p(int per_pencil_elems, size_t elem, size_t budget) {
     const size_t per = (size_t)per_pencil_elems * elem;
     int p = (int)(budget / per);
     if (p < 1) p = 1;
     if (p > 64) p = 64;
-    (void)n;
     return p;
 }
 
@@ -248,85 +285,151 @@ static int pencils(long long total_pencils, int pmax, long long want) {
     return (int)p;
 }
 
-template <typename T>
-static cudaError_t spectral_t(Ctx& c, T* sig, T* dg, const C2<T>* const* tw) {
-    const Grid& g = c.g;
-    C2<T>* spec = reinterpret_cast<C2<T>*>(c.spec);
-    const int* done = macro_field<int>(c.macro, offsetof(Macro, done));
-    const size_t es = sizeof(C2<T>);
-    const size_t budget = 72 * 1024;
-    int nsm = 152;
-    {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    }
-    const long long want = 4LL * nsm;
-    cudaError_t e;
-    {
-        ZArgs<T> za;
-        za.g = g; za.pl = c.pl[2]; za.done = done; za.sig = sig; za.dg = dg; za.spec = spec;
-        za.tw = tw[2]; za.dE9 = macro_field<double>(c.macro, offsetof(Macro, dE9));
-        za.invN = (T)(1.0 / (double)g.N);
-        const int ncol = g.n0 * g.n1;
-        za.P = pencils(ncol, pick_p<T>(g.n2, 2 * g.n2, es, budget), want);
-        if (za.P * g.n2 > 256 * INVZ_EPT) za.P = (256 * INVZ_EPT) / g.n2;
-        if (za.P < 1) za.P = 1;
-        const size_t sm = (size_t)(g.n2 + 2 * za.P * g.n2) * es;
-        cudaFuncSetAttribute(k_fwd_z<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        cudaFuncSetAttribute(k_inv_z<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        prof_mark(c, PG_FWD_Z, true);
-        k_fwd_z<T><<<(ncol + za.P - 1) / za.P, 256, sm, c.stream>>>(za);
-        prof_mark(c, PG_FWD_Z, false);
-        // y forward
-        YArgs<T> ya;
-        ya.g = g; ya.pl = c.pl[1]; ya.done = done; ya.spec = spec; ya.tw = tw[1]; ya.ncomp = 6;
-        ya.P = pencils((long long)g.n0 * g.nh, pick_p<T>(g.n1, 2 * (g.n1 + 1), es, budget), want);
-        if (ya.P > g.nh) ya.P = g.nh;
-        const size_t smy = (size_t)(g.n1 + 2 * ya.P * (g.n1 + 1)) * es;
-        cudaFuncSetAttribute(k_y<T, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smy);
-        cudaFuncSetAttribute(k_y<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smy);
-        const int ntile_y = (g.nh + ya.P - 1) / ya.P;
-        prof_mark(c, PG_FWD_Y, true);
-        k_y<T, -1><<<g.n0 * ntile_y, 256, smy, c.stream>>>(ya);
-        prof_mark(c, PG_FWD_Y, false);
-        // x + Green
-        XArgs<T> xa;
-        xa.g = g; xa.pl = c.pl[0]; xa.done = done; xa.spec = spec; xa.tw = tw[0];
-        xa.P = pencils((long long)g.n1 * g.nh, pick_p<T>(g.n0, 18 * (g.n0 + 1), es, 75 * 1024), want);
-        if (xa.P > g.nh) xa.P = g.nh;
-        const Material<T>& m = material_of<T>(c);
-        for (int i = 0; i < 81; i++) {
-            (&xa.gk.c0[0][0][0][0])[i] = (&m.c0[0][0][0][0])[i];
-            (&xa.gk.s0[0][0][0][0])[i] = (&m.s0[0][0][0][0])[i];
-        }
-        xa.gk.elast_bc = m.elast_bc;
-        const size_t smx = (size_t)(g.n0 + 18 * xa.P * (g.n0 + 1)) * es;
-        cudaFuncSetAttribute(k_x_green<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smx);
-        const int ntile_x = (g.nh + xa.P - 1) / xa.P;
-        prof_mark(c, PG_X_GREEN, true);
-        k_x_green<T><<<g.n1 * ntile_x, 256, smx, c.stream>>>(xa);
-        prof_mark(c, PG_X_GREEN, false);
-        // y inverse
-        ya.ncomp = 9;
-        prof_mark(c, PG_INV_Y, true);
-        k_y<T, 1><<<g.n0 * ntile_y, 256, smy, c.stream>>>(ya);
-        prof_mark(c, PG_INV_Y, false);
-        prof_mark(c, PG_INV_Z, true);
-        k_inv_z<T><<<(ncol + za.P - 1) / za.P, 256, sm, c.stream>>>(za);
-        prof_mark(c, PG_INV_Z, false);
-    }
-    e = cudaGetLastError();
-    return e;
+constexpr size_t SPEC_BUDGET = 72 * 1024;
+constexpr size_t SPEC_BUDGET_X = 75 * 1024;
+
+// Largest pencil counts the shared-memory budgets and the register prefetch
+// of the inverse-z pass allow, per pass (z, y, x).
+void spec_pmax(const Grid& g, size_t es, int pmax[3]) {
+    pmax[0] = pick_p(2 * g.n2, es, SPEC_BUDGET);
+    if (pmax[0] * g.n2 > SPEC_THREADS * INVZ_EPT) pmax[0] = (SPEC_THREADS * INVZ_EPT) / g.n2;
+    if (pmax[0] < 1) pmax[0] = 1;
+    pmax[1] = pick_p(2 * (g.n1 + 1), es, SPEC_BUDGET);
+    if (pmax[1] > g.nh) pmax[1] = g.nh;
+    pmax[2] = pick_p(18 * (g.n0 + 1), es, SPEC_BUDGET_X);
+    if (pmax[2] > g.nh) pmax[2] = g.nh;
 }
 
-cudaError_t launch_spectral(Ctx& c) {
+// Default pencils per CTA: the budget, reduced until the grid has 4 CTAs per SM.
+void spec_default_p(const Grid& g, size_t es, int nsm, int P[3]) {
+    int pmax[3];
+    spec_pmax(g, es, pmax);
+    const long long want = 4LL * nsm;
+    P[0] = pencils((long long)g.n0 * g.n1, pmax[0], want);
+    P[1] = pencils((long long)g.n0 * g.nh, pmax[1], want);
+    P[2] = pencils((long long)g.n1 * g.nh, pmax[2], want);
+}
+
+template <typename T> static SpecSet<T>& spec_of(KernelSets& k);
+template <> SpecSet<double>& spec_of<double>(KernelSets& k) { return k.s64; }
+template <> SpecSet<float>& spec_of<float>(KernelSets& k) { return k.s32; }
+
+template <typename T>
+static void build_spec_t(Ctx& c, T* sig, T* dg, const C2<T>* const* tw) {
+    const Grid& g = c.g;
+    SpecSet<T>& s = spec_of<T>(*c.ks);
+    C2<T>* spec = reinterpret_cast<C2<T>*>(c.spec);
+    const size_t es = sizeof(C2<T>);
+    int P[3];
+    for (int a = 0; a < 3; a++) P[a] = c.sched_p[a];
+    if (P[0] <= 0 || P[1] <= 0 || P[2] <= 0) {
+        int d[3];
+        spec_default_p(g, es, c.nsm, d);
+        for (int a = 0; a < 3; a++)
+            if (P[a] <= 0) P[a] = d[a];
+    }
+    ZArgs<T>& za = s.z;
+    za.g = g; za.pl = c.pl[2]; za.macro = c.macro; za.gate = GATE_RUNNING; za.sig = sig; za.dg = dg;
+    za.spec = spec; za.tw = tw[2]; za.dE9 = macro_field<double>(c.macro, offsetof(Macro, dE9));
+    za.invN = (T)(1.0 / (double)g.N);
+    za.P = P[0];
+    const int ncol = g.n0 * g.n1;
+    s.grid_z = (ncol + za.P - 1) / za.P;
+    s.sm_z = (size_t)(g.n2 + 2 * za.P * g.n2) * es;
+    YArgs<T>& ya = s.yf;
+    ya.g = g; ya.pl = c.pl[1]; ya.macro = c.macro; ya.gate = GATE_RUNNING; ya.spec = spec; ya.tw = tw[1];
+    ya.ncomp = 6;
+    ya.P = P[1];
+    s.yi = ya;
+    s.yi.ncomp = 9;
+    s.grid_y = g.n0 * ((g.nh + ya.P - 1) / ya.P);
+    s.sm_y = (size_t)(g.n1 + 2 * ya.P * (g.n1 + 1)) * es;
+    XArgs<T>& xa = s.x;
+    xa.g = g; xa.pl = c.pl[0]; xa.macro = c.macro; xa.gate = GATE_RUNNING; xa.spec = spec; xa.tw = tw[0];
+    xa.P = P[2];
+    const Material<T>& m = material_of<T>(c);
+    for (int i = 0; i < 81; i++) {
+        (&xa.gk.c0[0][0][0][0])[i] = (&m.c0[0][0][0][0])[i];
+        (&xa.gk.s0[0][0][0][0])[i] = (&m.s0[0][0][0][0])[i];
+    }
+    xa.gk.elast_bc = m.elast_bc;
+    s.grid_x = g.n1 * ((g.nh + xa.P - 1) / xa.P);
+    s.sm_x = (size_t)(g.n0 + 18 * xa.P * (g.n0 + 1)) * es;
+}
+
+void build_spectral_sets(Ctx& c) {
     if (c.precision == 0) {
         const double2* tw[3] = {c.tw64[0], c.tw64[1], c.tw64[2]};
-        return spectral_t<double>(c, c.sig64, c.dg64, tw);
+        build_spec_t<double>(c, c.sig64, c.dg64, tw);
+    } else {
+        const float2* tw[3] = {c.tw32[0], c.tw32[1], c.tw32[2]};
+        build_spec_t<float>(c, c.sig32, c.ddg32, tw);
     }
-    const float2* tw[3] = {c.tw32[0], c.tw32[1], c.tw32[2]};
-    return spectral_t<float>(c, c.sig32, c.ddg32, tw);
+}
+
+template <typename T> static void spec_attributes() {
+    const int mx = 227 * 1024;
+    cudaFuncSetAttribute(k_fwd_z<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(k_inv_z<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(k_y<T, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(k_y<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(k_x_green<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx - 2048);
+    cudaFuncSetAttribute(kb_fwd_z<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(kb_inv_z<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(kb_y<T, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(kb_y<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(kb_x_green<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx - 2048);
+}
+
+void spectral_attributes() {
+    spec_attributes<double>();
+    spec_attributes<float>();
+}
+
+template <typename T>
+static cudaError_t spectral_t(Ctx& c, int gate) {
+    SpecSet<T>& s = spec_of<T>(*c.ks);
+    ZArgs<T> za = s.z;
+    YArgs<T> yf = s.yf, yi = s.yi;
+    XArgs<T> xa = s.x;
+    za.gate = yf.gate = yi.gate = xa.gate = gate;
+    prof_mark(c, PG_FWD_Z, true);
+    k_fwd_z<T><<<s.grid_z, SPEC_THREADS, s.sm_z, c.stream>>>(za);
+    prof_mark(c, PG_FWD_Z, false);
+    prof_mark(c, PG_FWD_Y, true);
+    k_y<T, -1><<<s.grid_y, SPEC_THREADS, s.sm_y, c.stream>>>(yf);
+    prof_mark(c, PG_FWD_Y, false);
+    prof_mark(c, PG_X_GREEN, true);
+    k_x_green<T><<<s.grid_x, SPEC_THREADS, s.sm_x, c.stream>>>(xa);
+    prof_mark(c, PG_X_GREEN, false);
+    prof_mark(c, PG_INV_Y, true);
+    k_y<T, 1><<<s.grid_y, SPEC_THREADS, s.sm_y, c.stream>>>(yi);
+    prof_mark(c, PG_INV_Y, false);
+    prof_mark(c, PG_INV_Z, true);
+    k_inv_z<T><<<s.grid_z, SPEC_THREADS, s.sm_z, c.stream>>>(za);
+    prof_mark(c, PG_INV_Z, false);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_spectral(Ctx& c, int gate) {
+    return c.precision == 0 ? spectral_t<double>(c, gate) : spectral_t<float>(c, gate);
+}
+
+// One pass of the spectral chain for a batch: the five launches, each over
+// every RVE of the batch (BL_Z: fwd and inv z, BL_YF, BL_X, BL_YI).
+template <typename T>
+static cudaError_t spectral_batch_t(const BatchLaunch* L, cudaStream_t st) {
+    const BatchLaunch &z = L[BL_Z], &yf = L[BL_YF], &x = L[BL_X], &yi = L[BL_YI];
+    kb_fwd_z<T><<<z.nblk, SPEC_THREADS, z.smem, st>>>((const ZArgs<T>*)z.tab, z.map);
+    kb_y<T, -1><<<yf.nblk, SPEC_THREADS, yf.smem, st>>>((const YArgs<T>*)yf.tab, yf.map);
+    kb_x_green<T><<<x.nblk, SPEC_THREADS, x.smem, st>>>((const XArgs<T>*)x.tab, x.map);
+    kb_y<T, 1><<<yi.nblk, SPEC_THREADS, yi.smem, st>>>((const YArgs<T>*)yi.tab, yi.map);
+    kb_inv_z<T><<<z.nblk, SPEC_THREADS, z.smem, st>>>((const ZArgs<T>*)z.tab, z.map);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_spectral_batch(int precision, const BatchLaunch* L, cudaStream_t st) {
+    return precision == 0 ? spectral_batch_t<double>(L, st) : spectral_batch_t<float>(L, st);
 }
 
 }  // namespace evpg
@@ -339,7 +442,7 @@ cudaError_t launch_spectral(Ctx& c) {
 // a service whose device footprint must be fixed when the library loads --
 // this entry point runs the spectral chain of one equilibrium iteration on
 // caller-owned input and output buffers. Its scratch (the nine half spectra,
-// the twiddle tables, a zero loop flag and a zero macro correction) lives in
+// the twiddle tables and a zero macro correction) lives in
 // the file-scope array below, which every GPU that loads the library holds
 // until the process exits. Calls that overlap on the GPU share that array and
 // race; callers serialise them (one stream, or events).
@@ -358,7 +461,7 @@ constexpr long long NOALLOC_MAX_HALF = 32 * 32 * 17;  // n0*n1*(n2/2+1), e.g. 32
 constexpr size_t NOALLOC_SPEC_BYTES = 9 * NOALLOC_MAX_HALF * sizeof(double2);
 constexpr size_t NOALLOC_TW_OFF = NOALLOC_SPEC_BYTES;
 constexpr size_t NOALLOC_ZERO_OFF = NOALLOC_TW_OFF + 3 * NOALLOC_MAX_LEN * sizeof(double2);
-constexpr size_t NOALLOC_BYTES = NOALLOC_ZERO_OFF + 256;  // flag (int) + 9 doubles, padded
+constexpr size_t NOALLOC_BYTES = NOALLOC_ZERO_OFF + 256;  // 9 zero doubles, padded
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
 
@@ -451,32 +554,31 @@ extern "C" int evpg_green_correction_noalloc(const double* sig6, double* du9, in
     }
     double2* spec = (double2*)base;
     double2* twd = (double2*)(base + NOALLOC_TW_OFF);
-    int* zero_flag = (int*)(base + NOALLOC_ZERO_OFF);
     double* zero9 = (double*)(base + NOALLOC_ZERO_OFF + 16);
     const double2* twp[3] = {twd, twd + NOALLOC_MAX_LEN, twd + 2 * NOALLOC_MAX_LEN};
-    // the loop flag and the macro correction must read zero; the output is
-    // accumulated into, so it starts at zero too
+    // the macro correction must read zero; the output is accumulated into,
+    // so it starts at zero too
     if (cudaMemsetAsync(base + NOALLOC_ZERO_OFF, 0, 256, st) != cudaSuccess) return EVPG_ERR_CUDA;
     if (cudaMemsetAsync(du9, 0, (size_t)9 * g.N * sizeof(double), st) != cudaSuccess) return EVPG_ERR_CUDA;
     if (cudaMemcpyAsync(twd, tw, sizeof tw, cudaMemcpyHostToDevice, st) != cudaSuccess) return EVPG_ERR_CUDA;
 
     const size_t es = sizeof(double2), budget = 72 * 1024;
     ZArgs<double> za;
-    za.g = g; za.pl = pl[2]; za.done = zero_flag; za.sig = sig6; za.dg = du9; za.spec = spec;
+    za.g = g; za.pl = pl[2]; za.macro = nullptr; za.gate = GATE_ALWAYS; za.sig = sig6; za.dg = du9; za.spec = spec;
     za.tw = twp[2]; za.dE9 = zero9; za.invN = 1.0 / (double)g.N;
-    za.P = pick_p<double>(n2, 2 * n2, es, budget);
-    if (za.P * n2 > 256 * INVZ_EPT) za.P = (256 * INVZ_EPT) / n2;
+    za.P = pick_p(2 * n2, es, budget);
+    if (za.P * n2 > SPEC_THREADS * INVZ_EPT) za.P = (SPEC_THREADS * INVZ_EPT) / n2;
     const int ncol = n0 * n1;
     const size_t sm = (size_t)(n2 + 2 * za.P * n2) * es;
     YArgs<double> ya;
-    ya.g = g; ya.pl = pl[1]; ya.done = zero_flag; ya.spec = spec; ya.tw = twp[1]; ya.ncomp = 6;
-    ya.P = pick_p<double>(n1, 2 * (n1 + 1), es, budget);
+    ya.g = g; ya.pl = pl[1]; ya.macro = nullptr; ya.gate = GATE_ALWAYS; ya.spec = spec; ya.tw = twp[1]; ya.ncomp = 6;
+    ya.P = pick_p(2 * (n1 + 1), es, budget);
     if (ya.P > g.nh) ya.P = g.nh;
     const size_t smy = (size_t)(n1 + 2 * ya.P * (n1 + 1)) * es;
     const int ntile_y = (g.nh + ya.P - 1) / ya.P;
     XArgs<double> xa;
-    xa.g = g; xa.pl = pl[0]; xa.done = zero_flag; xa.spec = spec; xa.tw = twp[0];
-    xa.P = pick_p<double>(n0, 18 * (n0 + 1), es, 150 * 1024);
+    xa.g = g; xa.pl = pl[0]; xa.macro = nullptr; xa.gate = GATE_ALWAYS; xa.spec = spec; xa.tw = twp[0];
+    xa.P = pick_p(18 * (n0 + 1), es, 150 * 1024);
     if (xa.P > g.nh) xa.P = g.nh;
     for (int i = 0; i < 81; i++) {
         (&xa.gk.c0[0][0][0][0])[i] = c0[i];
@@ -485,16 +587,12 @@ extern "C" int evpg_green_correction_noalloc(const double* sig6, double* du9, in
     xa.gk.elast_bc = elast_bc;
     const size_t smx = (size_t)(n0 + 18 * xa.P * (n0 + 1)) * es;
     const int ntile_x = (g.nh + xa.P - 1) / xa.P;
-    cudaFuncSetAttribute(k_fwd_z<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    cudaFuncSetAttribute(k_inv_z<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    cudaFuncSetAttribute(k_y<double, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smy);
-    cudaFuncSetAttribute(k_y<double, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smy);
-    cudaFuncSetAttribute(k_x_green<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smx);
-    k_fwd_z<double><<<(ncol + za.P - 1) / za.P, 256, sm, st>>>(za);
-    k_y<double, -1><<<n0 * ntile_y, 256, smy, st>>>(ya);
-    k_x_green<double><<<n1 * ntile_x, 256, smx, st>>>(xa);
+    set_kernel_attributes();
+    k_fwd_z<double><<<(ncol + za.P - 1) / za.P, SPEC_THREADS, sm, st>>>(za);
+    k_y<double, -1><<<n0 * ntile_y, SPEC_THREADS, smy, st>>>(ya);
+    k_x_green<double><<<n1 * ntile_x, SPEC_THREADS, smx, st>>>(xa);
     ya.ncomp = 9;
-    k_y<double, 1><<<n0 * ntile_y, 256, smy, st>>>(ya);
-    k_inv_z<double><<<(ncol + za.P - 1) / za.P, 256, sm, st>>>(za);
+    k_y<double, 1><<<n0 * ntile_y, SPEC_THREADS, smy, st>>>(ya);
+    k_inv_z<double><<<(ncol + za.P - 1) / za.P, SPEC_THREADS, sm, st>>>(za);
     return cudaGetLastError() == cudaSuccess ? EVPG_OK : EVPG_ERR_CUDA;
 }

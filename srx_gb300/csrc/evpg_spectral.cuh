@@ -21,12 +21,6 @@
 
 namespace evpg {
 
-struct SpecArgsBase {
-    Grid g;
-    FftPlan px, py, pz;
-    const int* done;  // skip the launch when the loop has finished
-};
-
 // k-space unit vector, init.c:780-797 (TWO_PI as the reference writes it).
 template <typename T>
 __device__ __forceinline__ void kvec(int kx, int ky, int kz, const Grid& g, T n[3]) {

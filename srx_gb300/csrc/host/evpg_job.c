@@ -71,6 +71,7 @@ typedef struct evpg_job {
     double rho_avg[8];
     long long nr_iters;
     FILE *err_log;
+    int precision, nr_mode;
 } evpg_job;
 
 /* ------------------------------------------------------------- parsing */
@@ -670,6 +671,8 @@ int evpg_job_open(const char *input, const char *rho0, int32_t precision, int32_
         memcpy(d.udot_a, j->Udot_a, sizeof d.udot_a);
         d.err_tol = j->nl.Err;
         d.iter_max = j->nl.IterMax;
+        j->precision = precision;
+        j->nr_mode = nr_mode;
         d.precision = precision;
         d.nr_mode = nr_mode;
         st = evpg_create(&d, &j->ctx);
@@ -698,50 +701,103 @@ int evpg_job_nvox(void *jp, int32_t n[3])
 
 int evpg_job_nsteps(void *jp) { return jp ? ((evpg_job *)jp)->nl.N_steps : 0; }
 
-/* One increment of Evolution(), evolution.c:726-1520. */
-int evpg_job_increment(void *jp, int32_t istep, int32_t *iters)
+/* Load of a namelist's VelGrad_BC_Flag/VelGrad_BC/Stress_BC_Flag/Stress_BC
+ * into the job (init.c:865-901); returns nonzero for an inconsistent set. */
+static int job_load(evpg_job *j, const int32_t vflag[6], const double velgrad[6], const int32_t sflag[6],
+                    const double stress[6])
 {
-    evpg_job *j = (evpg_job *)jp;
-    const double dt = j->nl.TimeStep;
-    t2 udt;
-    evpg_iter_out io;
-    evpg_incr_out eo;
-    int a, b, st;
-    for (a = 0; a < 3; a++)
-        for (b = 0; b < 3; b++) udt[a][b] = j->Udot[a][b] * dt;
-    st = evpg_increment_begin(j->ctx, (const double(*)[3])udt, j->CREEP_FLAG == 1,
-                              (const double(*)[3])j->DisGradAvg_actual, j->TimeTot);
-    if (st) return st;
-    if (j->err_log) {
-        /* one device round trip per iteration, to log the reference's lines */
-        do {
-            st = evpg_equilibrium_iteration(j->ctx, j->e_vm, &io);
-            if (st) return st;
-            fprintf(j->err_log, "%d %d %.17g %.17g %.17g\n", istep, io.iter, io.err_e, io.err_s, io.s_vm);
-        } while (!io.converged && io.iter < j->nl.IterMax);
-    } else {
-        st = evpg_equilibrium_solve(j->ctx, j->e_vm, &io);
-        if (st) return st;
+    double vg[6];
+    int i, a, b;
+    for (i = 0; i < 6; i++) {
+        if ((sflag[i] * vflag[i] != 0) || ((sflag[i] + vflag[i]) != 1)) return EVPG_ERR_ARG;
+        j->nl.VelGrad_BC_Flag[i] = vflag[i];
+        j->nl.Stress_BC_Flag[i] = sflag[i];
+        vg[i] = velgrad[i] * vflag[i];
+        j->nl.VelGrad_BC[i] = vg[i];
+        j->nl.Stress_BC[i] = stress[i];
     }
-    if (iters) *iters = io.iter;
-    memcpy(j->SigAvg, io.sig_avg, sizeof(t2));
-    memcpy(j->SigAvg1, io.sig_avg_ph1, sizeof(t2));
-    j->s_vm = io.s_vm;
-    j->s_vm1 = io.s_vm1;
-    st = evpg_increment_end(j->ctx, (j->nl.Update_Flag == 1) && (istep > 1), &eo);
-    if (st) return st;
-    /* evolution.c:1273-1294 */
+    voigt_to_full(vg, j->Udot);
     for (a = 0; a < 3; a++)
         for (b = 0; b < 3; b++) {
-            j->DisGradAvg_actual[a][b] = j->DisGradAvg[a][b] + io.ddisgrad_acum[a][b];
+            j->Udot_s[a][b] = (j->Udot[a][b] + j->Udot[b][a]) / 2.;
+            j->Udot_a[a][b] = (j->Udot[a][b] - j->Udot[b][a]) / 2.;
+        }
+    j->CREEP_FLAG = 0;
+    for (i = 0; i < 6; i++) j->CREEP_FLAG += j->nl.Stress_BC_Flag[i];
+    j->CREEP_FLAG /= 6;
+    voigt_to_full(j->nl.Stress_BC, j->Scauchy);
+    return EVPG_OK;
+}
+
+/* Switch the job's loading before its next increment: the applied average
+ * of that increment becomes DisGradAvg_t + Udot_new*TimeStep. */
+int evpg_job_set_load(void *jp, const int32_t vflag[6], const double velgrad[6], const int32_t sflag[6],
+                      const double stress[6])
+{
+    evpg_job *j = (evpg_job *)jp;
+    int st, a, b;
+    if (!j || !vflag || !velgrad || !sflag || !stress) return EVPG_ERR_ARG;
+    st = job_load(j, vflag, velgrad, sflag, stress);
+    if (st) return st;
+    for (a = 0; a < 3; a++)
+        for (b = 0; b < 3; b++) j->DisGradAvg[a][b] = j->DisGradAvg_t[a][b] + j->Udot[a][b] * j->nl.TimeStep;
+    return evpg_set_load(j->ctx, j->nl.VelGrad_BC_Flag, j->nl.Stress_BC_Flag, (const double(*)[3])j->Scauchy,
+                         (const double(*)[3])j->Udot_a);
+}
+
+/* Load switch to the boundary conditions of another namelist file. */
+int evpg_job_set_load_from(void *jp, const char *input)
+{
+    evpg_namelist nl;
+    if (!jp || !input) return EVPG_ERR_ARG;
+    memset(&nl, 0, sizeof nl);
+    if (read_namelist(input, &nl)) return EVPG_ERR_IO;
+    return evpg_job_set_load(jp, nl.VelGrad_BC_Flag, nl.VelGrad_BC, nl.Stress_BC_Flag, nl.Stress_BC);
+}
+
+/* Grid of a namelist file (CellDim) without opening the job. */
+int evpg_job_grid(const char *input, int32_t n[3])
+{
+    evpg_namelist nl;
+    if (!input || !n) return EVPG_ERR_ARG;
+    memset(&nl, 0, sizeof nl);
+    if (read_namelist(input, &nl)) return EVPG_ERR_IO;
+    n[0] = nl.CellDim[0]; n[1] = nl.CellDim[1]; n[2] = nl.CellDim[2];
+    return EVPG_OK;
+}
+
+/* Controls of increment istep (evolution.c:1115-1128): Udot*TimeStep,
+ * creep, the applied average, TimeTot, the strain-error normaliser e_vm and
+ * whether update_orient runs in the tail (Update_Flag == 1 && istep > 1). */
+static void job_controls(const evpg_job *j, int istep, t2 udt, int *reorient)
+{
+    const double dt = j->nl.TimeStep;
+    int a, b;
+    for (a = 0; a < 3; a++)
+        for (b = 0; b < 3; b++) udt[a][b] = j->Udot[a][b] * dt;
+    *reorient = (j->nl.Update_Flag == 1) && (istep > 1);
+}
+
+/* Increment bookkeeping after the tail (evolution.c:1273-1332). */
+static void job_finish(evpg_job *j, const evpg_iter_out *io, const evpg_incr_out *eo)
+{
+    const double dt = j->nl.TimeStep;
+    int a, b;
+    memcpy(j->SigAvg, io->sig_avg, sizeof(t2));
+    memcpy(j->SigAvg1, io->sig_avg_ph1, sizeof(t2));
+    j->s_vm = io->s_vm;
+    j->s_vm1 = io->s_vm1;
+    for (a = 0; a < 3; a++)
+        for (b = 0; b < 3; b++) {
+            j->DisGradAvg_actual[a][b] = j->DisGradAvg[a][b] + io->ddisgrad_acum[a][b];
             j->VelGradAvg[a][b] = (j->DisGradAvg_actual[a][b] - j->DisGradAvg_t[a][b]) / dt;
         }
     j->e_vm = von_mises(j->DisGradAvg_actual);
     j->d_vm = von_mises(j->VelGradAvg);
     j->TimeTot += dt;
     memcpy(j->DisGradAvg_t, j->DisGradAvg_actual, sizeof(t2));
-    memcpy(j->EpsAvg, eo.eps_avg, sizeof(t2));
-    memcpy(j->EdotAvg, eo.edot_avg, sizeof(t2));
+    memcpy(j->EpsAvg, eo->eps_avg, sizeof(t2));
+    memcpy(j->EdotAvg, eo->edot_avg, sizeof(t2));
     j->evmp = 0.0;
     j->dvmp = 0.0;
     for (a = 0; a < 3; a++)
@@ -751,11 +807,125 @@ int evpg_job_increment(void *jp, int32_t istep, int32_t *iters)
         }
     j->evmp = sqrt(2. / 3. * j->evmp);
     j->dvmp = sqrt(2. / 3. * j->dvmp);
-    memcpy(j->rho_avg, eo.rho_avg, sizeof j->rho_avg);
-    j->nr_iters = eo.nr_iterations;
+    memcpy(j->rho_avg, eo->rho_avg, sizeof j->rho_avg);
+    j->nr_iters = eo->nr_iterations;
     for (a = 0; a < 3; a++)
         for (b = 0; b < 3; b++) j->DisGradAvg[a][b] = j->DisGradAvg_t[a][b] + j->Udot[a][b] * dt;
+}
+
+/* One increment of Evolution(), evolution.c:726-1520. */
+int evpg_job_increment(void *jp, int32_t istep, int32_t *iters)
+{
+    evpg_job *j = (evpg_job *)jp;
+    t2 udt;
+    evpg_iter_out io;
+    evpg_incr_out eo;
+    int st, reorient;
+    if (!j) return EVPG_ERR_ARG;
+    job_controls(j, istep, udt, &reorient);
+    if (j->err_log) {
+        st = evpg_increment_begin(j->ctx, (const double(*)[3])udt, j->CREEP_FLAG == 1,
+                                  (const double(*)[3])j->DisGradAvg_actual, j->TimeTot);
+        if (st) return st;
+        /* one device round trip per iteration, to log the reference's lines */
+        do {
+            st = evpg_equilibrium_iteration(j->ctx, j->e_vm, &io);
+            if (st) return st;
+            fprintf(j->err_log, "%d %d %.17g %.17g %.17g\n", istep, io.iter, io.err_e, io.err_s, io.s_vm);
+        } while (!io.converged && io.iter < j->nl.IterMax);
+        st = evpg_increment_end(j->ctx, reorient, &eo);
+        if (st) return st;
+    } else {
+        /* the whole increment as one graph launch */
+        st = evpg_increment(j->ctx, (const double(*)[3])udt, j->CREEP_FLAG == 1,
+                            (const double(*)[3])j->DisGradAvg_actual, j->TimeTot, j->e_vm, reorient, &io, &eo);
+        if (st) return st;
+    }
+    if (iters) *iters = io.iter;
+    job_finish(j, &io, &eo);
     return EVPG_OK;
+}
+
+/* Stage increment istep of a job into slot `slot` of a batch. */
+int evpg_job_stage(void *jp, void *batch, int32_t slot, int32_t istep)
+{
+    evpg_job *j = (evpg_job *)jp;
+    t2 udt;
+    int reorient;
+    if (!j || !batch) return EVPG_ERR_ARG;
+    job_controls(j, istep, udt, &reorient);
+    return evpg_batch_stage(batch, slot, (const double(*)[3])udt, j->CREEP_FLAG == 1,
+                            (const double(*)[3])j->DisGradAvg_actual, j->TimeTot, j->e_vm, reorient);
+}
+
+/* After a round: if the job's increment in `slot` ended, do its bookkeeping
+ * and set *ended = 1 (iters: its equilibrium iterations). A slot that
+ * stopped on an error returns that error. */
+int evpg_job_collect(void *jp, void *batch, int32_t slot, int32_t *ended, int32_t *iters)
+{
+    evpg_job *j = (evpg_job *)jp;
+    evpg_iter_out io;
+    evpg_incr_out eo;
+    int32_t phase = 0, status = 0;
+    int st;
+    if (!j || !batch || !ended) return EVPG_ERR_ARG;
+    *ended = 0;
+    st = evpg_batch_slot(batch, slot, &phase, &status, &io, &eo);
+    if (st) return st;
+    if (status) return status;
+    if (phase != 3) return EVPG_OK;
+    *ended = 1;
+    if (iters) *iters = io.iter;
+    job_finish(j, &io, &eo);
+    return EVPG_OK;
+}
+
+/* Run increments [0, nsteps[i]) of n jobs of one precision and NR mode in
+ * one batch, rounds of at most max_ticks iterations; iters[i*stride + k]
+ * receives job i's iterations of increment k (stride >= max nsteps). */
+int evpg_jobs_run_batched(void *const *jobs, int32_t n, const int32_t *nsteps, int32_t max_ticks,
+                          int32_t *iters, int32_t stride, int64_t *rounds_out)
+{
+    void *batch = 0;
+    void **ctxs;
+    int32_t *next;
+    int i, st, prec, mode, left;
+    int64_t rounds = 0;
+    if (!jobs || n < 1 || !nsteps || max_ticks < 1) return EVPG_ERR_ARG;
+    prec = ((evpg_job *)jobs[0])->precision;
+    mode = ((evpg_job *)jobs[0])->nr_mode;
+    st = evpg_batch_create(prec, mode, &batch);
+    if (st) return st;
+    ctxs = (void **)calloc((size_t)n, sizeof(void *));
+    next = (int32_t *)calloc((size_t)n, sizeof(int32_t));
+    for (i = 0; i < n; i++) ctxs[i] = ((evpg_job *)jobs[i])->ctx;
+    st = evpg_batch_set(batch, ctxs, n);
+    left = 0;
+    for (i = 0; i < n && !st; i++)
+        if (nsteps[i] > 0) {
+            st = evpg_job_stage(jobs[i], batch, i, 0);
+            left++;
+        }
+    while (!st && left > 0) {
+        int32_t ticks = 0;
+        st = evpg_batch_round(batch, max_ticks, &ticks);
+        rounds++;
+        for (i = 0; i < n && !st; i++) {
+            int32_t ended = 0, it = 0;
+            if (next[i] >= nsteps[i]) continue;
+            st = evpg_job_collect(jobs[i], batch, i, &ended, &it);
+            if (st || !ended) continue;
+            if (iters) iters[(size_t)i * stride + next[i]] = it;
+            next[i]++;
+            if (next[i] < nsteps[i]) st = evpg_job_stage(jobs[i], batch, i, next[i]);
+            else left--;
+        }
+    }
+    if (rounds_out) *rounds_out = rounds;
+    evpg_batch_destroy(batch);
+    free(ctxs);
+    free(next);
+    return st;
 }
 
 int evpg_job_scalars(void *jp, double *o, int32_t count)

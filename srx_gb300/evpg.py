@@ -74,6 +74,22 @@ def lib() -> C.CDLL:
         L.evpg_increment_end.argtypes = [vp, i32, C.POINTER(IncrOut)]
         L.evpg_synchronize.argtypes = [vp]
         L.evpg_device_bytes.argtypes = [vp, C.POINTER(C.c_int64)]
+        L.evpg_launch_count.argtypes = [vp, C.POINTER(C.c_int64)]
+        L.evpg_set_stream.argtypes = [vp, vp]
+        L.evpg_increment.argtypes = [vp, C.POINTER(d), i32, C.POINTER(d), d, d, i32,
+                                     C.POINTER(IterOut), C.POINTER(IncrOut)]
+        L.evpg_batch_create.argtypes = [i32, i32, C.POINTER(vp)]
+        L.evpg_batch_destroy.argtypes = [vp]
+        L.evpg_batch_set.argtypes = [vp, C.POINTER(vp), i32]
+        L.evpg_batch_stage.argtypes = [vp, i32, C.POINTER(d), i32, C.POINTER(d), d, d, i32]
+        L.evpg_batch_round.argtypes = [vp, i32, C.POINTER(i32)]
+        L.evpg_batch_slot.argtypes = [vp, i32, C.POINTER(i32), C.POINTER(i32), C.POINTER(IterOut),
+                                      C.POINTER(IncrOut)]
+        L.evpg_batch_launch_count.argtypes = [vp, C.POINTER(C.c_int64)]
+        L.evpg_job_stage.argtypes = [vp, vp, i32, i32]
+        L.evpg_job_collect.argtypes = [vp, vp, i32, C.POINTER(i32), C.POINTER(i32)]
+        L.evpg_jobs_run_batched.argtypes = [C.POINTER(vp), i32, C.POINTER(i32), i32, C.POINTER(i32),
+                                            i32, C.POINTER(C.c_int64)]
         _LIB = L
     return _LIB
 
@@ -153,3 +169,22 @@ class Job:
         b = C.c_int64()
         check(lib().evpg_device_bytes(self.ctx, C.byref(b)))
         return b.value
+
+    def launches(self) -> int:
+        n = C.c_int64()
+        check(lib().evpg_launch_count(self.ctx, C.byref(n)))
+        return n.value
+
+
+def run_batched(jobs, nsteps, max_ticks: int = 16):
+    """Advance ``nsteps[i]`` increments of every job in one batch (rounds of
+    at most ``max_ticks`` equilibrium iterations). Returns the per-increment
+    iteration counts (list of lists) and the number of rounds."""
+    n = len(jobs)
+    stride = max(nsteps) if nsteps else 1
+    hs = (C.c_void_p * n)(*[j._h for j in jobs])
+    ns = (C.c_int32 * n)(*nsteps)
+    it = (C.c_int32 * (n * stride))()
+    rounds = C.c_int64()
+    check(lib().evpg_jobs_run_batched(hs, n, ns, max_ticks, it, stride, C.byref(rounds)))
+    return [list(it[i * stride:i * stride + nsteps[i]]) for i in range(n)], rounds.value

@@ -300,3 +300,34 @@ def bicrystal8_case(dirpath: str, n_steps: int = 5, print_every: int = 1) -> dic
     write_sx(os.path.join(dirpath, "cu.sx"), mat.tau0)
     write_namelist(os.path.join(dirpath, "input"), job, mat, "ms.txt", "cu.sx")
     return {"dir": dirpath, "input": os.path.join(dirpath, "input"), "rho0": None}
+
+
+def main(argv=None) -> None:
+    """Write one seeded synthetic case directory:
+
+        python -m srx_gb300.rve --out DIR --n 64 --grains 125 [--seed S]
+            [--load tension|compression|shear] [--rate R] [--steps K]
+            [--rho0 LO HI]
+    """
+    import argparse
+    p = argparse.ArgumentParser(prog="python -m srx_gb300.rve")
+    p.add_argument("--out", required=True)
+    p.add_argument("--n", type=int, nargs="+", default=[32])
+    p.add_argument("--grains", type=int, default=27)
+    p.add_argument("--seed", type=int, default=2025)
+    p.add_argument("--load", default="tension", choices=["tension", "compression", "shear"])
+    p.add_argument("--rate", type=float, default=1e-3)
+    p.add_argument("--strain-per-step", type=float, default=2e-4)
+    p.add_argument("--steps", type=int, default=50)
+    p.add_argument("--err", type=float, default=1e-5)
+    p.add_argument("--rho0", type=float, nargs=2, default=None)
+    a = p.parse_args(argv)
+    n = tuple(a.n * 3 if len(a.n) == 1 else a.n)
+    job = Job(n=n, load=a.load, rate=a.rate, strain_per_step=a.strain_per_step,
+              n_steps=a.steps, err=a.err)
+    c = make_case(a.out, n, a.grains, a.seed, job, rho0=a.rho0)
+    print(c["input"], c["rho0"] or "")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,102 @@
+"""Batched RVEs (one launch per kernel over all RVEs, one CUDA graph per
+round) against the same RVEs run alone through the C ABI.
+
+Every RVE of a batch runs the same per-RVE arithmetic as alone (same pencil
+schedules, deterministic reductions), so the results must be bit-identical:
+iteration counts per increment and every state field. Uneven grids
+(including odd and mixed-radix lengths), loads and strain rates are mixed,
+and rounds are cut short (max_ticks) so RVEs finish their increments in
+different rounds and start the next one while others are still iterating.
+Shear increments are 1e-4 (the reference's NR fails on xy shear at 2e-4 per
+increment with this material)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = None
+
+
+def _evpg():
+    from srx_gb300 import build, evpg
+    build.build()
+    return evpg
+
+
+def _cases(tmp_path):
+    from srx_gb300 import rve
+    specs = [
+        ((16, 16, 16), 8, "tension", 1e-3, 2e-4, 11),
+        ((12, 10, 9), 6, "compression", 3e-3, 2e-4, 12),
+        ((16, 12, 8), 10, "shear", 1e-3, 1e-4, 13),
+        ((20, 16, 12), 5, "tension", 5e-4, 2e-4, 14),
+        ((8, 8, 8), 3, "shear", 2e-3, 1e-4, 15),
+    ]
+    out = []
+    for i, (n, grains, load, rate, sps, seed) in enumerate(specs):
+        job = rve.Job(n=n, load=load, rate=rate, strain_per_step=sps, n_steps=4)
+        out.append(rve.make_case(str(tmp_path / ("c%d" % i)), n, grains, seed, job, rho0=(0.5, 5.0)))
+    return out
+
+
+def _state(evpg, j):
+    return {f: j.download(f) for f in (evpg.F_SIG6, evpg.F_DISGRAD, evpg.F_RHO_S, evpg.F_EPS,
+                                       evpg.F_TRANMAT, evpg.F_GAM_ACUM)}
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_batch_equals_alone(tmp_path, precision):
+    evpg = _evpg()
+    cases = _cases(tmp_path)
+    nsteps = [3, 2, 3, 1, 3]
+    alone_it, alone_st, alone_sc = [], [], []
+    for c, ns in zip(cases, nsteps):
+        with evpg.Job(c["input"], c["rho0"], precision=precision, nr_mode=1) as j:
+            alone_it.append([j.increment(k) for k in range(ns)])
+            alone_st.append(_state(evpg, j))
+            alone_sc.append(j.scalars())
+    jobs = [evpg.Job(c["input"], c["rho0"], precision=precision, nr_mode=1) for c in cases]
+    try:
+        its, rounds = evpg.run_batched(jobs, nsteps, max_ticks=23)
+        assert its == alone_it
+        assert rounds > max(sum(x) for x in alone_it) // 23  # rounds were cut short
+        for j, st, sc in zip(jobs, alone_st, alone_sc):
+            got = _state(evpg, j)
+            for f, v in st.items():
+                assert np.array_equal(got[f], v), f
+            assert np.array_equal(j.scalars(), sc)
+    finally:
+        for j in jobs:
+            j.close()
+
+
+def test_graph_increment_launch_count(tmp_path):
+    """One increment through the round graph launches prologue + ticks x body
+    kernels; the context's counter reflects the kernels that ran."""
+    evpg = _evpg()
+    c = _cases(tmp_path)[0]
+    with evpg.Job(c["input"], c["rho0"], precision=1, nr_mode=1) as j:
+        n0 = j.launches()
+        it = j.increment(0)
+        n1 = j.launches()
+    # prologue 3 (macro reset, head, round start); body: 5 spectral + NR +
+    # macro + fold + refine + tail 2 + advance = 12 per iteration
+    assert n1 - n0 == 3 + 12 * it
+
+
+def test_batch_rejects_mixed_precision(tmp_path):
+    import ctypes as C
+    evpg = _evpg()
+    c = _cases(tmp_path)[4]
+    a = evpg.Job(c["input"], c["rho0"], precision=0, nr_mode=1)
+    b = evpg.Job(c["input"], c["rho0"], precision=1, nr_mode=1)
+    try:
+        L = evpg.lib()
+        h = C.c_void_p()
+        evpg.check(L.evpg_batch_create(0, 1, C.byref(h)))
+        ctxs = (C.c_void_p * 2)(a.ctx.value, b.ctx.value)
+        assert L.evpg_batch_set(h, ctxs, 2) == 1
+        L.evpg_batch_destroy(h)
+    finally:
+        a.close()
+        b.close()
