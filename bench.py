@@ -56,6 +56,11 @@ def parse():
     p.add_argument("--fp64-steps", type=int, default=2)
     p.add_argument("--e2e-steps", type=int, default=2)
     p.add_argument("--workdir", default=None)
+    p.add_argument("--batch-count", type=int, default=64)
+    p.add_argument("--batch-steps", type=int, default=2)
+    p.add_argument("--serve-requests", type=int, default=24)
+    p.add_argument("--serve-rates", default="2,16")
+    p.add_argument("--forms", default="batch,serve", help="extra forms to measure ('' for none)")
     return p.parse_args()
 
 
@@ -231,6 +236,70 @@ def reference_arm(a, ws, rank):
     print(json.dumps(line), flush=True)
 
 
+def batch_leg(a, evpg, root):
+    """Batching form: RVEs of uneven grids, loads and rates advanced in one
+    batch (one launch per kernel over all RVEs, one CUDA graph per round),
+    against the same RVEs run one after another alone (their own per-increment
+    graphs). Host wall time around synchronous calls."""
+    from srx_gb300 import workloads
+    cases = workloads.batch_set(os.path.join(root, "batch"), count=a.batch_count, steps=a.batch_steps)
+    nsteps = [a.batch_steps] * len(cases)
+    out = {"rves": len(cases), "increments_per_rve": a.batch_steps,
+           "grids": sorted(set(c["n"] for c in cases)), "voxels": int(sum(c["N"] for c in cases)),
+           "loads": {k: sum(1 for c in cases if c["load"] == k) for k in ("tension", "compression", "shear")}}
+    for prec, tag in ((evpg.FP32_BULK, "fp32"), (evpg.FP64, "fp64")):
+        jobs = [evpg.Job(c["input"], c["rho0"], precision=prec, nr_mode=evpg.NR_LINESEARCH) for c in cases]
+        t0 = time.perf_counter()
+        its, rounds = evpg.run_batched(jobs, nsteps, max_ticks=32)
+        tb = time.perf_counter() - t0
+        vi = float(sum(c["N"] * sum(i) for c, i in zip(cases, its)))
+        for j in jobs:
+            j.close()
+        rec = {"value": vi / tb, "unit": UNIT, "seconds": tb, "rounds": rounds,
+               "iterations": int(sum(sum(i) for i in its))}
+        if tag == "fp32":
+            jobs = [evpg.Job(c["input"], c["rho0"], precision=prec, nr_mode=evpg.NR_LINESEARCH) for c in cases]
+            t0 = time.perf_counter()
+            its_alone = [[j.increment(k) for k in range(a.batch_steps)] for j in jobs]
+            ta = time.perf_counter() - t0
+            for j in jobs:
+                j.close()
+            rec["alone_sequential"] = {"value": vi / ta, "seconds": ta,
+                                       "same_iterations": its_alone == its}
+            rec["batch_over_alone"] = ta / tb
+        out[tag] = rec
+    return out
+
+
+def serve_leg(a, evpg, root, budget):
+    """Serving form: Poisson request streams through the continuous-batching
+    server (FP32-bulk); latency per solve and per increment, solves/s."""
+    from srx_gb300 import workloads
+    rates = [float(r) for r in a.serve_rates.split(",") if r]
+    base = workloads.serve_stream(os.path.join(root, "serve"), count=a.serve_requests, rate_hz=1.0,
+                                  steps=(2, 4), distinct=min(12, a.serve_requests))
+    out = {"requests": len(base), "grids": sorted(set(c["n"] for c in base)),
+           "increments_per_request": [2, 4], "rates": {}}
+    for rate in rates:
+        with evpg.Server(precision=evpg.FP32_BULK, nr_mode=evpg.NR_LINESEARCH, hbm_budget=budget,
+                         max_slots=64, round_ticks=16, loaders=4) as srv:
+            t0 = time.perf_counter()
+            for c in base:
+                dt = t0 + c["t"] / rate - time.perf_counter()
+                if dt > 0:
+                    time.sleep(dt)
+                srv.submit(c["input"], c["steps"], rho0=c["rho0"], switch_step=c["switch"],
+                           switch_input=c["switch_input"])
+            srv.wait(1800)
+            st = srv.stats()
+        out["rates"][str(rate)] = {
+            "solves_per_s": st.solves_per_s, "solve_p50_s": st.solve_p50, "solve_p99_s": st.solve_p99,
+            "increment_p50_s": st.incr_p50, "increment_p99_s": st.incr_p99,
+            "completed": st.completed, "failed": st.failed, "rounds": st.rounds,
+            "iterations": int(st.iterations), "span_s": st.span}
+    return out
+
+
 def gpu_arm(a, ws, rank, local):
     import torch
     torch.cuda.set_device(local)
@@ -291,7 +360,7 @@ def gpu_arm(a, ws, rank, local):
         t0 = time.perf_counter()
         s0 = a.warmup + a.steps
         for s in range(s0, s0 + a.e2e_steps):
-            e2e_iters += j32.increment(s)  # udot*dt (72 B) goes down as kernel arguments
+            e2e_iters += j32.increment(s)  # the increment's controls (184 B) go down by one copy
             hostv[:] = j32.download(evpg.F_SIG6)
         torch.cuda.synchronize()
         te2e = time.perf_counter() - t0
@@ -329,6 +398,14 @@ def gpu_arm(a, ws, rank, local):
         torch.cuda.synchronize()
         t64 = e0.elapsed_time(e1) / 1e3
         j64.close()
+
+        forms = {}
+        wanted = [f for f in a.forms.split(",") if f]
+        if "batch" in wanted:
+            forms["batching"] = batch_leg(a, evpg, d)
+        if "serve" in wanted:
+            free, _ = torch.cuda.mem_get_info()
+            forms["serving"] = serve_leg(a, evpg, d, int(0.8 * free))
 
     k64 = len(iters64)
     value64 = N * sum(iters64) / t64
@@ -372,7 +449,7 @@ def gpu_arm(a, ws, rank, local):
             "warmup": a.warmup, "ms_per_step": ms_inc32, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 BC/norms/state)",
             "data": "synthetic", "config": workload_config(a),
-            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 72,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 184,
                     "d2h_bytes_per_step": N * 6 * 8 + 4 * 1024},
             "gpu_launches": int(nlaunch),
             "roofline": roofline,
@@ -384,6 +461,7 @@ def gpu_arm(a, ws, rank, local):
             "fp32_macro_sigma_rel_err": macro_err,
             "kernels": prof,
         }
+        line.update(forms)
         print(json.dumps(line), flush=True)
 
 

@@ -343,6 +343,7 @@ typedef struct evpg_server_cfg {
     int32_t max_slots;     /* RVEs advanced together */
     int32_t round_ticks;   /* equilibrium iterations per round */
     int32_t loaders;       /* host threads opening requests */
+    int32_t keep_fields;   /* keep each finished solve's stress, SSD density and scalars */
 } evpg_server_cfg;
 
 typedef struct evpg_request_info {
@@ -370,6 +371,10 @@ int evpg_server_submit(void *server, const char *input_path, const char *rho0_pa
 int evpg_server_wait(void *server, double timeout_s);
 int evpg_server_request(void *server, int64_t id, evpg_request_info *info);
 int evpg_server_stats(void *server, evpg_serve_stats *stats);
+/* Kept results of a finished request (keep_fields): stress [nvox][6] in
+ * .iout order, rho_s [nvox][12], the 34 scalars of evpg_job_scalars; any
+ * output may be NULL. */
+int evpg_server_result(void *server, int64_t id, double *sig6, double *rho_s, size_t nvox, double *scalars);
 int evpg_server_destroy(void *server);
 
 #ifdef __cplusplus

@@ -37,6 +37,8 @@ typedef struct req {
     long long iters;
     int64_t bytes;
     void *job;
+    double *sig6, *rho_s, scalars[34];   /* kept results (cfg.keep_fields) */
+    int nvox;
 } req;
 
 typedef struct server {
@@ -149,6 +151,21 @@ static int compose(server *s)
 
 static void finish_req(server *s, req *r, int state, int status)
 {
+    if (state == RQ_DONE && s->cfg.keep_fields) {
+        int32_t n[3];
+        if (!evpg_job_nvox(r->job, n)) {
+            const size_t N = (size_t)n[0] * n[1] * n[2];
+            r->sig6 = (double *)malloc(sizeof(double) * 6 * N);
+            r->rho_s = (double *)malloc(sizeof(double) * 12 * N);
+            if (r->sig6 && r->rho_s) {
+                void *c = evpg_job_ctx(r->job);
+                if (evpg_download(c, EVPG_F_SIG6, r->sig6, 6 * N) || evpg_download(c, EVPG_F_RHO_S, r->rho_s, 12 * N))
+                    status = EVPG_ERR_CUDA;
+                evpg_job_scalars(r->job, r->scalars, 34);
+                r->nvox = (int)N;
+            }
+        }
+    }
     evpg_job_close(r->job);
     r->job = NULL;
     pthread_mutex_lock(&s->mu);
@@ -360,6 +377,25 @@ int evpg_server_request(void *sp, int64_t id, evpg_request_info *o)
     return EVPG_OK;
 }
 
+int evpg_server_result(void *sp, int64_t id, double *sig6, double *rho_s, size_t nvox, double *scalars)
+{
+    server *s = (server *)sp;
+    req *r;
+    int st = EVPG_OK;
+    if (!s) return EVPG_ERR_ARG;
+    pthread_mutex_lock(&s->mu);
+    if (id < 0 || id >= s->nall) { pthread_mutex_unlock(&s->mu); return EVPG_ERR_ARG; }
+    r = s->all[id];
+    if (r->state != RQ_DONE || !r->sig6 || (size_t)r->nvox != nvox) st = EVPG_ERR_ARG;
+    else {
+        if (sig6) memcpy(sig6, r->sig6, sizeof(double) * 6 * nvox);
+        if (rho_s) memcpy(rho_s, r->rho_s, sizeof(double) * 12 * nvox);
+        if (scalars) memcpy(scalars, r->scalars, sizeof r->scalars);
+    }
+    pthread_mutex_unlock(&s->mu);
+    return st;
+}
+
 static int cmpd(const void *a, const void *b)
 {
     const double x = *(const double *)a, y = *(const double *)b;
@@ -433,7 +469,11 @@ int evpg_server_destroy(void *sp)
         if (s->act[i]->job) evpg_job_close(s->act[i]->job);
     for (i = 0; i < s->nready; i++)
         if (s->ready[i]->job) evpg_job_close(s->ready[i]->job);
-    for (i = 0; i < s->nall; i++) free(s->all[i]);
+    for (i = 0; i < s->nall; i++) {
+        free(s->all[i]->sig6);
+        free(s->all[i]->rho_s);
+        free(s->all[i]);
+    }
     free(s->all);
     free(s->ready);
     free(s->act);

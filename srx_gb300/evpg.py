@@ -175,6 +175,11 @@ class Job:
         check(lib().evpg_launch_count(self.ctx, C.byref(n)))
         return n.value
 
+    def set_load_from(self, input_path: str) -> None:
+        """Switch to the boundary conditions of another namelist."""
+        lib().evpg_job_set_load_from.argtypes = [C.c_void_p, C.c_char_p]
+        check(lib().evpg_job_set_load_from(self._h, input_path.encode()))
+
 
 def run_batched(jobs, nsteps, max_ticks: int = 16):
     """Advance ``nsteps[i]`` increments of every job in one batch (rounds of
@@ -188,3 +193,87 @@ def run_batched(jobs, nsteps, max_ticks: int = 16):
     rounds = C.c_int64()
     check(lib().evpg_jobs_run_batched(hs, n, ns, max_ticks, it, stride, C.byref(rounds)))
     return [list(it[i * stride:i * stride + nsteps[i]]) for i in range(n)], rounds.value
+
+
+class RequestInfo(C.Structure):
+    _fields_ = [("state", C.c_int32), ("status", C.c_int32), ("increments", C.c_int32),
+                ("iterations", C.c_int64), ("t_submit", C.c_double), ("t_admit", C.c_double),
+                ("t_done", C.c_double), ("device_bytes", C.c_int64)]
+
+
+class ServeStats(C.Structure):
+    _fields_ = [("completed", C.c_int32), ("failed", C.c_int32), ("increments", C.c_int64),
+                ("iterations", C.c_int64), ("rounds", C.c_int64), ("ticks", C.c_int64),
+                ("solve_p50", C.c_double), ("solve_p99", C.c_double), ("incr_p50", C.c_double),
+                ("incr_p99", C.c_double), ("span", C.c_double), ("solves_per_s", C.c_double)]
+
+
+class ServerCfg(C.Structure):
+    _fields_ = [("precision", C.c_int32), ("nr_mode", C.c_int32), ("hbm_budget", C.c_int64),
+                ("max_slots", C.c_int32), ("round_ticks", C.c_int32), ("loaders", C.c_int32),
+                ("keep_fields", C.c_int32)]
+
+
+class Server:
+    """Continuous-batching server of ``include/evpg.h`` (evpg_server_*)."""
+
+    def __init__(self, precision: int = FP32_BULK, nr_mode: int = NR_LINESEARCH,
+                 hbm_budget: int = 64 << 30, max_slots: int = 64, round_ticks: int = 16,
+                 loaders: int = 4, keep_fields: bool = False):
+        L = lib()
+        vp = C.c_void_p
+        L.evpg_server_create.argtypes = [C.POINTER(ServerCfg), C.POINTER(vp)]
+        L.evpg_server_submit.argtypes = [vp, C.c_char_p, C.c_char_p, C.c_int32, C.c_int32, C.c_char_p,
+                                         C.POINTER(C.c_int64)]
+        L.evpg_server_wait.argtypes = [vp, C.c_double]
+        L.evpg_server_request.argtypes = [vp, C.c_int64, C.POINTER(RequestInfo)]
+        L.evpg_server_stats.argtypes = [vp, C.POINTER(ServeStats)]
+        L.evpg_server_result.argtypes = [vp, C.c_int64, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                         C.c_size_t, C.POINTER(C.c_double)]
+        L.evpg_server_destroy.argtypes = [vp]
+        cfg = ServerCfg(precision, nr_mode, hbm_budget, max_slots, round_ticks, loaders,
+                        1 if keep_fields else 0)
+        h = C.c_void_p()
+        check(L.evpg_server_create(C.byref(cfg), C.byref(h)))
+        self._h = h
+
+    def submit(self, input_path: str, nsteps: int, rho0: Optional[str] = None,
+               switch_step: int = -1, switch_input: Optional[str] = None) -> int:
+        rid = C.c_int64()
+        check(lib().evpg_server_submit(self._h, input_path.encode(), rho0.encode() if rho0 else None,
+                                       nsteps, switch_step,
+                                       switch_input.encode() if switch_input else None, C.byref(rid)))
+        return rid.value
+
+    def wait(self, timeout_s: float = 3600.0) -> None:
+        check(lib().evpg_server_wait(self._h, timeout_s))
+
+    def request(self, rid: int) -> RequestInfo:
+        info = RequestInfo()
+        check(lib().evpg_server_request(self._h, rid, C.byref(info)))
+        return info
+
+    def stats(self) -> ServeStats:
+        s = ServeStats()
+        check(lib().evpg_server_stats(self._h, C.byref(s)))
+        return s
+
+    def result(self, rid: int, nvox: int):
+        sig = np.empty(6 * nvox)
+        rho = np.empty(12 * nvox)
+        sc = np.empty(34)
+        dp = C.POINTER(C.c_double)
+        check(lib().evpg_server_result(self._h, rid, sig.ctypes.data_as(dp), rho.ctypes.data_as(dp),
+                                       nvox, sc.ctypes.data_as(dp)))
+        return sig.reshape(nvox, 6), rho.reshape(nvox, 12), sc
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().evpg_server_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

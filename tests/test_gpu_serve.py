@@ -1,0 +1,104 @@
+"""Continuous-batching server (evpg_server_*): every request's result is the
+same alone and in the mix -- bit-identical stress, SSD density and scalars
+-- while requests of different grids, loads and lengths arrive during
+others' work, wait for slots, and (with a small device-memory budget) wait
+for memory. Includes a tension-then-shear request (mid-run load switch)."""
+import os
+import time
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _evpg():
+    from srx_gb300 import build, evpg
+    build.build()
+    return evpg
+
+
+def _requests(tmp_path):
+    from srx_gb300 import rve
+    specs = [  # grid, grains, load, rate, strain/increment, increments, switch step
+        ((16, 16, 16), 8, "tension", 1e-3, 2e-4, 3, -1),
+        ((12, 10, 9), 6, "compression", 3e-3, 2e-4, 2, -1),
+        ((16, 12, 8), 10, "tension", 1e-3, 1e-4, 4, 2),   # then shear
+        ((20, 16, 12), 5, "shear", 5e-4, 1e-4, 2, -1),
+        ((8, 8, 8), 3, "tension", 2e-3, 2e-4, 3, -1),
+    ]
+    out = []
+    for i, (n, grains, load, rate, sps, steps, sw) in enumerate(specs):
+        d = str(tmp_path / ("r%d" % i))
+        job = rve.Job(n=n, load=load, rate=rate, strain_per_step=sps, n_steps=steps)
+        c = rve.make_case(d, n, grains, 100 + i, job, rho0=(0.5, 5.0))
+        c["steps"], c["switch"], c["N"] = steps, sw, int(np.prod(n))
+        c["switch_input"] = None
+        if sw > 0:
+            shear = rve.Job(n=n, load="shear", rate=rate, strain_per_step=sps, n_steps=steps)
+            p = os.path.join(d, "input_shear")
+            rve.write_namelist(p, shear, rve.Material(), "ms.txt", "cu.sx")
+            c["switch_input"] = p
+        out.append(c)
+    return out
+
+
+def _alone(evpg, c, precision):
+    with evpg.Job(c["input"], c["rho0"], precision=precision, nr_mode=1) as j:
+        for k in range(c["steps"]):
+            if c["switch"] > 0 and k == c["switch"]:
+                j.set_load_from(c["switch_input"])
+            j.increment(k)
+        return j.download(evpg.F_SIG6), j.download(evpg.F_RHO_S), j.scalars()
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_served_results_equal_alone(tmp_path, precision):
+    evpg = _evpg()
+    reqs = _requests(tmp_path)
+    ref = [_alone(evpg, c, precision) for c in reqs]
+    with evpg.Server(precision=precision, nr_mode=1, max_slots=3, round_ticks=13, loaders=2,
+                     keep_fields=True) as srv:
+        ids = []
+        for c in reqs:
+            ids.append(srv.submit(c["input"], c["steps"], rho0=c["rho0"], switch_step=c["switch"],
+                                  switch_input=c["switch_input"]))
+            time.sleep(0.02)
+        srv.wait(600)
+        st = srv.stats()
+        assert st.completed == len(reqs) and st.failed == 0
+        assert st.increments == sum(c["steps"] for c in reqs)
+        assert 0 < st.incr_p50 <= st.incr_p99 and 0 < st.solve_p50 <= st.solve_p99
+        assert st.solves_per_s > 0
+        for rid, c, (sig, rho, sc) in zip(ids, reqs, ref):
+            info = srv.request(rid)
+            assert info.state == 4 and info.increments == c["steps"]
+            gs, gr, gsc = srv.result(rid, c["N"])
+            assert np.array_equal(gs, sig)
+            assert np.array_equal(gr, rho)
+            assert np.array_equal(gsc, sc)
+
+
+def test_admission_by_memory_budget(tmp_path):
+    """With room for one request at a time, solves run one after another."""
+    evpg = _evpg()
+    reqs = _requests(tmp_path)[:3]
+    with evpg.Server(precision=1, nr_mode=1, hbm_budget=100 << 20, max_slots=8, round_ticks=16,
+                     loaders=3) as srv:
+        ids = [srv.submit(c["input"], c["steps"], rho0=c["rho0"], switch_step=c["switch"],
+                          switch_input=c["switch_input"]) for c in reqs]
+        srv.wait(600)
+        iv = sorted((srv.request(i).t_admit, srv.request(i).t_done) for i in ids)
+        assert all(srv.request(i).state == 4 for i in ids)
+        for (a0, d0), (a1, d1) in zip(iv, iv[1:]):
+            assert d0 <= a1
+
+
+def test_request_larger_than_budget_fails(tmp_path):
+    evpg = _evpg()
+    c = _requests(tmp_path)[0]
+    with evpg.Server(precision=1, nr_mode=1, hbm_budget=1 << 20, max_slots=4, round_ticks=16) as srv:
+        rid = srv.submit(c["input"], 1, rho0=c["rho0"])
+        srv.wait(60)
+        info = srv.request(rid)
+        assert info.state == 5 and info.status == 3  # EVPG_ERR_NOMEM
