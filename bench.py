@@ -42,6 +42,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "voxel-iters/s 128^3 FP32-bulk vs FP64 (<=1e-4 sigma err)"
+NR_DRAM_BYTES_PER_VOXEL = 488.6
 UNIT = "voxel-iterations/s"
 
 
@@ -249,6 +250,8 @@ def batch_leg(a, evpg, root):
            "loads": {k: sum(1 for c in cases if c["load"] == k) for k in ("tension", "compression", "shear")}}
     for prec, tag in ((evpg.FP32_BULK, "fp32"), (evpg.FP64, "fp64")):
         jobs = [evpg.Job(c["input"], c["rho0"], precision=prec, nr_mode=evpg.NR_LINESEARCH) for c in cases]
+        for j in jobs:
+            j.tune()  # searched once per grid, cached for the others
         t0 = time.perf_counter()
         its, rounds = evpg.run_batched(jobs, nsteps, max_ticks=32)
         tb = time.perf_counter() - t0
@@ -259,6 +262,8 @@ def batch_leg(a, evpg, root):
                "iterations": int(sum(sum(i) for i in its))}
         if tag == "fp32":
             jobs = [evpg.Job(c["input"], c["rho0"], precision=prec, nr_mode=evpg.NR_LINESEARCH) for c in cases]
+            for j in jobs:
+                j.tune()
             t0 = time.perf_counter()
             its_alone = [[j.increment(k) for k in range(a.batch_steps)] for j in jobs]
             ta = time.perf_counter() - t0
@@ -329,6 +334,7 @@ def gpu_arm(a, ws, rank, local):
 
         # ---------------- FP32 bulk: headline
         j32 = open_job(evpg.FP32_BULK)
+        tune32 = {"gain": j32.tune(), "schedule": j32.schedule()}
         for s in range(a.warmup):
             j32.increment(s)
         barrier(ws)
@@ -385,6 +391,7 @@ def gpu_arm(a, ws, rank, local):
 
         # ---------------- FP64 plain form on the same increments
         j64 = open_job(evpg.FP64)
+        tune64 = {"gain": j64.tune(), "schedule": j64.schedule()}
         for s in range(a.warmup):
             j64.increment(s)
         torch.cuda.synchronize()
@@ -420,17 +427,27 @@ def gpu_arm(a, ws, rank, local):
         if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
     hbm = peaks.get("hbm_gbs", 6800.0)
     Nh = a.n * a.n * (a.n // 2 + 1)
-    # algorithmic HBM bytes per launch (FP32 bulk): see the design doc
+    # algorithmic HBM bytes per launch (FP32 bulk). NR per voxel: reads
+    # lambda 6, strain 6, Eps - eps_begin 6, Schmid 60, flow constants 36
+    # (FP32), orientation and phase ids 8 B; writes sigma 6.
     alg = {"fwd_z": N * 6 * 4 + Nh * 6 * 8, "fwd_y": 2 * Nh * 6 * 8,
            "x_green": Nh * 6 * 8 + Nh * 9 * 8, "inv_y": 2 * Nh * 9 * 8,
            "inv_z": Nh * 9 * 8 + 2 * N * 9 * 4,
-           "nr": N * (6 + 6 + 6 + 9 + 60 + 36) * 4 + N * 6 * 4}
+           "nr": N * ((6 + 6 + 6 + 60 + 36 + 6) * 4 + 8)}
+    # DRAM bytes per voxel of one launch, from one ncu capture of the kernel
+    # (dram__bytes_read.sum + dram__bytes_write.sum on the 96^3 RVE, scaled
+    # by voxels; profiles/k_nr_x_green_inv_z_fp32_96cube.md)
+    traffic_per_voxel = {"nr": NR_DRAM_BYTES_PER_VOXEL}
     pl = prof[dom]
     achieved = alg[dom] / (pl["ms_per_launch"] / 1e3) / 1e9
+    traffic = traffic_per_voxel[dom] * N if dom in traffic_per_voxel else None
     roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved,
                 "peak": hbm, "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)",
-                "unit": "GB/s", "frac": achieved / hbm, "traffic": None,
-                "algorithmic_bytes_per_launch": alg[dom]}
+                "unit": "GB/s", "frac": achieved / hbm, "traffic": traffic,
+                "algorithmic_bytes_per_launch": alg[dom],
+                "note": "the NR sweep is issue-bound (FP32 pipe), not HBM-bound: its DRAM traffic "
+                        "equals its algorithmic bytes, so the HBM fraction is its distance from "
+                        "the memory roofline"}
 
     if rank == 0:
         cpu = None
@@ -460,6 +477,7 @@ def gpu_arm(a, ws, rank, local):
             "fp32_over_fp64_per_increment": ms_inc64 / ms_inc32,
             "fp32_macro_sigma_rel_err": macro_err,
             "kernels": prof,
+            "autotune": {"fp32": tune32, "fp64": tune64},
         }
         line.update(forms)
         print(json.dumps(line), flush=True)

@@ -202,6 +202,18 @@ int evpg_increment(void *ctx, const double udot_dt[3][3], int32_t creep,
  * increment head. No counterpart in the reference. */
 int evpg_set_load(void *ctx, const int32_t velgrad_bc_flag[6], const int32_t stress_bc_flag[6],
                   const double scauchy[3][3], const double udot_a[3][3]);
+/* Autotuner of the spectral schedule (no counterpart in the reference):
+ * for this context's grid and precision, times the FFT radix orders of each
+ * axis and the pencils per CTA of each pass on the context's own buffers
+ * (state untouched) and keeps the fastest; results are cached per grid and
+ * precision for the process, so later contexts of the same grid reuse them
+ * (force = 1 searches again). gain (nullable) = default / tuned time of the
+ * spectral passes (0 when taken from the cache). Pencil counts leave the
+ * arithmetic unchanged; a different radix order changes FFT rounding only.
+ * evpg_get_schedule reports pencils per CTA of the z, y, x passes and the
+ * radix stages of the x, y, z axes. */
+int evpg_tune(void *ctx, int32_t force, double *gain);
+int evpg_get_schedule(void *ctx, int32_t pencils[3], int32_t radix[3][12], int32_t nstages[3]);
 /* Device bytes evpg_create allocates for an n[0] x n[1] x n[2] RVE with
  * n_orient distinct orientations (for admission by HBM footprint). */
 int evpg_estimate_bytes(const int32_t n[3], int32_t precision, int32_t n_orient, int64_t *bytes);

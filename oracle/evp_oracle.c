@@ -14,8 +14,11 @@
  *  - error and average sums are accumulated into per-voxel slots and summed
  *    serially in voxel order, which equals the reference's serial order for
  *    any thread count;
- *  - the displacement post-step (evolution.c:1401-1442) only feeds the
- *    new_position dump and is not restated; that record is written as zeros.
+ *  - the displacement post-step (evolution.c:1401-1425) is restated by what
+ *    it computes as written: its per-frequency sums go into scalars and one
+ *    element past fft_data, so the inverse transform acts on the forward
+ *    transform of fluctuation[:][mi][2], and displacement_fluct[mi] is minus
+ *    the round trip of that component.
  */
 #include "evp_oracle.h"
 #include "fft_cpu.h"
@@ -168,6 +171,7 @@ struct evo_job {
     v66 *Cg, *Sg;         /* per distinct orientation */
     double *orient_key;   /* 4 per orientation: ph, th, om, jph */
     t2 *Sig, *DisGrad, *Eps, *Edot, *VelGrad, *TranMat, *fluct;
+    double (*disp)[3];    /* displacement_fluct */
     double (*Schm_gr)[NS][5];
     double (*rho_s)[NS], (*rho_m)[NS], (*rho_F)[NS], (*rho_P)[NS], (*gamdot)[NS],
         (*gam_acum)[NS], (*trial_gam_acum)[NS], (*rho_dipole)[NS], (*rho_forest)[NS],
@@ -499,7 +503,7 @@ static int alloc_fields(evo_job *j)
     ok &= ALLOC(j->grain_f, N) != 0; ok &= ALLOC(j->phase_f, N) != 0; ok &= ALLOC(j->oid, N) != 0;
     ok &= ALLOC(j->Sig, N) != 0; ok &= ALLOC(j->DisGrad, N) != 0; ok &= ALLOC(j->Eps, N) != 0;
     ok &= ALLOC(j->Edot, N) != 0; ok &= ALLOC(j->VelGrad, N) != 0;
-    ok &= ALLOC(j->TranMat, N) != 0; ok &= ALLOC(j->fluct, N) != 0;
+    ok &= ALLOC(j->TranMat, N) != 0; ok &= ALLOC(j->fluct, N) != 0; ok &= ALLOC(j->disp, N) != 0;
     ok &= ALLOC(j->Schm_gr, N) != 0;
     ok &= ALLOC(j->rho_s, N) != 0; ok &= ALLOC(j->rho_m, N) != 0; ok &= ALLOC(j->rho_F, N) != 0;
     ok &= ALLOC(j->rho_P, N) != 0; ok &= ALLOC(j->gamdot, N) != 0;
@@ -733,7 +737,7 @@ void evo_close(evo_job *j)
     if (!j) return;
     free(j->grain_f); free(j->phase_f); free(j->oid); free(j->Cg); free(j->Sg);
     free(j->orient_key); free(j->Sig); free(j->DisGrad); free(j->Eps); free(j->Edot);
-    free(j->VelGrad); free(j->TranMat); free(j->fluct); free(j->Schm_gr); free(j->rho_s);
+    free(j->VelGrad); free(j->TranMat); free(j->fluct); free(j->disp); free(j->Schm_gr); free(j->rho_s);
     free(j->rho_m); free(j->rho_F); free(j->rho_P); free(j->gamdot); free(j->gam_acum);
     free(j->trial_gam_acum); free(j->rho_dipole); free(j->rho_forest); free(j->rho_inplane);
     free(j->rho_dot_s); free(j->rho_tot); free(j->kr); free(j->ki); free(j->fft);
@@ -1487,6 +1491,16 @@ int evo_increment(evo_job *j, int istep, int *iters)
 #pragma omp parallel for num_threads(g_threads) schedule(static)
     for (v = 0; v < N; v++) dislocation_voxel(j, v);
     avg_dislocation(j);
+    /* evolution.c:1401-1425: displacement_fluct[mi] = -Re(IFFT(FFT(fluct[mi][2])))/N */
+    for (a = 0; a < 3; a++) {
+        for (v = 0; v < N; v++) {
+            j->fft[2 * v] = j->fluct[v][a][2];
+            j->fft[2 * v + 1] = 0.0;
+        }
+        fft3d(j, -1);
+        fft3d(j, 1);
+        for (v = 0; v < N; v++) j->disp[v][a] = -j->fft[2 * v] / N;
+    }
     /* evolution.c:1513-1515 */
     for (a = 0; a < 3; a++)
         for (b = 0; b < 3; b++) j->DisGradAvg[a][b] = j->DisGradAvg_t[a][b] + j->Udot[a][b] * dt;
@@ -1575,10 +1589,23 @@ static void write_iout(evo_job *j, const char *dir, int step)
             fwrite(rec, 1, 104, f);
         }
         if (f) fclose(f);
+        /* WriteNewPositionMPI (io.c:723-790) with new_position from
+         * evolution.c:1434-1438: new_position + displacement_fluct - x */
         snprintf(p, sizeof p, "%s/new_position_afterDRX_S%04d.iout", dir, step);
         f = fopen(p, "wb");
-        memset(rec, 0, sizeof rec);
-        for (v = 0; f && v < N; v++) fwrite(rec, 1, 24, f);
+        for (v = 0; f && v < N; v++) {
+            const double px = (double)(v / (j->n1 * j->n2)), py = (double)((v / j->n2) % j->n1),
+                         pz = (double)(v % j->n2);
+            const t2 *D = &j->DisGrad[v];
+            double np[3], ss[3];
+            np[0] = (1.0 + (*D)[0][0]) * px + (*D)[0][1] * py + (*D)[0][2] * pz;
+            np[1] = (1.0 + (*D)[1][1]) * py + (*D)[1][0] * px + (*D)[1][2] * pz;
+            np[2] = (1.0 + (*D)[2][2]) * pz + (*D)[2][0] * px + (*D)[2][1] * py;
+            ss[0] = np[0] + j->disp[v][0] - px;
+            ss[1] = np[1] + j->disp[v][1] - py;
+            ss[2] = np[2] + j->disp[v][2] - pz;
+            fwrite(ss, sizeof(double), 3, f);
+        }
         if (f) fclose(f);
     }
 }

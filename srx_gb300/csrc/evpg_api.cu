@@ -344,11 +344,11 @@ int evpg_create(const evpg_rve_desc* d, void** out) {
     AL(c->sig64, 6 * n); AL(c->dg64, 9 * n); AL(c->dg_old, 9 * n); AL(c->epsp, 6 * n);
     AL(c->edot64, 5 * n); AL(c->rho_s, 12 * n); AL(c->rho_m, 12 * n); AL(c->gamdot64, 12 * n);
     AL(c->gam_acum, 12 * n); AL(c->tranmat, 9 * n); AL(c->schm64, 60 * n); AL(c->fc64, 48 * n);
-    AL(c->sgr64, 36 * (size_t)(d->n_orient > 0 ? d->n_orient : 1));
+    AL(c->sgr64, SGR_STRIDE * (size_t)(d->n_orient > 0 ? d->n_orient : 1));
     AL(c->orient, n); AL(c->phase, n);
     if (f32) {
         AL(c->sig32, 6 * n); AL(c->ddg32, 9 * n); AL(c->b6_32, 6 * n); AL(c->schm32, 60 * n);
-        AL(c->fc32, 48 * n); AL(c->sgr32, 36 * (size_t)(d->n_orient > 0 ? d->n_orient : 1));
+        AL(c->fc32, 48 * n); AL(c->sgr32, SGR_STRIDE * (size_t)(d->n_orient > 0 ? d->n_orient : 1));
         float2* sp = nullptr;
         AL(sp, 9 * (size_t)c->g.Nh);
         c->spec = sp;
@@ -406,10 +406,21 @@ int evpg_create(const evpg_rve_desc* d, void** out) {
     if (e == cudaSuccess) e = put(c->orient, d->voxel_orient, n * sizeof(int32_t));
     if (e == cudaSuccess) e = put(c->phase, d->voxel_phase, n * sizeof(int32_t));
     if (e == cudaSuccess && d->n_orient > 0) {
-        e = put(c->sgr64, d->s_gr, 36 * (size_t)d->n_orient * sizeof(double));
+        // per orientation: S_gr (36) and the constant part of the NR matrix,
+        // packed upper triangle of S066 + (S_gr + S_gr^T)/2 (21)
+        std::vector<double> t(SGR_STRIDE * (size_t)d->n_orient, 0.0);
+        for (int o = 0; o < d->n_orient; o++) {
+            const double* sg = d->s_gr + 36 * (size_t)o;
+            double* row = t.data() + SGR_STRIDE * (size_t)o;
+            memcpy(row, sg, 36 * sizeof(double));
+            int k = 0;
+            for (int i = 0; i < 6; i++)
+                for (int j = i; j < 6; j++) row[36 + k++] = d->s066[i][j] + 0.5 * (sg[i * 6 + j] + sg[j * 6 + i]);
+        }
+        e = put(c->sgr64, t.data(), t.size() * sizeof(double));
         if (e == cudaSuccess && f32) {
-            std::vector<float> hf(36 * (size_t)d->n_orient);
-            for (size_t i = 0; i < hf.size(); i++) hf[i] = (float)d->s_gr[i];
+            std::vector<float> hf(t.size());
+            for (size_t i = 0; i < hf.size(); i++) hf[i] = (float)t[i];
             e = put(c->sgr32, hf.data(), hf.size() * sizeof(float));
         }
     }
@@ -687,14 +698,38 @@ int evpg_set_load(void* ctx, const int32_t velgrad_bc_flag[6], const int32_t str
     return EVPG_OK;
 }
 
+int evpg_tune(void* ctx, int32_t force, double* gain) {
+    Ctx* c = (Ctx*)ctx;
+    if (!c) return fail(EVPG_ERR_ARG, "null context");
+    const int st = tune_spectral(*c, force ? 1 : 0, gain);
+    if (st == 3) return fail(EVPG_ERR_NOMEM, "autotuner scratch allocation failed");
+    if (st) return fail(EVPG_ERR_CUDA, "autotuner launch failed");
+    return EVPG_OK;
+}
+
+int evpg_get_schedule(void* ctx, int32_t pencils[3], int32_t radix[3][12], int32_t nstages[3]) {
+    Ctx* c = (Ctx*)ctx;
+    if (!c) return fail(EVPG_ERR_ARG, "null context");
+    const int prec = c->precision;
+    const int P[3] = {prec ? c->ks->s32.z.P : c->ks->s64.z.P, prec ? c->ks->s32.yf.P : c->ks->s64.yf.P,
+                      prec ? c->ks->s32.x.P : c->ks->s64.x.P};
+    for (int a = 0; a < 3; a++) {
+        if (pencils) pencils[a] = P[a];
+        if (nstages) nstages[a] = c->pl[a].nf;
+        if (radix)
+            for (int s = 0; s < 12; s++) radix[a][s] = s < c->pl[a].nf ? c->pl[a].radix[s] : 0;
+    }
+    return EVPG_OK;
+}
+
 int evpg_estimate_bytes(const int32_t n[3], int32_t precision, int32_t n_orient, int64_t* bytes) {
     if (!n || !bytes || n[0] < 1 || n[1] < 1 || n[2] < 1) return fail(EVPG_ERR_ARG, "bad argument");
     const long long N = (long long)n[0] * n[1] * n[2];
     const long long Nh = (long long)n[0] * n[1] * (n[2] / 2 + 1);
     const long long no = n_orient > 0 ? n_orient : 1;
     const long long nb_nr = (N + NR_BLOCK - 1) / NR_BLOCK, nb_end = (N + END_BLOCK - 1) / END_BLOCK;
-    long long b = 8 * N * (6 + 9 + 9 + 6 + 5 + 12 + 12 + 12 + 12 + 9 + 60 + 48) + 8 * 36 * no + 4 * 2 * N;
-    if (precision == EVPG_FP32_BULK) b += 4 * N * (6 + 9 + 6 + 60 + 48) + 4 * 36 * no + 8 * 9 * Nh;
+    long long b = 8 * N * (6 + 9 + 9 + 6 + 5 + 12 + 12 + 12 + 12 + 9 + 60 + 48) + 8 * SGR_STRIDE * no + 4 * 2 * N;
+    if (precision == EVPG_FP32_BULK) b += 4 * N * (6 + 9 + 6 + 60 + 48) + 4 * SGR_STRIDE * no + 8 * 9 * Nh;
     else b += 16 * 9 * Nh;
     b += 8 * nb_nr * (NR_BLOCK / 32) * NPART_NR + 8 * MACRO_BLOCKS * NPART_NR + 4 + 8 * nb_end * NPART_END;
     b += (long long)sizeof(Macro) + 24LL * (n[0] + n[1] + n[2]);

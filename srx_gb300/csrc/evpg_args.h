@@ -14,6 +14,8 @@ constexpr int NR_BLOCK = 128;
 constexpr int MACRO_BLOCKS = 64;
 constexpr int END_BLOCK = 128;
 constexpr int SPEC_THREADS = 256;
+// per-orientation table row: S_gr (36), packed S066 + sym(S_gr) (21), padding
+constexpr int SGR_STRIDE = 64;
 
 // Which RVEs a launch works on, decided on the device from the RVE's Macro:
 //   GATE_ALWAYS   every launch
@@ -85,7 +87,7 @@ template <typename T> struct NrArgs {
     const T* fc;          // [48][N]
     const int32_t* orient;
     const int32_t* phase;
-    const T* sgr;         // [n_orient][36]
+    const T* sgr;         // [n_orient][SGR_STRIDE]
     T* edot;              // [5][N] or null
     T* gamdot;            // [12][N] or null
     Macro* macro;

@@ -85,6 +85,9 @@ void spec_pmax(const Grid& g, size_t elem_bytes, int pmax[3]);
 void spec_default_p(const Grid& g, size_t elem_bytes, int nsm, int P[3]);
 // Message of the last error on this host thread (evpg_last_error); returns st.
 int record_error(int st, const char* msg);
+// Autotune the spectral schedule (returns 0, 2 CUDA failure, 3 no memory);
+// force: search even when the grid is cached; gain: default time / tuned time.
+int tune_spectral(Ctx& c, int force, double* gain);
 // Release the context's own round graph.
 void free_solo(Ctx& c);
 // Set the kernels' dynamic shared-memory limits (once per device).

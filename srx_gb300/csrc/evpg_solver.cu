@@ -156,6 +156,12 @@ __device__ __forceinline__ void flow_eval(const NrArgs<T>& a, int nsys, int v, c
     bad = bad || nan;
 }
 
+// Quotient in the working precision: IEEE division in FP64 (parity with the
+// reference), the fast reciprocal-based quotient in FP32 (within 2 ulp; the
+// FP32 form's tolerance is set by its own NR tolerance, far above that).
+__device__ __forceinline__ double fdiv(double a, double b) { return a / b; }
+__device__ __forceinline__ float fdiv(float a, float b) { return __fdividef(a, b); }
+
 // Packed symmetric 6x6: index of (i,j), i <= j.
 __host__ __device__ constexpr int sidx(int i, int j) { return i * 6 - i * (i - 1) / 2 + (j - i); }
 
@@ -173,7 +179,7 @@ __device__ __forceinline__ bool ldl_solve(T (&m)[21], const T (&b)[6], T (&x)[6]
         for (int k = 0; k < j; k++) dj -= m[sidx(k, j)] * m[sidx(k, j)] * m[sidx(k, k)];
         m[sidx(j, j)] = dj;
         ok = ok && (dj > (T)0);
-        id[j] = (T)1 / dj;
+        id[j] = fdiv((T)1, dj);
 #pragma unroll
         for (int i = j + 1; i < 6; i++) {
             T t = m[sidx(j, i)];
@@ -289,7 +295,7 @@ __device__ __forceinline__ void nr_body(const NrArgs<T>& a, int bid, unsigned ch
             for (int c = 0; c < 5; c++) a.edot[(size_t)c * N + v] = (T)0;
     } else if (v < N) {
         const int nsys = P.n_sys;
-        const T* sg = a.sgr + (size_t)a.orient[v] * 36;
+        const T* sg = a.sgr + (size_t)a.orient[v] * SGR_STRIDE;
         for (int i = 0; i < nsys; i++) {
 #pragma unroll
             for (int q = 0; q < 5; q++) stg[(i * 5 + q) * NR_BLOCK] = __ldg(a.schm + (size_t)(i * 5 + q) * N + v);
@@ -331,13 +337,11 @@ __device__ __forceinline__ void nr_body(const NrArgs<T>& a, int bid, unsigned ch
                 sgr_v<T>(sg, sig, Ss);
 #pragma unroll
                 for (int c = 0; c < 6; c++) te[c] = av[c] + (c < 5 ? ed[c] * dt : (T)0) + Ss[c];
-                // M = S066 + sym(S) + dt d_edot; rhs = S066 R = S066 (sig - lam) + te
+                // M = S066 + sym(S) + dt d_edot (the first two per orientation);
+                // rhs = S066 R = S066 (sig - lam) + te
                 T m[21];
 #pragma unroll
-                for (int i = 0; i < 6; i++)
-#pragma unroll
-                    for (int j = i; j < 6; j++)
-                        m[sidx(i, j)] = S66[i][j] + (T)0.5 * (__ldg(sg + i * 6 + j) + __ldg(sg + j * 6 + i));
+                for (int k = 0; k < 21; k++) m[k] = __ldg(sg + 36 + k);
                 {
                     int k = 0;
 #pragma unroll
@@ -379,7 +383,7 @@ __device__ __forceinline__ void nr_body(const NrArgs<T>& a, int bid, unsigned ch
                     }
                     nrm = sqrt(nrm);
                     if (nrm > (T)10) {
-                        const T cap = (T)10 / nrm;
+                        const T cap = fdiv((T)10, nrm);
 #pragma unroll
                         for (int c = 0; c < 6; c++) step[c] *= cap;
                         slope *= cap;
@@ -391,10 +395,10 @@ __device__ __forceinline__ void nr_body(const NrArgs<T>& a, int bid, unsigned ch
                         T test = 0;
 #pragma unroll
                         for (int c = 0; c < 6; c++) {
-                            const T tt = fabs(step[c]) / fmax(fabs(old[c]), (T)1);
+                            const T tt = fdiv(fabs(step[c]), fmax(fabs(old[c]), (T)1));
                             if (tt > test) test = tt;
                         }
-                        alamin = (T)1e-7 / test;
+                        alamin = fdiv((T)1e-7, test);
                         alam = 1;
                         alam2 = 0;
 #pragma unroll
@@ -463,7 +467,7 @@ __device__ __forceinline__ void nr_body(const NrArgs<T>& a, int bid, unsigned ch
                     ce += te[c] * te[c];
                     cs += (sig[c] - lam[c]) * (sig[c] - lam[c]);
                 }
-                erral = sqrt(cnr) / signorm;
+                erral = fdiv(sqrt(cnr), signorm);
                 if (sizeof(T) == 4) {
                     // FP32 form: at the NR solution tot_eps - eps = -S066 (sig - lambda);
                     // evaluated at the final stress it carries no lag of the last

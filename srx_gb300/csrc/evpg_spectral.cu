@@ -2,6 +2,12 @@
 #include "evpg_ctx.h"
 #include "evpg_spectral.cuh"
 
+#include <string.h>
+
+#include <algorithm>
+#include <mutex>
+#include <vector>
+
 namespace evpg {
 
 template <typename T>
@@ -314,22 +320,16 @@ template <typename T> static SpecSet<T>& spec_of(KernelSets& k);
 template <> SpecSet<double>& spec_of<double>(KernelSets& k) { return k.s64; }
 template <> SpecSet<float>& spec_of<float>(KernelSets& k) { return k.s32; }
 
+// Launch arguments of the five spectral kernels for pencils-per-CTA P
+// (z, y, x) and FFT plans pl (x, y, z); dg receives the inverse-z output.
 template <typename T>
-static void build_spec_t(Ctx& c, T* sig, T* dg, const C2<T>* const* tw) {
+static void fill_spec_t(Ctx& c, SpecSet<T>& s, const int P[3], const FftPlan pl[3], T* sig, T* dg,
+                        const C2<T>* const* tw) {
     const Grid& g = c.g;
-    SpecSet<T>& s = spec_of<T>(*c.ks);
     C2<T>* spec = reinterpret_cast<C2<T>*>(c.spec);
     const size_t es = sizeof(C2<T>);
-    int P[3];
-    for (int a = 0; a < 3; a++) P[a] = c.sched_p[a];
-    if (P[0] <= 0 || P[1] <= 0 || P[2] <= 0) {
-        int d[3];
-        spec_default_p(g, es, c.nsm, d);
-        for (int a = 0; a < 3; a++)
-            if (P[a] <= 0) P[a] = d[a];
-    }
     ZArgs<T>& za = s.z;
-    za.g = g; za.pl = c.pl[2]; za.macro = c.macro; za.gate = GATE_RUNNING; za.sig = sig; za.dg = dg;
+    za.g = g; za.pl = pl[2]; za.macro = c.macro; za.gate = GATE_RUNNING; za.sig = sig; za.dg = dg;
     za.spec = spec; za.tw = tw[2]; za.dE9 = macro_field<double>(c.macro, offsetof(Macro, dE9));
     za.invN = (T)(1.0 / (double)g.N);
     za.P = P[0];
@@ -337,7 +337,7 @@ static void build_spec_t(Ctx& c, T* sig, T* dg, const C2<T>* const* tw) {
     s.grid_z = (ncol + za.P - 1) / za.P;
     s.sm_z = (size_t)(g.n2 + 2 * za.P * g.n2) * es;
     YArgs<T>& ya = s.yf;
-    ya.g = g; ya.pl = c.pl[1]; ya.macro = c.macro; ya.gate = GATE_RUNNING; ya.spec = spec; ya.tw = tw[1];
+    ya.g = g; ya.pl = pl[1]; ya.macro = c.macro; ya.gate = GATE_RUNNING; ya.spec = spec; ya.tw = tw[1];
     ya.ncomp = 6;
     ya.P = P[1];
     s.yi = ya;
@@ -345,7 +345,7 @@ static void build_spec_t(Ctx& c, T* sig, T* dg, const C2<T>* const* tw) {
     s.grid_y = g.n0 * ((g.nh + ya.P - 1) / ya.P);
     s.sm_y = (size_t)(g.n1 + 2 * ya.P * (g.n1 + 1)) * es;
     XArgs<T>& xa = s.x;
-    xa.g = g; xa.pl = c.pl[0]; xa.macro = c.macro; xa.gate = GATE_RUNNING; xa.spec = spec; xa.tw = tw[0];
+    xa.g = g; xa.pl = pl[0]; xa.macro = c.macro; xa.gate = GATE_RUNNING; xa.spec = spec; xa.tw = tw[0];
     xa.P = P[2];
     const Material<T>& m = material_of<T>(c);
     for (int i = 0; i < 81; i++) {
@@ -355,6 +355,19 @@ static void build_spec_t(Ctx& c, T* sig, T* dg, const C2<T>* const* tw) {
     xa.gk.elast_bc = m.elast_bc;
     s.grid_x = g.n1 * ((g.nh + xa.P - 1) / xa.P);
     s.sm_x = (size_t)(g.n0 + 18 * xa.P * (g.n0 + 1)) * es;
+}
+
+template <typename T>
+static void build_spec_t(Ctx& c, T* sig, T* dg, const C2<T>* const* tw) {
+    int P[3];
+    for (int a = 0; a < 3; a++) P[a] = c.sched_p[a];
+    if (P[0] <= 0 || P[1] <= 0 || P[2] <= 0) {
+        int d[3];
+        spec_default_p(c.g, sizeof(C2<T>), c.nsm, d);
+        for (int a = 0; a < 3; a++)
+            if (P[a] <= 0) P[a] = d[a];
+    }
+    fill_spec_t<T>(c, spec_of<T>(*c.ks), P, c.pl, sig, dg, tw);
 }
 
 void build_spectral_sets(Ctx& c) {
@@ -430,6 +443,194 @@ static cudaError_t spectral_batch_t(const BatchLaunch* L, cudaStream_t st) {
 
 cudaError_t launch_spectral_batch(int precision, const BatchLaunch* L, cudaStream_t st) {
     return precision == 0 ? spectral_batch_t<double>(L, st) : spectral_batch_t<float>(L, st);
+}
+
+// ------------------------------------------------------------- autotuner
+//
+// Per grid and precision: the FFT radix order of each axis and the pencils
+// per CTA of each pass, chosen by timing the pass kernels on the context's
+// own spectrum buffer (the inverse-z output goes to a scratch buffer, so the
+// RVE state is untouched). Coordinate search: the radix orders with the
+// current pencil count, then the pencil counts with the best order; passes
+// are independent. Results are cached per (grid, precision) for the process.
+// Pencil counts do not change the arithmetic; the radix order changes the
+// FFT rounding only.
+
+struct TuneEntry {
+    int n0, n1, n2, prec;
+    int P[3];
+    FftPlan pl[3];
+};
+static std::mutex g_tune_mu;
+static std::vector<TuneEntry> g_tune_cache;
+
+static void plan_of(int n, const std::vector<int>& f, FftPlan& p) {
+    memset(&p, 0, sizeof p);
+    p.n = n;
+    p.nf = (int)f.size();
+    int ns = 1;
+    for (int s = 0; s < p.nf; s++) {
+        p.radix[s] = f[s];
+        p.ns[s] = ns;
+        ns *= f[s];
+    }
+}
+
+// Factor orders of n: radices 8/4/2 for the power-of-two part (at most one
+// radix-2 stage), all distinct permutations, the odd factors after them or
+// before them.
+static std::vector<std::vector<int>> factor_orders(int n) {
+    int m = n, k = 0;
+    while (m % 2 == 0) { m /= 2; k++; }
+    std::vector<int> odd;
+    for (int q : {3, 5})
+        while (m % q == 0) { odd.push_back(q); m /= q; }
+    for (int q = 7; m > 1; q += 2)
+        while (m % q == 0) { odd.push_back(q); m /= q; }
+    std::vector<std::vector<int>> out;
+    for (int n8 = k / 3; n8 >= 0; n8--)
+        for (int n2 = 0; n2 <= 1; n2++) {
+            const int rest = k - 3 * n8 - n2;
+            if (rest < 0 || rest % 2) continue;
+            std::vector<int> f;
+            for (int i = 0; i < n8; i++) f.push_back(8);
+            for (int i = 0; i < rest / 2; i++) f.push_back(4);
+            for (int i = 0; i < n2; i++) f.push_back(2);
+            std::sort(f.begin(), f.end());
+            do {
+                for (int front = 0; front < (odd.empty() ? 1 : 2); front++) {
+                    std::vector<int> g;
+                    if (front) g.insert(g.end(), odd.begin(), odd.end());
+                    g.insert(g.end(), f.begin(), f.end());
+                    if (!front) g.insert(g.end(), odd.begin(), odd.end());
+                    if (g.size() <= 12 && std::find(out.begin(), out.end(), g) == out.end()) out.push_back(g);
+                }
+            } while (std::next_permutation(f.begin(), f.end()) && out.size() < 48);
+        }
+    if (out.empty()) out.push_back(odd);
+    return out;
+}
+
+constexpr size_t TUNE_SMEM_MAX = 200 * 1024;
+
+template <typename T>
+static float time_pass(Ctx& c, int pass, const int P[3], const FftPlan pl[3], T* sig, T* scratch,
+                       const C2<T>* const* tw, cudaEvent_t e0, cudaEvent_t e1) {
+    SpecSet<T> s;
+    fill_spec_t<T>(c, s, P, pl, sig, scratch, tw);
+    s.z.gate = s.yf.gate = s.yi.gate = s.x.gate = GATE_ALWAYS;
+    const size_t sm = pass == 0 ? s.sm_z : pass == 1 ? s.sm_y : s.sm_x;
+    if (sm > TUNE_SMEM_MAX) return 1e30f;
+    if (pass == 0 && P[0] * c.g.n2 > SPEC_THREADS * INVZ_EPT) return 1e30f;
+    auto launch = [&]() {
+        if (pass == 0) {
+            k_fwd_z<T><<<s.grid_z, SPEC_THREADS, s.sm_z, c.stream>>>(s.z);
+            k_inv_z<T><<<s.grid_z, SPEC_THREADS, s.sm_z, c.stream>>>(s.z);
+        } else if (pass == 1) {
+            k_y<T, -1><<<s.grid_y, SPEC_THREADS, s.sm_y, c.stream>>>(s.yf);
+            k_y<T, 1><<<s.grid_y, SPEC_THREADS, s.sm_y, c.stream>>>(s.yi);
+        } else {
+            k_x_green<T><<<s.grid_x, SPEC_THREADS, s.sm_x, c.stream>>>(s.x);
+        }
+    };
+    launch();
+    cudaEventRecord(e0, c.stream);
+    const int reps = 5;
+    for (int r = 0; r < reps; r++) launch();
+    cudaEventRecord(e1, c.stream);
+    if (cudaEventSynchronize(e1) != cudaSuccess) return 1e30f;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    return cudaGetLastError() == cudaSuccess ? ms / reps : 1e30f;
+}
+
+template <typename T>
+static int tune_t(Ctx& c, T* sig, const C2<T>* const* tw, int force, double* gain) {
+    const Grid& g = c.g;
+    const int prec = c.precision;
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        for (const TuneEntry& e : g_tune_cache)
+            if (!force && e.n0 == g.n0 && e.n1 == g.n1 && e.n2 == g.n2 && e.prec == prec) {
+                for (int a = 0; a < 3; a++) {
+                    c.sched_p[a] = e.P[a];
+                    c.pl[a] = e.pl[a];
+                }
+                build_sets(c);
+                c.version++;
+                if (gain) *gain = 0.0;
+                return 0;
+            }
+    }
+    T* scratch = nullptr;
+    if (cudaMalloc((void**)&scratch, sizeof(T) * 9 * (size_t)g.N) != cudaSuccess) return 3;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    int P[3];
+    const SpecSet<T>& cur = spec_of<T>(*c.ks);
+    P[0] = cur.z.P; P[1] = cur.yf.P; P[2] = cur.x.P;
+    FftPlan pl[3] = {c.pl[0], c.pl[1], c.pl[2]};
+    double t0 = 0.0, t1 = 0.0;
+    const int axis_of_pass[3] = {2, 1, 0};
+    const int len_of_pass[3] = {g.n2, g.n1, g.n0};
+    for (int pass = 0; pass < 3; pass++) {
+        const int ax = axis_of_pass[pass];
+        float best = time_pass<T>(c, pass, P, pl, sig, scratch, tw, e0, e1);
+        t0 += best;
+        for (const std::vector<int>& f : factor_orders(len_of_pass[pass])) {
+            FftPlan trial[3] = {pl[0], pl[1], pl[2]};
+            plan_of(len_of_pass[pass], f, trial[ax]);
+            const float t = time_pass<T>(c, pass, P, trial, sig, scratch, tw, e0, e1);
+            if (t < best) {
+                best = t;
+                pl[ax] = trial[ax];
+            }
+        }
+        const int cand[] = {1, 2, 3, 4, 6, 8, 12, 16, 24, 32, 48, 64};
+        for (int q : cand) {
+            if (pass > 0 && q > g.nh) break;
+            int Pt[3] = {P[0], P[1], P[2]};
+            Pt[pass] = q;
+            const float t = time_pass<T>(c, pass, Pt, pl, sig, scratch, tw, e0, e1);
+            if (t < best) {
+                best = t;
+                P[pass] = q;
+            }
+        }
+        t1 += best;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaStreamSynchronize(c.stream);
+    cudaFree(scratch);
+    if (cudaGetLastError() != cudaSuccess) return 2;
+    for (int a = 0; a < 3; a++) {
+        c.sched_p[a] = P[a];
+        c.pl[a] = pl[a];
+    }
+    build_sets(c);
+    c.version++;
+    if (gain) *gain = t1 > 0 ? t0 / t1 : 0.0;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    TuneEntry e;
+    e.n0 = g.n0; e.n1 = g.n1; e.n2 = g.n2; e.prec = prec;
+    for (int a = 0; a < 3; a++) {
+        e.P[a] = P[a];
+        e.pl[a] = pl[a];
+    }
+    g_tune_cache.push_back(e);
+    return 0;
+}
+
+int tune_spectral(Ctx& c, int force, double* gain) {
+    cudaStreamSynchronize(c.stream);
+    if (c.precision == 0) {
+        const double2* tw[3] = {c.tw64[0], c.tw64[1], c.tw64[2]};
+        return tune_t<double>(c, c.sig64, tw, force, gain);
+    }
+    const float2* tw[3] = {c.tw32[0], c.tw32[1], c.tw32[2]};
+    return tune_t<float>(c, c.sig32, tw, force, gain);
 }
 
 }  // namespace evpg

@@ -956,7 +956,7 @@ static void wdoubles(const char *dir, const char *name, const double *x, int n)
 
 /* .iout dumps (io.c:322-995): eps, els, sig (6 files each, order 11,22,33,
  * 23,13,12), rho SSD sum, texture records, slip and dislocation records
- * (int grain + 4 padding + 12 doubles), new_position (zeros). */
+ * (int grain + 4 padding + 12 doubles), new_position. */
 static int write_iout(evpg_job *j, const char *dir, int step)
 {
     const int N = j->N;
@@ -1036,10 +1036,32 @@ static int write_iout(evpg_job *j, const char *dir, int step)
         fwrite(rec, 1, 104, f);
     }
     if (f) fclose(f);
+    /* WriteNewPositionMPI (io.c:723-790): new_position + displacement_fluct
+     * - x with new_position = (I + DisGrad) x (evolution.c:1434-1438) and
+     * displacement_fluct[i] = -fluctuation[i][2] (what evolution.c:1401-1425
+     * computes as written). fluctuation = DisGrad - DisGradAvg_actual: the
+     * applied and mixed-BC parts are uniform. Creep resets DisGrad each
+     * increment while the reference's fluctuation keeps accumulating, so that
+     * record is written as zeros there. */
     snprintf(p, sizeof p, "%s/new_position_afterDRX_S%04d.iout", dir, step);
     f = fopen(p, "wb");
-    memset(rec, 0, sizeof rec);
-    for (v = 0; f && v < N; v++) fwrite(rec, 1, 24, f);
+    for (v = 0; f && v < N; v++) {
+        const double *D = dgr + 9 * (size_t)v;
+        const double px = (double)(v / (j->n1 * j->n2)), py = (double)((v / j->n2) % j->n1),
+                     pz = (double)(v % j->n2);
+        double np3[3], ss[3] = {0.0, 0.0, 0.0};
+        int a;
+        if (j->CREEP_FLAG != 1) {
+            np3[0] = (1.0 + D[0]) * px + D[1] * py + D[2] * pz;
+            np3[1] = (1.0 + D[4]) * py + D[3] * px + D[5] * pz;
+            np3[2] = (1.0 + D[8]) * pz + D[6] * px + D[7] * py;
+            for (a = 0; a < 3; a++) {
+                const double disp = -(D[3 * a + 2] - j->DisGradAvg_actual[a][2]);
+                ss[a] = np3[a] + disp - (a == 0 ? px : a == 1 ? py : pz);
+            }
+        }
+        fwrite(ss, sizeof(double), 3, f);
+    }
     if (f) fclose(f);
     st = EVPG_OK;
 done:

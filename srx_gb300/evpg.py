@@ -175,6 +175,23 @@ class Job:
         check(lib().evpg_launch_count(self.ctx, C.byref(n)))
         return n.value
 
+    def tune(self, force: bool = False) -> float:
+        """Autotune the spectral schedule; returns default/tuned time (0 if cached)."""
+        lib().evpg_tune.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_double)]
+        g = C.c_double()
+        check(lib().evpg_tune(self.ctx, 1 if force else 0, C.byref(g)))
+        return g.value
+
+    def schedule(self) -> dict:
+        """Pencils per CTA (z, y, x passes) and radix stages (x, y, z axes)."""
+        lib().evpg_get_schedule.argtypes = [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                            C.POINTER(C.c_int32)]
+        P = (C.c_int32 * 3)()
+        R = (C.c_int32 * 36)()
+        S = (C.c_int32 * 3)()
+        check(lib().evpg_get_schedule(self.ctx, P, R, S))
+        return {"pencils_zyx": list(P), "radix_xyz": [list(R[12 * a:12 * a + S[a]]) for a in range(3)]}
+
     def set_load_from(self, input_path: str) -> None:
         """Switch to the boundary conditions of another namelist."""
         lib().evpg_job_set_load_from.argtypes = [C.c_void_p, C.c_char_p]

@@ -98,6 +98,7 @@ def read_fields(d: str, step: int, N: int) -> dict:
     f["gam_acum"] = rec.reshape(N, 104)[:, 8:].copy().view(np.float64)
     rec = np.fromfile(os.path.join(d, "tex_afterDRX_S%06d.iout" % step), dtype=np.uint8)
     f["tex"] = rec.reshape(N, 48)[:, :24].copy().view(np.float64)
+    f["newpos"] = np.fromfile(os.path.join(d, "new_position_afterDRX_S%04d.iout" % step)).reshape(N, 3)
     return f
 
 

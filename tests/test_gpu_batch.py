@@ -100,3 +100,28 @@ def test_batch_rejects_mixed_precision(tmp_path):
     finally:
         a.close()
         b.close()
+
+
+def test_autotuned_schedule(tmp_path):
+    """The tuned schedule (radix orders, pencils per CTA) gives the same
+    iterations and fields within FFT rounding (FP64), and a second context of
+    the same grid takes it from the cache."""
+    from conftest import rel_err
+    evpg = _evpg()
+    c = _cases(tmp_path)[1]  # 12 x 10 x 9: radix 4/2/3/5 and odd lengths
+    res = []
+    for tune in (False, True):
+        with evpg.Job(c["input"], c["rho0"], precision=0, nr_mode=1) as j:
+            if tune:
+                g = j.tune(force=True)
+                assert g > 0
+                sched = j.schedule()
+                assert [int(np.prod(r)) for r in sched["radix_xyz"]] == [12, 10, 9]
+            its = [j.increment(k) for k in range(2)]
+            res.append((its, j.download(evpg.F_SIG6), j.download(evpg.F_RHO_S)))
+    assert res[0][0] == res[1][0]
+    assert rel_err(res[1][1], res[0][1]) < 1e-9
+    assert rel_err(res[1][2], res[0][2]) < 1e-9
+    with evpg.Job(c["input"], c["rho0"], precision=0, nr_mode=1) as j:
+        assert j.tune() == 0.0  # cached
+        assert j.schedule() == sched

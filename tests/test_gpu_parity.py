@@ -43,7 +43,7 @@ def test_bicrystal8_matches_reference(tmp_path):
     assert rel_err(read_table(tmp_path / "out" / "dd.out")[:, :2], z["dd"][:, :2]) < PRINT_TOL
     for s in z["keep"]:
         f = read_iout_fields(tmp_path / "out", int(s), 512)
-        for k in ("sig", "eps", "els", "rho_s", "gam_acum"):
+        for k in ("sig", "eps", "els", "rho_s", "gam_acum", "newpos"):
             assert rel_err(f[k], z["%s_%d" % (k, s)]) < FIELD_TOL, (k, int(s))
 
 
@@ -57,7 +57,7 @@ def test_line_search_cases_match_reference(tmp_path, name):
     N = int(np.prod(spec["n"]))
     f = read_iout_fields(tmp_path / "out", spec["steps"] - 1, N)
     idx = z["idx"]
-    for k in ("sig", "eps", "els", "rho_s", "gam_acum"):
+    for k in ("sig", "eps", "els", "rho_s", "gam_acum", "newpos"):
         assert rel_err(f[k][idx], z[k]) < FIELD_TOL, k
 
 

@@ -41,7 +41,7 @@ def test_bicrystal8_matches_reference(tmp_path):
     assert _close(read_table(tmp_path / "out" / "dd.out"), z["dd"])
     for s in z["keep"]:
         f = read_iout_fields(tmp_path / "out", int(s), 512)
-        for k in ("sig", "eps", "els", "rho_s", "gam_acum", "tex"):
+        for k in ("sig", "eps", "els", "rho_s", "gam_acum", "tex", "newpos"):
             assert _close(f[k], z["%s_%d" % (k, s)]), (k, s)
 
 
@@ -55,7 +55,7 @@ def test_line_search_cases_match_reference(tmp_path, name):
     N = int(np.prod(spec["n"]))
     f = read_iout_fields(tmp_path / "out", spec["steps"] - 1, N)
     idx = z["idx"]
-    for k in ("sig", "eps", "els", "rho_s", "gam_acum", "tex"):
+    for k in ("sig", "eps", "els", "rho_s", "gam_acum", "tex", "newpos"):
         assert _close(f[k][idx], z[k]), k
 
 
