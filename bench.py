@@ -17,7 +17,7 @@ sum over timed increments of N x equilibrium iterations / time.
 The headline is the FP32-bulk form; the plain FP64 form is timed on the same
 increments of its own run for the speed-up and error figures.
 
-  python bench.py [--steps K] [--warmup W] [--impl gpu|reference] [--n 128]
+  python bench.py [--steps K] [--warmup W] [--impl gpu|reference] [--grid 128]
                   [--grains 1000] [--fp64-steps K64]
 
 Under torchrun each rank runs an independent replica (the path does not
@@ -52,7 +52,7 @@ def parse():
     p.add_argument("--steps", type=int, default=3)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
-    p.add_argument("--n", type=int, default=128)
+    p.add_argument("--grid", type=int, default=128, help="RVE edge length in voxels")
     p.add_argument("--grains", type=int, default=1000)
     p.add_argument("--fp64-steps", type=int, default=2)
     p.add_argument("--e2e-steps", type=int, default=2)
@@ -67,17 +67,17 @@ def parse():
 
 def workload_config(a):
     return {"workload": "%d^3 RVE, %d Voronoi grains, FCC Cu, rho0 log-uniform [5e11,5e12]/grain, "
-                        "z tension 1e-3/s, 2e-4/increment, line-search NR" % (a.n, a.grains),
-            "grid": [a.n, a.n, a.n], "grains": a.grains, "increments_per_step": 1,
+                        "z tension 1e-3/s, 2e-4/increment, line-search NR" % (a.grid, a.grains),
+            "grid": [a.grid, a.grid, a.grid], "grains": a.grains, "increments_per_step": 1,
             "err_tol": 1e-5, "seed": 2025,
             "l2": "inputs larger than L2 (per-voxel state ~2.5 KB/voxel, GBs resident)"}
 
 
 def make_workload(a, d):
     from srx_gb300 import rve
-    job = rve.Job(n=(a.n,) * 3, load="tension", rate=1e-3, strain_per_step=2e-4, n_steps=250,
+    job = rve.Job(n=(a.grid,) * 3, load="tension", rate=1e-3, strain_per_step=2e-4, n_steps=250,
                   err=1e-5, iter_max=1000)
-    return rve.make_case(d, (a.n,) * 3, a.grains, 2025, job, rho0=(0.5, 5.0))
+    return rve.make_case(d, (a.grid,) * 3, a.grains, 2025, job, rho0=(0.5, 5.0))
 
 
 class Clocks:
@@ -152,24 +152,27 @@ def barrier(ws):
         dist.barrier()
 
 
+def _reduce(x, op):
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=op)
+    return float(t.item())
+
+
 def allmax(ws, x):
     if ws == 1:
         return x
-    import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    return float(t.item())
+    return _reduce(x, dist.ReduceOp.MAX)
 
 
 def allsum(ws, x):
     if ws == 1:
         return x
-    import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.SUM)
-    return float(t.item())
+    return _reduce(x, dist.ReduceOp.SUM)
 
 
 # ------------------------------------------------------------- CPU oracle
@@ -220,7 +223,7 @@ def reference_arm(a, ws, rank):
     with tempfile.TemporaryDirectory(dir=a.workdir) as d:
         case = make_workload(a, d)
         times = cpu_sample(case, a.warmup + a.steps, threads)
-    N = a.n ** 3
+    N = a.grid ** 3
     t = sum(times[a.warmup:])
     value = N * a.steps / t
     line = {
@@ -231,7 +234,7 @@ def reference_arm(a, ws, rank):
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": "one step = one equilibrium iteration (FFT, Green, inverse FFT, "
                                    "line-search NR, get_smacro) of increment 0 of the %d^3 RVE; "
-                                   "FFT is the project's CPU mixed-radix DFT, not FFTW" % a.n},
+                                   "FFT is the project's CPU mixed-radix DFT, not FFTW" % a.grid},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -316,7 +319,7 @@ def gpu_arm(a, ws, rank, local):
     L.evpg_profile.argtypes = [C.c_void_p, C.c_int32]
     L.evpg_profile_read.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int64), C.c_int32]
     L.evpg_launch_count.argtypes = [C.c_void_p, C.POINTER(C.c_int64)]
-    N = a.n ** 3
+    N = a.grid ** 3
 
     with tempfile.TemporaryDirectory(dir=a.workdir) as d:
         case = make_workload(a, d)
@@ -426,7 +429,7 @@ def gpu_arm(a, ws, rank, local):
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) \
         if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
     hbm = peaks.get("hbm_gbs", 6800.0)
-    Nh = a.n * a.n * (a.n // 2 + 1)
+    Nh = a.grid * a.grid * (a.grid // 2 + 1)
     # algorithmic HBM bytes per launch (FP32 bulk). NR per voxel: reads
     # lambda 6, strain 6, Eps - eps_begin 6, Schmid 60, flow constants 36
     # (FP32), orientation and phase ids 8 B; writes sigma 6.
@@ -438,6 +441,10 @@ def gpu_arm(a, ws, rank, local):
     # (dram__bytes_read.sum + dram__bytes_write.sum on the 96^3 RVE, scaled
     # by voxels; profiles/k_nr_x_green_inv_z_fp32_96cube.md)
     traffic_per_voxel = {"nr": NR_DRAM_BYTES_PER_VOXEL}
+    for k, b in alg.items():
+        if prof[k]["ms_per_launch"]:
+            gbs = b / (prof[k]["ms_per_launch"] / 1e3) / 1e9
+            prof[k].update({"algorithmic_bytes": b, "achieved_gbs": gbs, "hbm_frac": gbs / hbm})
     pl = prof[dom]
     achieved = alg[dom] / (pl["ms_per_launch"] / 1e3) / 1e9
     traffic = traffic_per_voxel[dom] * N if dom in traffic_per_voxel else None
@@ -458,7 +465,7 @@ def gpu_arm(a, ws, rank, local):
                 times = cpu_sample(case, 2, threads)
             cpu = {"value": N * 2 / sum(times), "unit": UNIT, "cores": threads, "kind": "port",
                    "sample": "2 equilibrium iterations of increment 0 of the same %d^3 RVE "
-                             "(line-search NR; FFT is the project's CPU DFT, not FFTW)" % a.n}
+                             "(line-search NR; FFT is the project's CPU DFT, not FFTW)" % a.grid}
         except Exception as e:  # the baseline must not hide the GPU number
             cpu = {"value": None, "unit": UNIT, "cores": None, "kind": "port", "sample": str(e)}
         line = {

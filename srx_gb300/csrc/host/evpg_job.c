@@ -72,6 +72,7 @@ typedef struct evpg_job {
     long long nr_iters;
     FILE *err_log;
     int precision, nr_mode;
+    t2 dE_unapplied;  /* sum over increments of the last iteration's dDisGradAvg */
 } evpg_job;
 
 /* ------------------------------------------------------------- parsing */
@@ -785,6 +786,10 @@ static void job_finish(evpg_job *j, const evpg_iter_out *io, const evpg_incr_out
     int a, b;
     memcpy(j->SigAvg, io->sig_avg, sizeof(t2));
     memcpy(j->SigAvg1, io->sig_avg_ph1, sizeof(t2));
+    /* the correction of the loop's last get_smacro enters dDisGradAvg_acum
+     * but never DisGrad (the loop ends before the next update) */
+    for (a = 0; a < 3; a++)
+        for (b = 0; b < 3; b++) j->dE_unapplied[a][b] += io->ddisgrad[a][b];
     j->s_vm = io->s_vm;
     j->s_vm1 = io->s_vm1;
     for (a = 0; a < 3; a++)
@@ -1039,8 +1044,9 @@ static int write_iout(evpg_job *j, const char *dir, int step)
     /* WriteNewPositionMPI (io.c:723-790): new_position + displacement_fluct
      * - x with new_position = (I + DisGrad) x (evolution.c:1434-1438) and
      * displacement_fluct[i] = -fluctuation[i][2] (what evolution.c:1401-1425
-     * computes as written). fluctuation = DisGrad - DisGradAvg_actual: the
-     * applied and mixed-BC parts are uniform. Creep resets DisGrad each
+     * computes as written). fluctuation = DisGrad minus its uniform part,
+     * DisGradAvg_actual less the mixed-BC corrections of each loop's last
+     * iteration, which never reached DisGrad. Creep resets DisGrad each
      * increment while the reference's fluctuation keeps accumulating, so that
      * record is written as zeros there. */
     snprintf(p, sizeof p, "%s/new_position_afterDRX_S%04d.iout", dir, step);
@@ -1056,7 +1062,7 @@ static int write_iout(evpg_job *j, const char *dir, int step)
             np3[1] = (1.0 + D[4]) * py + D[3] * px + D[5] * pz;
             np3[2] = (1.0 + D[8]) * pz + D[6] * px + D[7] * py;
             for (a = 0; a < 3; a++) {
-                const double disp = -(D[3 * a + 2] - j->DisGradAvg_actual[a][2]);
+                const double disp = -(D[3 * a + 2] - (j->DisGradAvg_actual[a][2] - j->dE_unapplied[a][2]));
                 ss[a] = np3[a] + disp - (a == 0 ? px : a == 1 ? py : pz);
             }
         }
