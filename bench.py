@@ -370,7 +370,7 @@ def gpu_arm(a, ws, rank, local):
         s0 = a.warmup + a.steps
         for s in range(s0, s0 + a.e2e_steps):
             e2e_iters += j32.increment(s)  # the increment's controls (184 B) go down by one copy
-            hostv[:] = j32.download(evpg.F_SIG6)
+            j32.download_into(evpg.F_SIG6, hostv)  # pinned: packed on the device, one D2H per chunk
         torch.cuda.synchronize()
         te2e = time.perf_counter() - t0
         e2e_value = allsum(ws, float(N * e2e_iters)) / allmax(ws, te2e)
@@ -474,7 +474,7 @@ def gpu_arm(a, ws, rank, local):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 BC/norms/state)",
             "data": "synthetic", "config": workload_config(a),
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 184,
-                    "d2h_bytes_per_step": N * 6 * 8 + 4 * 1024},
+                    "d2h_bytes_per_step": N * 6 * 8 + 2 * 4 * 1024},
             "gpu_launches": int(nlaunch),
             "roofline": roofline,
             "cpu_baseline": cpu,

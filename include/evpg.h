@@ -214,6 +214,11 @@ int evpg_set_load(void *ctx, const int32_t velgrad_bc_flag[6], const int32_t str
  * radix stages of the x, y, z axes. */
 int evpg_tune(void *ctx, int32_t force, double *gain);
 int evpg_get_schedule(void *ctx, int32_t pencils[3], int32_t radix[3][12], int32_t nstages[3]);
+/* Fused z+y passes (one x plane per CTA, warp-register FFTs along z and y;
+ * n1 == n2 in {32, 64, 128} when the planes fit in shared memory): mode -1
+ * default (on for FP32 bulk where eligible), 0 off, 1 on where eligible.
+ * evpg_get_schedule then reports 0 pencils for the z and y passes. */
+int evpg_set_fused(void *ctx, int32_t mode);
 /* Device bytes evpg_create allocates for an n[0] x n[1] x n[2] RVE with
  * n_orient distinct orientations (for admission by HBM footprint). */
 int evpg_estimate_bytes(const int32_t n[3], int32_t precision, int32_t n_orient, int64_t *bytes);

@@ -224,6 +224,10 @@ static void free_ctx(Ctx* c) {
         if (p) cudaFree(p);
     if (c->macro_host) cudaFreeHost(c->macro_host);
     if (c->ctl_host) cudaFreeHost(c->ctl_host);
+    if (c->dl_dev) cudaFree(c->dl_dev);
+    if (c->dl_host) cudaFreeHost(c->dl_host);
+    for (int i = 0; i < 2; i++)
+        if (c->dl_ev[i]) cudaEventDestroy(c->dl_ev[i]);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     delete c->ks;
     delete c;
@@ -453,6 +457,12 @@ int evpg_create(const evpg_rve_desc* d, void** out) {
         cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, dev);
     }
     set_kernel_attributes();
+    c->sched_fused = -1;
+    for (int i = 0; i < 2 && e == cudaSuccess; i++) e = cudaEventCreateWithFlags(&c->dl_ev[i], cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+        free_ctx(c);
+        return fail(EVPG_ERR_CUDA, "event creation: %s", cudaGetErrorString(e));
+    }
     c->ks = new KernelSets();
     memset((void*)c->ks, 0, sizeof(KernelSets));
     build_sets(*c);
@@ -545,6 +555,43 @@ __global__ void k_set_evm(Macro* m, double e_vm) {
 }
 
 __global__ void k_set_reorient(Macro* m, int r) { m->ctl.reorient = r; }
+
+// Field packing for downloads: SoA planes (B basis) -> voxel-major records
+// in the host layout of evpg_download, for voxels [v0, v0 + nv).
+enum PackKind { PK_TENSOR6 = 0, PK_SIG6 = 1, PK_TENSOR9 = 2, PK_EDOT5 = 3, PK_COPY = 4 };
+
+__global__ void k_pack(const double* __restrict__ src, size_t N, int planes, int kind, size_t v0, int nv,
+                       double* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nv) return;
+    const size_t v = v0 + (size_t)i;
+    double q[12];
+#pragma unroll
+    for (int p = 0; p < 12; p++) q[p] = p < planes ? src[(size_t)p * N + v] : 0.0;
+    if (kind == PK_COPY) {
+        for (int p = 0; p < planes; p++) out[(size_t)i * planes + p] = q[p];
+        return;
+    }
+    double t[3][3];
+    if (kind == PK_TENSOR9) {
+        b6_to_sym<double>(q, t);
+        t[0][1] += q[6]; t[1][0] -= q[6];
+        t[0][2] += q[7]; t[2][0] -= q[7];
+        t[1][2] += q[8]; t[2][1] -= q[8];
+    } else {
+        if (kind == PK_EDOT5) q[5] = 0.0;
+        b6_to_sym<double>(q, t);
+    }
+    if (kind == PK_SIG6) {
+        double* o = out + (size_t)i * 6;
+        o[0] = t[0][0]; o[1] = t[1][1]; o[2] = t[2][2];
+        o[3] = t[1][2]; o[4] = t[0][2]; o[5] = t[0][1];
+    } else {
+        double* o = out + (size_t)i * 9;
+        for (int a = 0; a < 3; a++)
+            for (int b = 0; b < 3; b++) o[3 * a + b] = t[a][b];
+    }
+}
 
 static int read_macro(Ctx* c) {
     CK(cudaMemcpyAsync(c->macro_host, c->macro, sizeof(Macro), cudaMemcpyDeviceToHost, c->stream));
@@ -707,11 +754,24 @@ int evpg_tune(void* ctx, int32_t force, double* gain) {
     return EVPG_OK;
 }
 
+int evpg_set_fused(void* ctx, int32_t mode) {
+    Ctx* c = (Ctx*)ctx;
+    if (!c || mode < -1 || mode > 1) return fail(EVPG_ERR_ARG, "bad argument");
+    CK(cudaStreamSynchronize(c->stream));
+    c->sched_fused = mode;
+    build_sets(*c);
+    c->version++;
+    return EVPG_OK;
+}
+
 int evpg_get_schedule(void* ctx, int32_t pencils[3], int32_t radix[3][12], int32_t nstages[3]) {
     Ctx* c = (Ctx*)ctx;
     if (!c) return fail(EVPG_ERR_ARG, "null context");
     const int prec = c->precision;
-    const int P[3] = {prec ? c->ks->s32.z.P : c->ks->s64.z.P, prec ? c->ks->s32.yf.P : c->ks->s64.yf.P,
+    const int epl = prec ? c->ks->s32.epl : c->ks->s64.epl;
+    // fused z+y plane kernels: the z and y entries are 0 (one x plane per CTA)
+    const int P[3] = {epl ? 0 : (prec ? c->ks->s32.z.P : c->ks->s64.z.P),
+                      epl ? 0 : (prec ? c->ks->s32.yf.P : c->ks->s64.yf.P),
                       prec ? c->ks->s32.x.P : c->ks->s64.x.P};
     for (int a = 0; a < 3; a++) {
         if (pencils) pencils[a] = P[a];
@@ -733,6 +793,7 @@ int evpg_estimate_bytes(const int32_t n[3], int32_t precision, int32_t n_orient,
     else b += 16 * 9 * Nh;
     b += 8 * nb_nr * (NR_BLOCK / 32) * NPART_NR + 8 * MACRO_BLOCKS * NPART_NR + 4 + 8 * nb_end * NPART_END;
     b += (long long)sizeof(Macro) + 24LL * (n[0] + n[1] + n[2]);
+    b += 2LL * (long long)dl_chunk_doubles((size_t)N) * 8;  // download packing buffers
     *bytes = b;
     return EVPG_OK;
 }
@@ -742,45 +803,59 @@ int evpg_download(void* ctx, int32_t field, double* host, size_t count) {
     if (!c || !host) return fail(EVPG_ERR_ARG, "null argument");
     const size_t n = (size_t)c->g.N;
     const double* src = nullptr;
-    int planes = 0;
+    int planes = 0, kind = PK_COPY, outw = 12;
     switch (field) {
-        case EVPG_F_SIG: case EVPG_F_SIG6: src = c->sig64; planes = 6; break;
-        case EVPG_F_DISGRAD: src = c->dg64; planes = 9; break;
-        case EVPG_F_EPS: src = c->epsp; planes = 6; break;
-        case EVPG_F_EDOT: src = c->edot64; planes = 5; break;
-        case EVPG_F_TRANMAT: src = c->tranmat; planes = 9; break;
+        case EVPG_F_SIG: src = c->sig64; planes = 6; kind = PK_TENSOR6; outw = 9; break;
+        case EVPG_F_SIG6: src = c->sig64; planes = 6; kind = PK_SIG6; outw = 6; break;
+        case EVPG_F_DISGRAD: src = c->dg64; planes = 9; kind = PK_TENSOR9; outw = 9; break;
+        case EVPG_F_EPS: src = c->epsp; planes = 6; kind = PK_TENSOR6; outw = 9; break;
+        case EVPG_F_EDOT: src = c->edot64; planes = 5; kind = PK_EDOT5; outw = 9; break;
+        case EVPG_F_TRANMAT: src = c->tranmat; planes = 9; kind = PK_COPY; outw = 9; break;
         case EVPG_F_RHO_S: src = c->rho_s; planes = 12; break;
         case EVPG_F_RHO_M: src = c->rho_m; planes = 12; break;
         case EVPG_F_GAMDOT: src = c->gamdot64; planes = 12; break;
         case EVPG_F_GAM_ACUM: src = c->gam_acum; planes = 12; break;
-        case EVPG_F_VELGRAD: src = c->dg_old; planes = 9; break;
+        case EVPG_F_VELGRAD: src = c->dg_old; planes = 9; kind = PK_TENSOR9; outw = 9; break;
         default: return fail(EVPG_ERR_ARG, "unknown field %d", field);
     }
-    const int outw = (field == EVPG_F_SIG6) ? 6 : (planes == 12 ? 12 : 9);
     if (count < (size_t)outw * n) return fail(EVPG_ERR_ARG, "buffer too small");
-    std::vector<double> h((size_t)planes * n);
-    CK(cudaMemcpyAsync(h.data(), src, h.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaStreamSynchronize(c->stream));
-    for (size_t v = 0; v < n; v++) {
-        double q[12] = {0};
-        for (int p = 0; p < planes; p++) q[p] = h[p * n + v];
-        double* o = host + (size_t)outw * v;
-        if (planes == 12) {
-            memcpy(o, q, 12 * sizeof(double));
-        } else if (field == EVPG_F_TRANMAT) {
-            memcpy(o, q, 9 * sizeof(double));
-        } else {
-            double t[3][3];
-            if (planes == 9) nine_to_tensor(q, t);
-            else b6_to_sym<double>(q, t);  // EDOT: q[5] = 0
-            if (field == EVPG_F_SIG6) {
-                o[0] = t[0][0]; o[1] = t[1][1]; o[2] = t[2][2];
-                o[3] = t[1][2]; o[4] = t[0][2]; o[5] = t[0][1];
-            } else {
-                memcpy(o, t, sizeof t);
-            }
-        }
+    // packed on the device in chunks, copied through a pinned staging buffer
+    // (or straight into the caller's buffer when it is pinned)
+    const size_t cap = dl_chunk_doubles(n);
+    const size_t chunk = cap / (size_t)outw;
+    if (!c->dl_dev) {
+        CK(cudaMalloc((void**)&c->dl_dev, 2 * cap * sizeof(double)));
+        c->bytes += 2 * cap * sizeof(double);
+        CK(cudaMallocHost((void**)&c->dl_host, 2 * cap * sizeof(double)));
     }
+    cudaPointerAttributes pa;
+    bool pinned = cudaPointerGetAttributes(&pa, host) == cudaSuccess && pa.type == cudaMemoryTypeHost;
+    cudaGetLastError();
+    int k = 0;
+    size_t done_v = 0, pend_v0 = 0, pend_nv = 0;
+    for (size_t v0 = 0; v0 < n; v0 += chunk, k ^= 1) {
+        const size_t nv = (n - v0 < chunk) ? n - v0 : chunk;
+        double* dbuf = c->dl_dev + (size_t)k * cap;
+        k_pack<<<(unsigned)((nv + 255) / 256), 256, 0, c->stream>>>(src, n, planes, kind, v0, (int)nv, dbuf);
+        c->launches++;
+        double* dst = pinned ? host + v0 * outw : c->dl_host + (size_t)k * cap;
+        CK(cudaMemcpyAsync(dst, dbuf, nv * outw * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+        if (!pinned) {
+            // finish the previous chunk on the host while this one copies
+            if (pend_nv) {
+                CK(cudaEventSynchronize(c->dl_ev[k ^ 1]));
+                memcpy(host + pend_v0 * outw, c->dl_host + (size_t)(k ^ 1) * cap, pend_nv * outw * sizeof(double));
+            }
+            CK(cudaEventRecord(c->dl_ev[k], c->stream));
+            pend_v0 = v0;
+            pend_nv = nv;
+        }
+        done_v += nv;
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    if (!pinned && pend_nv)
+        memcpy(host + pend_v0 * outw, c->dl_host + (size_t)(k ^ 1) * cap, pend_nv * outw * sizeof(double));
+    (void)done_v;
     return EVPG_OK;
 }
 

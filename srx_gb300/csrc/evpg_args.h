@@ -168,6 +168,25 @@ struct EndReduceArgs {
     double wgt;
 };
 
+// Fused z and y passes: one CTA per (x plane, component pair), warp-register
+// FFTs along z and y, the plane's half spectra staged in shared memory.
+constexpr int PLANE_THREADS = 512;
+constexpr int PLANE_WARPS = PLANE_THREADS / 32;
+
+template <typename T> struct PlaneArgs {
+    Grid g;
+    const Macro* macro;
+    int gate;
+    const T* sig;        // [6][N] real (forward)
+    T* dg;               // [9][N] real (inverse, += correction)
+    C2<T>* spec;         // [9][Nh]
+    const C2<T>* twz;    // W_n2^t
+    const C2<T>* twy;    // W_n1^t
+    const double* dE9;   // macro correction added in the inverse pass
+    T invN;
+    int nhp;             // row length of the shared-memory planes (odd, >= nh)
+};
+
 // Everything one RVE context launches, with grid sizes and dynamic shared
 // memory, in the context's working precision T.
 template <typename T> struct SpecSet {
@@ -176,6 +195,11 @@ template <typename T> struct SpecSet {
     XArgs<T> x;
     int grid_z, grid_y, grid_x;
     size_t sm_z, sm_y, sm_x;
+    // fused z+y passes (epl = n2/32 = n1/32 elements per lane; 0: not used)
+    PlaneArgs<T> pl;
+    int epl;
+    int grid_pf, grid_pi;
+    size_t sm_p;
 };
 
 template <typename T> struct NrSet {

@@ -102,6 +102,7 @@ struct Batch {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     int prologue_kernels = 0, body_kernels = 0;
+    int epl = 0;               // fused z+y passes in the batched launches
     long long launches = 0;
     long long rounds = 0;
 };
@@ -177,6 +178,26 @@ static cudaError_t build_tables_t(Batch& b) {
             if (s.sm_z > smz) smz = s.sm_z;
             if (s.sm_y > smy) smy = s.sm_y;
             if (s.sm_x > smx) smx = s.sm_x;
+        }
+        // fused z+y passes only when every slot uses them with one lane layout
+        int epl = sset<T>(*b.slots[0]).epl;
+        for (Ctx* c : b.slots)
+            if (sset<T>(*c).epl != epl) epl = 0;
+        b.epl = epl;
+        if (epl) {
+            std::vector<PlaneArgs<T>> pa;
+            std::vector<int> gf, gi;
+            size_t smp = 0;
+            for (Ctx* c : b.slots) {
+                const SpecSet<T>& s = sset<T>(*c);
+                pa.push_back(s.pl);
+                pa.back().gate = GATE_RUNNING;
+                gf.push_back(s.grid_pf);
+                gi.push_back(s.grid_pi);
+                if (s.sm_p > smp) smp = s.sm_p;
+            }
+            if (e == cudaSuccess) e = put_table(b, BL_PF, pa, gf, smp);
+            if (e == cudaSuccess) e = put_table(b, BL_PI, pa, gi, smp);
         }
         if (e == cudaSuccess) e = put_table(b, BL_Z, z, gz, smz);
         if (e == cudaSuccess) e = put_table(b, BL_YF, yf, gy, smy);
@@ -300,7 +321,8 @@ static int build_graph(Batch& b) {
         launch_spectral(*c0, GATE_RUNNING);
         launch_nr(*c0, 0, GATE_RUNNING);
         launch_macro(*c0);
-        nb = 7;
+        const int fused = c0->precision ? c0->ks->s32.epl : c0->ks->s64.epl;
+        nb = (fused ? 3 : 5) + 2;
         if (c0->precision != 0) {
             launch_fold(*c0, GATE_ENDING);
             launch_nr(*c0, 1, GATE_ENDING);
@@ -310,10 +332,10 @@ static int build_graph(Batch& b) {
         nb += 2;
         c0->stream = cs;
     } else {
-        launch_spectral_batch(b.precision, b.L, b.stream);
+        launch_spectral_batch(b.precision, b.L, b.stream, b.epl);
         launch_nr_batch(b.precision, b.nr_mode, b.L[BL_NR], b.stream);
         launch_macro_batch(b.L[BL_MACRO], b.stream);
-        nb = 7;
+        nb = b.epl ? 5 : 7;
         launch_end_batch(b.precision, b.nr_mode, b.L, b.stream);
         nb += (b.precision != 0) ? 4 : 2;
     }

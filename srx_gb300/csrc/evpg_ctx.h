@@ -9,6 +9,13 @@ namespace evpg {
 
 // Kernel groups timed by the optional profiler (CUDA events on the context's
 // stream around each launch).
+// doubles per download chunk (packed records, at most 12 per voxel); two
+// chunks per buffer
+constexpr size_t DL_CHUNK_DOUBLES = (size_t)1 << 22;
+inline size_t dl_chunk_doubles(size_t nvox) {
+    return 12 * nvox < DL_CHUNK_DOUBLES ? 12 * nvox : DL_CHUNK_DOUBLES;
+}
+
 enum ProfGroup { PG_FWD_Z, PG_FWD_Y, PG_X_GREEN, PG_INV_Y, PG_INV_Z, PG_NR, PG_MACRO,
                  PG_BEGIN, PG_END, PG_REFINE, PG_COUNT };
 
@@ -49,8 +56,12 @@ struct Ctx {
     IncrCtl* ctl_host;  // pinned staging of the next increment's controls
     KernelSets* ks;     // launch arguments of every kernel (built at creation)
     int sched_p[3];     // pencils per CTA of the z, y, x passes (0: default)
+    int sched_fused;    // fused z+y passes: -1 default (FP32 bulk when eligible), 0 off, 1 on
     int nsm;            // SM count of the device
     long long version;  // bumped whenever ks changes (batches refresh their tables)
+    double* dl_dev;     // download packing buffers (2 chunks, allocated on first use)
+    double* dl_host;    // pinned staging (2 chunks)
+    cudaEvent_t dl_ev[2];
     void* solo;         // batch of this context alone (evpg_increment's round graph)
     LoopCfg cfg;
     Material<double> m64;
@@ -105,8 +116,11 @@ struct BatchLaunch {
     size_t smem;
 };
 enum BatchKind { BL_Z, BL_YF, BL_X, BL_YI, BL_NR, BL_MACRO, BL_MBEGIN, BL_BEGIN, BL_FOLD,
-                 BL_REFINE, BL_END, BL_ENDR, BL_COUNT };
-cudaError_t launch_spectral_batch(int precision, const BatchLaunch* L, cudaStream_t st);
+                 BL_REFINE, BL_END, BL_ENDR, BL_PF, BL_PI, BL_COUNT };
+// epl > 0: the fused z+y plane kernels (tables BL_PF, BL_PI) with that many
+// elements per lane, else the separate z and y passes
+cudaError_t launch_spectral_batch(int precision, const BatchLaunch* L, cudaStream_t st, int epl);
+int plane_epl(const Grid& g, size_t elem_bytes);
 // NR sweep, macro update for every slot
 cudaError_t launch_nr_batch(int precision, int nr_mode, const BatchLaunch& L, cudaStream_t st);
 cudaError_t launch_macro_batch(const BatchLaunch& L, cudaStream_t st);

@@ -161,4 +161,39 @@ __device__ C2<T>* fft_batch(C2<T>* a, C2<T>* b, int npen, int ps, const FftPlan&
     return in;
 }
 
+// Warp-register FFT of length n = 32*EPL (EPL = 1, 2, 4 or 8): lane l holds
+// x[l + 32 q] in v[q]. Four-step split n = EPL x 32: a length-EPL DFT in
+// registers, twiddles W_n^(l k2), then for every k2 a 32-point radix-2
+// decimation-in-frequency transform across the lanes with shuffles. On
+// return lane l holds X[k2 + EPL * brev5(l)] in v[k2]. tw: W_n^t table.
+__device__ __forceinline__ int brev5(int l) { return (int)(__brev((unsigned)l) >> 27); }
+
+template <typename T, int EPL, int SIGN>
+__device__ __forceinline__ void warp_fft(C2<T> (&v)[EPL], const C2<T>* tw, int lane) {
+    if (EPL == 2) {
+        const C2<T> a = v[0], b = v[1];
+        v[0] = cadd<T>(a, b);
+        v[1] = csub<T>(a, b);
+    } else if (EPL == 4) {
+        dft4<T, SIGN>(v[0], v[1], v[2], v[3]);
+    } else if (EPL == 8) {
+        dft8<T, SIGN>(v);
+    }
+#pragma unroll
+    for (int k2 = 1; k2 < EPL; k2++) v[k2] = cmul<T>(v[k2], twid<T, SIGN>(tw, lane * k2));
+#pragma unroll
+    for (int h = 16; h >= 1; h >>= 1) {
+        const bool hi = (lane & h) != 0;
+        const C2<T> w = twid<T, SIGN>(tw, (lane & (h - 1)) * (16 / h) * EPL);
+#pragma unroll
+        for (int k2 = 0; k2 < EPL; k2++) {
+            const C2<T> u = v[k2];
+            C2<T> p;
+            p.x = __shfl_xor_sync(0xffffffffu, u.x, h);
+            p.y = __shfl_xor_sync(0xffffffffu, u.y, h);
+            v[k2] = hi ? cmul<T>(csub<T>(p, u), w) : cadd<T>(u, p);
+        }
+    }
+}
+
 }  // namespace evpg

@@ -657,12 +657,24 @@ __device__ __forceinline__ void macro_body(const MacroArgs& a, int bid) {
     __syncthreads();
     if (!last) return;
     __threadfence();
-    // last block: sum the block rows in a fixed order, then the macro update
+    // last block: one block row per thread, then the same fixed-order
+    // warp/block tree as above, then the macro update
     __shared__ double tot[NPART_NR];
+#pragma unroll
+    for (int q = 0; q < NPART_NR; q++)
+        v[q] = (int)threadIdx.x < nb ? __ldcg(a.part2 + (size_t)threadIdx.x * NPART_NR + q) : 0.0;
+#pragma unroll
+    for (int q = 0; q < NPART_NR; q++) {
+        double x = v[q];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+        if (lane == 0) red[q][wid] = x;
+    }
+    __syncthreads();
     if (threadIdx.x < NPART_NR) {
-        double s = 0.0;
-        for (int b = 0; b < nb; b++) s += __ldcg(a.part2 + (size_t)b * NPART_NR + threadIdx.x);
-        tot[threadIdx.x] = s;
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += red[threadIdx.x][w];
+        tot[threadIdx.x] = t;
     }
     __syncthreads();
     if (threadIdx.x == 0) {

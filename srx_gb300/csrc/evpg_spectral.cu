@@ -15,6 +15,20 @@ __device__ __forceinline__ void load_tw(C2<T>* tw, const C2<T>* src, int n) {
     for (int i = threadIdx.x; i < n; i += blockDim.x) tw[i] = src[i];
 }
 
+// Asynchronous global -> shared copy of one complex element (cp.async, 8 or
+// 16 bytes, both addresses aligned to the element size); completes at
+// cp_async_wait_all.
+template <typename T>
+__device__ __forceinline__ void cp_async_elem(C2<T>* dst, const C2<T>* src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(d), "l"(src), "n"(sizeof(C2<T>))
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+}
+
 // Forward z: three complex FFTs of (sig[2p] + i sig[2p+1]) per column, split
 // into the two half spectra. bid: CTA index within this RVE's grid.
 template <typename T>
@@ -61,8 +75,9 @@ __device__ __forceinline__ void y_body(const YArgs<T>& a, int bid, unsigned char
         C2<T>* base = a.spec + (size_t)c * g.Nh + (size_t)x * n * nh + kz0;
         for (int i = threadIdx.x; i < n * np; i += blockDim.x) {
             const int y = i / np, kk = i - y * np;
-            bA[kk * ps + y] = base[(size_t)y * nh + kk];
+            cp_async_elem<T>(bA + kk * ps + y, base + (size_t)y * nh + kk);
         }
+        cp_async_wait_all();
         __syncthreads();
         const C2<T>* r = fft_batch<T, SIGN>(bA, bB, np, ps, a.pl, tw);
         for (int i = threadIdx.x; i < n * np; i += blockDim.x) {
@@ -88,8 +103,9 @@ __device__ __forceinline__ void x_green_body(const XArgs<T>& a, const GreenK<T>&
     load_tw<T>(tw, a.tw, n);
     for (int i = threadIdx.x; i < 6 * n * np; i += blockDim.x) {
         const int c = i / (n * np), rem = i - c * n * np, x = rem / np, kk = rem - x * np;
-        bA[(c * np + kk) * ps + x] = a.spec[(size_t)c * g.Nh + x * xs + (size_t)y * nh + kz0 + kk];
+        cp_async_elem<T>(bA + (c * np + kk) * ps + x, a.spec + (size_t)c * g.Nh + x * xs + (size_t)y * nh + kz0 + kk);
     }
+    cp_async_wait_all();
     __syncthreads();
     C2<T>* R = fft_batch<T, -1>(bA, bB, 6 * np, ps, a.pl, tw);
     C2<T>* W = (R == bA) ? bB : bA;
@@ -189,6 +205,192 @@ __device__ __forceinline__ void inv_z_body(const ZArgs<T>& a, int bid, unsigned 
         }
         __syncthreads();
     }
+}
+
+// ---- fused z+y passes on x planes (power-of-two n1 == n2 = 32*E)
+//
+// Forward, CTA (x, pair p): every warp takes z rows of the plane, loads
+// sig[2p] + i sig[2p+1] (coalesced), transforms it in registers, splits the
+// two half spectra through a per-warp row buffer into the shared planes A and
+// B; then every warp takes kz columns of A and B and transforms them along y
+// in registers, in place; finally the planes are stored contiguously
+// (spec[c][x] is one n1*nh block). Inverse, CTA (x, pair p of the nine
+// components): load the planes, inverse along y in place, then per z row the
+// Hermitian pair is rebuilt, inverse-transformed in registers and added to
+// DisGrad (same update as the separate inverse-z pass). No intermediate
+// spectrum goes through global memory between the z and y transforms.
+
+template <typename T, int E>
+__device__ __forceinline__ void plane_fwd_body(const PlaneArgs<T>& a, int bid, unsigned char* smem) {
+    const Grid& g = a.g;
+    const int n = g.n2, nh = g.nh, nhp = a.nhp;
+    const int x = bid / 3, p = bid - 3 * x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    C2<T>* twz = reinterpret_cast<C2<T>*>(smem);
+    C2<T>* twy = twz + n;
+    C2<T>* SA = twy + g.n1;
+    C2<T>* SB = SA + (size_t)g.n1 * nhp;
+    C2<T>* R = SB + (size_t)g.n1 * nhp + (size_t)warp * n;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) twz[i] = a.twz[i];
+    for (int i = threadIdx.x; i < g.n1; i += blockDim.x) twy[i] = a.twy[i];
+    __syncthreads();
+    const T* sa = a.sig + (size_t)(2 * p) * g.N + (size_t)x * g.n1 * n;
+    const T* sb = a.sig + (size_t)(2 * p + 1) * g.N + (size_t)x * g.n1 * n;
+    // rows are software-pipelined: the next row's loads are in flight while
+    // the current row is transformed
+    C2<T> nxt[E];
+    if (warp < g.n1)
+#pragma unroll
+        for (int q = 0; q < E; q++) nxt[q] = mk<T>(sa[(size_t)warp * n + lane + 32 * q], sb[(size_t)warp * n + lane + 32 * q]);
+    for (int y = warp; y < g.n1; y += PLANE_WARPS) {
+        C2<T> v[E];
+#pragma unroll
+        for (int q = 0; q < E; q++) v[q] = nxt[q];
+        const int yn = y + PLANE_WARPS;
+        if (yn < g.n1)
+#pragma unroll
+            for (int q = 0; q < E; q++) nxt[q] = mk<T>(sa[(size_t)yn * n + lane + 32 * q], sb[(size_t)yn * n + lane + 32 * q]);
+        warp_fft<T, E, -1>(v, twz, lane);
+        const int b = brev5(lane);
+#pragma unroll
+        for (int k2 = 0; k2 < E; k2++) R[k2 + E * b] = v[k2];
+        __syncwarp();
+        for (int k = lane; k < nh; k += 32) {
+            const C2<T> z = R[k];
+            const C2<T> w = R[k == 0 ? 0 : n - k];
+            // A = (Z(k) + conj Z(n-k))/2, B = (Z(k) - conj Z(n-k))/(2i)
+            SA[y * nhp + k] = mk<T>((T)0.5 * (z.x + w.x), (T)0.5 * (z.y - w.y));
+            SB[y * nhp + k] = mk<T>((T)0.5 * (z.y + w.y), (T)-0.5 * (z.x - w.x));
+        }
+        __syncwarp();
+    }
+    __syncthreads();
+    for (int c = warp; c < 2 * nh; c += PLANE_WARPS) {
+        C2<T>* S = (c < nh) ? SA : SB;
+        const int kz = (c < nh) ? c : c - nh;
+        C2<T> v[E];
+#pragma unroll
+        for (int q = 0; q < E; q++) v[q] = S[(lane + 32 * q) * nhp + kz];
+        warp_fft<T, E, -1>(v, twy, lane);
+        const int b = brev5(lane);
+#pragma unroll
+        for (int k2 = 0; k2 < E; k2++) S[(k2 + E * b) * nhp + kz] = v[k2];
+    }
+    __syncthreads();
+    C2<T>* oa = a.spec + (size_t)(2 * p) * g.Nh + (size_t)x * g.n1 * nh;
+    C2<T>* ob = a.spec + (size_t)(2 * p + 1) * g.Nh + (size_t)x * g.n1 * nh;
+    for (int i = threadIdx.x; i < g.n1 * nh; i += blockDim.x) {
+        const int y = i / nh, k = i - y * nh;
+        oa[i] = SA[y * nhp + k];
+        ob[i] = SB[y * nhp + k];
+    }
+}
+
+template <typename T, int E>
+__device__ __forceinline__ void plane_inv_body(const PlaneArgs<T>& a, int bid, unsigned char* smem) {
+    const Grid& g = a.g;
+    const int n = g.n2, nh = g.nh, nhp = a.nhp;
+    const int x = bid / 5, p = bid - 5 * x;
+    const int ca = 2 * p, cb = 2 * p + 1;
+    const bool hasb = cb < 9;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    C2<T>* twz = reinterpret_cast<C2<T>*>(smem);
+    C2<T>* twy = twz + n;
+    C2<T>* SA = twy + g.n1;
+    C2<T>* SB = SA + (size_t)g.n1 * nhp;
+    C2<T>* R = SB + (size_t)g.n1 * nhp + (size_t)warp * n;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) twz[i] = a.twz[i];
+    for (int i = threadIdx.x; i < g.n1; i += blockDim.x) twy[i] = a.twy[i];
+    const C2<T>* ia = a.spec + (size_t)ca * g.Nh + (size_t)x * g.n1 * nh;
+    const C2<T>* ib = a.spec + (size_t)(hasb ? cb : ca) * g.Nh + (size_t)x * g.n1 * nh;
+    for (int i = threadIdx.x; i < g.n1 * nh; i += blockDim.x) {
+        const int y = i / nh, k = i - y * nh;
+        cp_async_elem<T>(SA + y * nhp + k, ia + i);
+        if (hasb) cp_async_elem<T>(SB + y * nhp + k, ib + i);
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    for (int c = warp; c < (hasb ? 2 : 1) * nh; c += PLANE_WARPS) {
+        C2<T>* S = (c < nh) ? SA : SB;
+        const int kz = (c < nh) ? c : c - nh;
+        C2<T> v[E];
+#pragma unroll
+        for (int q = 0; q < E; q++) v[q] = S[(lane + 32 * q) * nhp + kz];
+        warp_fft<T, E, 1>(v, twy, lane);
+        const int b = brev5(lane);
+#pragma unroll
+        for (int k2 = 0; k2 < E; k2++) S[(k2 + E * b) * nhp + kz] = v[k2];
+    }
+    __syncthreads();
+    const T ea = (T)a.dE9[ca], eb = hasb ? (T)a.dE9[cb] : (T)0;
+    for (int y = warp; y < g.n1; y += PLANE_WARPS) {
+        T* da = a.dg + (size_t)ca * g.N + ((size_t)x * g.n1 + y) * n;
+        T* db = a.dg + (size_t)(hasb ? cb : ca) * g.N + ((size_t)x * g.n1 + y) * n;
+        // DisGrad of this row, loaded before the transform hides its latency
+        T pa[E], pb[E];
+#pragma unroll
+        for (int q = 0; q < E; q++) {
+            pa[q] = da[lane + 32 * q];
+            pb[q] = hasb ? db[lane + 32 * q] : (T)0;
+        }
+        C2<T> v[E];
+#pragma unroll
+        for (int q = 0; q < E; q++) {
+            const int m = lane + 32 * q;
+            const int mm = m < nh ? m : n - m;
+            const C2<T> u = SA[y * nhp + mm];
+            const C2<T> w = hasb ? SB[y * nhp + mm] : mk<T>((T)0, (T)0);
+            if (m < nh) v[q] = mk<T>(u.x - w.y, u.y + w.x);   // u + i w
+            else v[q] = mk<T>(u.x + w.y, -u.y + w.x);         // conj u + i conj w
+        }
+        warp_fft<T, E, 1>(v, twz, lane);
+        const int b = brev5(lane);
+#pragma unroll
+        for (int k2 = 0; k2 < E; k2++) R[k2 + E * b] = v[k2];
+        __syncwarp();
+#pragma unroll
+        for (int q = 0; q < E; q++) {
+            const int m = lane + 32 * q;
+            const C2<T> z = R[m];
+            da[m] = pa[q] + (ea + z.x * a.invN);
+            if (hasb) db[m] = pb[q] + (eb + z.y * a.invN);
+        }
+        __syncwarp();
+    }
+}
+
+template <typename T, int E>
+__global__ void __launch_bounds__(PLANE_THREADS) k_plane_fwd(const __grid_constant__ PlaneArgs<T> a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    if (!gate_open(a.macro, a.gate)) return;
+    plane_fwd_body<T, E>(a, blockIdx.x, smem);
+}
+
+template <typename T, int E>
+__global__ void __launch_bounds__(PLANE_THREADS) k_plane_inv(const __grid_constant__ PlaneArgs<T> a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    if (!gate_open(a.macro, a.gate)) return;
+    plane_inv_body<T, E>(a, blockIdx.x, smem);
+}
+
+template <typename T, int E>
+__global__ void __launch_bounds__(PLANE_THREADS) kb_plane_fwd(const PlaneArgs<T>* __restrict__ tab,
+                                                              const int2* __restrict__ map) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int2 m = map[blockIdx.x];
+    const PlaneArgs<T>& a = tab[m.x];
+    if (!gate_open(a.macro, a.gate)) return;
+    plane_fwd_body<T, E>(a, m.y, smem);
+}
+
+template <typename T, int E>
+__global__ void __launch_bounds__(PLANE_THREADS) kb_plane_inv(const PlaneArgs<T>* __restrict__ tab,
+                                                              const int2* __restrict__ map) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int2 m = map[blockIdx.x];
+    const PlaneArgs<T>& a = tab[m.x];
+    if (!gate_open(a.macro, a.gate)) return;
+    plane_inv_body<T, E>(a, m.y, smem);
 }
 
 // ---- single-RVE kernels: arguments in the constant bank
@@ -322,9 +524,22 @@ template <> SpecSet<float>& spec_of<float>(KernelSets& k) { return k.s32; }
 
 // Launch arguments of the five spectral kernels for pencils-per-CTA P
 // (z, y, x) and FFT plans pl (x, y, z); dg receives the inverse-z output.
+constexpr size_t PLANE_SMEM_MAX = 200 * 1024;
+
+// Elements per lane of the fused z+y passes for this grid (0: not eligible):
+// n1 == n2 in {32, 64, 128} and the two planes fit in shared memory.
+int plane_epl(const Grid& g, size_t elem) {
+    if (g.n1 != g.n2) return 0;
+    const int E = g.n2 / 32;
+    if (E * 32 != g.n2 || (E != 1 && E != 2 && E != 4)) return 0;
+    const int nhp = g.nh | 1;
+    const size_t sm = (size_t)(g.n2 + g.n1 + 2 * g.n1 * nhp + PLANE_WARPS * g.n2) * elem;
+    return sm <= PLANE_SMEM_MAX ? E : 0;
+}
+
 template <typename T>
 static void fill_spec_t(Ctx& c, SpecSet<T>& s, const int P[3], const FftPlan pl[3], T* sig, T* dg,
-                        const C2<T>* const* tw) {
+                        const C2<T>* const* tw, int fused) {
     const Grid& g = c.g;
     C2<T>* spec = reinterpret_cast<C2<T>*>(c.spec);
     const size_t es = sizeof(C2<T>);
@@ -355,6 +570,13 @@ static void fill_spec_t(Ctx& c, SpecSet<T>& s, const int P[3], const FftPlan pl[
     xa.gk.elast_bc = m.elast_bc;
     s.grid_x = g.n1 * ((g.nh + xa.P - 1) / xa.P);
     s.sm_x = (size_t)(g.n0 + 18 * xa.P * (g.n0 + 1)) * es;
+    s.epl = fused ? plane_epl(g, es) : 0;
+    PlaneArgs<T>& pa = s.pl;
+    pa.g = g; pa.macro = c.macro; pa.gate = GATE_RUNNING; pa.sig = sig; pa.dg = dg; pa.spec = spec;
+    pa.twz = tw[2]; pa.twy = tw[1]; pa.dE9 = za.dE9; pa.invN = za.invN; pa.nhp = g.nh | 1;
+    s.grid_pf = 3 * g.n0;
+    s.grid_pi = 5 * g.n0;
+    s.sm_p = (size_t)(g.n2 + g.n1 + 2 * g.n1 * pa.nhp + PLANE_WARPS * g.n2) * es;
 }
 
 template <typename T>
@@ -367,7 +589,9 @@ static void build_spec_t(Ctx& c, T* sig, T* dg, const C2<T>* const* tw) {
         for (int a = 0; a < 3; a++)
             if (P[a] <= 0) P[a] = d[a];
     }
-    fill_spec_t<T>(c, spec_of<T>(*c.ks), P, c.pl, sig, dg, tw);
+    // fused z+y passes: FP32-bulk by default, FP64 only when chosen (tuner)
+    const int fused = c.sched_fused < 0 ? (sizeof(T) == 4) : c.sched_fused;
+    fill_spec_t<T>(c, spec_of<T>(*c.ks), P, c.pl, sig, dg, tw, fused);
 }
 
 void build_spectral_sets(Ctx& c) {
@@ -392,6 +616,45 @@ template <typename T> static void spec_attributes() {
     cudaFuncSetAttribute(kb_y<T, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
     cudaFuncSetAttribute(kb_y<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
     cudaFuncSetAttribute(kb_x_green<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx - 2048);
+    cudaFuncSetAttribute(k_plane_fwd<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(k_plane_fwd<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(k_plane_fwd<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(k_plane_inv<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(k_plane_inv<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(k_plane_inv<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(kb_plane_fwd<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(kb_plane_fwd<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(kb_plane_fwd<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(kb_plane_inv<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(kb_plane_inv<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(kb_plane_inv<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+}
+
+template <typename T>
+static void plane_launch(int fwd, int E, int grid, size_t sm, cudaStream_t st, const PlaneArgs<T>& a) {
+    if (fwd) {
+        if (E == 1) k_plane_fwd<T, 1><<<grid, PLANE_THREADS, sm, st>>>(a);
+        else if (E == 2) k_plane_fwd<T, 2><<<grid, PLANE_THREADS, sm, st>>>(a);
+        else k_plane_fwd<T, 4><<<grid, PLANE_THREADS, sm, st>>>(a);
+    } else {
+        if (E == 1) k_plane_inv<T, 1><<<grid, PLANE_THREADS, sm, st>>>(a);
+        else if (E == 2) k_plane_inv<T, 2><<<grid, PLANE_THREADS, sm, st>>>(a);
+        else k_plane_inv<T, 4><<<grid, PLANE_THREADS, sm, st>>>(a);
+    }
+}
+
+template <typename T>
+static void plane_launch_batch(int fwd, int E, const BatchLaunch& L, cudaStream_t st) {
+    const PlaneArgs<T>* tab = (const PlaneArgs<T>*)L.tab;
+    if (fwd) {
+        if (E == 1) kb_plane_fwd<T, 1><<<L.nblk, PLANE_THREADS, L.smem, st>>>(tab, L.map);
+        else if (E == 2) kb_plane_fwd<T, 2><<<L.nblk, PLANE_THREADS, L.smem, st>>>(tab, L.map);
+        else kb_plane_fwd<T, 4><<<L.nblk, PLANE_THREADS, L.smem, st>>>(tab, L.map);
+    } else {
+        if (E == 1) kb_plane_inv<T, 1><<<L.nblk, PLANE_THREADS, L.smem, st>>>(tab, L.map);
+        else if (E == 2) kb_plane_inv<T, 2><<<L.nblk, PLANE_THREADS, L.smem, st>>>(tab, L.map);
+        else kb_plane_inv<T, 4><<<L.nblk, PLANE_THREADS, L.smem, st>>>(tab, L.map);
+    }
 }
 
 void spectral_attributes() {
@@ -406,6 +669,20 @@ static cudaError_t spectral_t(Ctx& c, int gate) {
     YArgs<T> yf = s.yf, yi = s.yi;
     XArgs<T> xa = s.x;
     za.gate = yf.gate = yi.gate = xa.gate = gate;
+    if (s.epl) {
+        PlaneArgs<T> pa = s.pl;
+        pa.gate = gate;
+        prof_mark(c, PG_FWD_Z, true);
+        plane_launch<T>(1, s.epl, s.grid_pf, s.sm_p, c.stream, pa);
+        prof_mark(c, PG_FWD_Z, false);
+        prof_mark(c, PG_X_GREEN, true);
+        k_x_green<T><<<s.grid_x, SPEC_THREADS, s.sm_x, c.stream>>>(xa);
+        prof_mark(c, PG_X_GREEN, false);
+        prof_mark(c, PG_INV_Z, true);
+        plane_launch<T>(0, s.epl, s.grid_pi, s.sm_p, c.stream, pa);
+        prof_mark(c, PG_INV_Z, false);
+        return cudaGetLastError();
+    }
     prof_mark(c, PG_FWD_Z, true);
     k_fwd_z<T><<<s.grid_z, SPEC_THREADS, s.sm_z, c.stream>>>(za);
     prof_mark(c, PG_FWD_Z, false);
@@ -431,8 +708,14 @@ cudaError_t launch_spectral(Ctx& c, int gate) {
 // One pass of the spectral chain for a batch: the five launches, each over
 // every RVE of the batch (BL_Z: fwd and inv z, BL_YF, BL_X, BL_YI).
 template <typename T>
-static cudaError_t spectral_batch_t(const BatchLaunch* L, cudaStream_t st) {
+static cudaError_t spectral_batch_t(const BatchLaunch* L, cudaStream_t st, int epl) {
     const BatchLaunch &z = L[BL_Z], &yf = L[BL_YF], &x = L[BL_X], &yi = L[BL_YI];
+    if (epl) {
+        plane_launch_batch<T>(1, epl, L[BL_PF], st);
+        kb_x_green<T><<<x.nblk, SPEC_THREADS, x.smem, st>>>((const XArgs<T>*)x.tab, x.map);
+        plane_launch_batch<T>(0, epl, L[BL_PI], st);
+        return cudaGetLastError();
+    }
     kb_fwd_z<T><<<z.nblk, SPEC_THREADS, z.smem, st>>>((const ZArgs<T>*)z.tab, z.map);
     kb_y<T, -1><<<yf.nblk, SPEC_THREADS, yf.smem, st>>>((const YArgs<T>*)yf.tab, yf.map);
     kb_x_green<T><<<x.nblk, SPEC_THREADS, x.smem, st>>>((const XArgs<T>*)x.tab, x.map);
@@ -441,8 +724,8 @@ static cudaError_t spectral_batch_t(const BatchLaunch* L, cudaStream_t st) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_spectral_batch(int precision, const BatchLaunch* L, cudaStream_t st) {
-    return precision == 0 ? spectral_batch_t<double>(L, st) : spectral_batch_t<float>(L, st);
+cudaError_t launch_spectral_batch(int precision, const BatchLaunch* L, cudaStream_t st, int epl) {
+    return precision == 0 ? spectral_batch_t<double>(L, st, epl) : spectral_batch_t<float>(L, st, epl);
 }
 
 // ------------------------------------------------------------- autotuner
@@ -460,6 +743,7 @@ struct TuneEntry {
     int n0, n1, n2, prec;
     int P[3];
     FftPlan pl[3];
+    int fused;
 };
 static std::mutex g_tune_mu;
 static std::vector<TuneEntry> g_tune_cache;
@@ -513,17 +797,23 @@ static std::vector<std::vector<int>> factor_orders(int n) {
 
 constexpr size_t TUNE_SMEM_MAX = 200 * 1024;
 
+// pass 0: z (forward + inverse), 1: y (forward + inverse), 2: x with the
+// Green contraction, 3: fused z+y plane kernels (forward + inverse)
 template <typename T>
 static float time_pass(Ctx& c, int pass, const int P[3], const FftPlan pl[3], T* sig, T* scratch,
                        const C2<T>* const* tw, cudaEvent_t e0, cudaEvent_t e1) {
     SpecSet<T> s;
-    fill_spec_t<T>(c, s, P, pl, sig, scratch, tw);
-    s.z.gate = s.yf.gate = s.yi.gate = s.x.gate = GATE_ALWAYS;
-    const size_t sm = pass == 0 ? s.sm_z : pass == 1 ? s.sm_y : s.sm_x;
+    fill_spec_t<T>(c, s, P, pl, sig, scratch, tw, pass == 3);
+    s.z.gate = s.yf.gate = s.yi.gate = s.x.gate = s.pl.gate = GATE_ALWAYS;
+    if (pass == 3 && !s.epl) return 1e30f;
+    const size_t sm = pass == 0 ? s.sm_z : pass == 1 ? s.sm_y : pass == 2 ? s.sm_x : s.sm_p;
     if (sm > TUNE_SMEM_MAX) return 1e30f;
     if (pass == 0 && P[0] * c.g.n2 > SPEC_THREADS * INVZ_EPT) return 1e30f;
     auto launch = [&]() {
-        if (pass == 0) {
+        if (pass == 3) {
+            plane_launch<T>(1, s.epl, s.grid_pf, s.sm_p, c.stream, s.pl);
+            plane_launch<T>(0, s.epl, s.grid_pi, s.sm_p, c.stream, s.pl);
+        } else if (pass == 0) {
             k_fwd_z<T><<<s.grid_z, SPEC_THREADS, s.sm_z, c.stream>>>(s.z);
             k_inv_z<T><<<s.grid_z, SPEC_THREADS, s.sm_z, c.stream>>>(s.z);
         } else if (pass == 1) {
@@ -556,6 +846,7 @@ static int tune_t(Ctx& c, T* sig, const C2<T>* const* tw, int force, double* gai
                     c.sched_p[a] = e.P[a];
                     c.pl[a] = e.pl[a];
                 }
+                c.sched_fused = e.fused;
                 build_sets(c);
                 c.version++;
                 if (gain) *gain = 0.0;
@@ -571,13 +862,16 @@ static int tune_t(Ctx& c, T* sig, const C2<T>* const* tw, int force, double* gai
     const SpecSet<T>& cur = spec_of<T>(*c.ks);
     P[0] = cur.z.P; P[1] = cur.yf.P; P[2] = cur.x.P;
     FftPlan pl[3] = {c.pl[0], c.pl[1], c.pl[2]};
-    double t0 = 0.0, t1 = 0.0;
+    double t0 = 0.0, t1 = 0.0, tb[3] = {0.0, 0.0, 0.0};
     const int axis_of_pass[3] = {2, 1, 0};
     const int len_of_pass[3] = {g.n2, g.n1, g.n0};
+    // the fused z+y kernels use the default radix-free warp transforms
+    const float tf = time_pass<T>(c, 3, P, pl, sig, scratch, tw, e0, e1);
+    const bool fused_default = cur.epl != 0;
     for (int pass = 0; pass < 3; pass++) {
         const int ax = axis_of_pass[pass];
         float best = time_pass<T>(c, pass, P, pl, sig, scratch, tw, e0, e1);
-        t0 += best;
+        if (pass == 2 || !fused_default) t0 += best;
         for (const std::vector<int>& f : factor_orders(len_of_pass[pass])) {
             FftPlan trial[3] = {pl[0], pl[1], pl[2]};
             plan_of(len_of_pass[pass], f, trial[ax]);
@@ -598,8 +892,11 @@ static int tune_t(Ctx& c, T* sig, const C2<T>* const* tw, int force, double* gai
                 P[pass] = q;
             }
         }
-        t1 += best;
+        tb[pass] = best;
     }
+    if (fused_default) t0 += tf;
+    const int fused = tf < tb[0] + tb[1] ? 1 : 0;
+    t1 = (fused ? tf : tb[0] + tb[1]) + tb[2];
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     cudaStreamSynchronize(c.stream);
@@ -609,12 +906,14 @@ static int tune_t(Ctx& c, T* sig, const C2<T>* const* tw, int force, double* gai
         c.sched_p[a] = P[a];
         c.pl[a] = pl[a];
     }
+    c.sched_fused = fused;
     build_sets(c);
     c.version++;
     if (gain) *gain = t1 > 0 ? t0 / t1 : 0.0;
     std::lock_guard<std::mutex> lk(g_tune_mu);
     TuneEntry e;
     e.n0 = g.n0; e.n1 = g.n1; e.n2 = g.n2; e.prec = prec;
+    e.fused = fused;
     for (int a = 0; a < 3; a++) {
         e.P[a] = P[a];
         e.pl[a] = pl[a];

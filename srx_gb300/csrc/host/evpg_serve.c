@@ -100,7 +100,7 @@ static void *loader_main(void *arg)
         st = evpg_job_grid(r->input, n);
         if (!st) st = evpg_estimate_bytes(n, s->cfg.precision, 0, &bytes);
         /* orientation rows and allocator granularity */
-        bytes += bytes / 16 + (64 << 20);
+        bytes += bytes / 16 + (16 << 20);
         pthread_mutex_lock(&s->mu);
         if (!st && bytes > s->cfg.hbm_budget) st = EVPG_ERR_NOMEM;
         while (!st && !s->shutdown && s->used + bytes > s->cfg.hbm_budget) pthread_cond_wait(&s->cv_load, &s->mu);

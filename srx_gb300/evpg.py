@@ -161,6 +161,16 @@ class Job:
                                   out.size))
         return out.reshape(self.N, w)
 
+    def download_into(self, field: int, out: np.ndarray) -> np.ndarray:
+        """Download into a caller's C-contiguous float64 array (pinned memory
+        is written directly by the copy engine)."""
+        w = FIELD_WIDTH[field]
+        if out.dtype != np.float64 or not out.flags["C_CONTIGUOUS"] or out.size < self.N * w:
+            raise ValueError("need a C-contiguous float64 array of %d values" % (self.N * w))
+        check(lib().evpg_download(self.ctx, field, out.ctypes.data_as(C.POINTER(C.c_double)),
+                                  out.size))
+        return out
+
     def upload(self, field: int, arr: np.ndarray) -> None:
         a = np.ascontiguousarray(arr, dtype=np.float64).reshape(-1)
         check(lib().evpg_upload(self.ctx, field, a.ctypes.data_as(C.POINTER(C.c_double)), a.size))
@@ -181,6 +191,11 @@ class Job:
         g = C.c_double()
         check(lib().evpg_tune(self.ctx, 1 if force else 0, C.byref(g)))
         return g.value
+
+    def set_fused(self, mode: int) -> None:
+        """Fused z+y passes: -1 default, 0 off, 1 on where eligible."""
+        lib().evpg_set_fused.argtypes = [C.c_void_p, C.c_int32]
+        check(lib().evpg_set_fused(self.ctx, mode))
 
     def schedule(self) -> dict:
         """Pencils per CTA (z, y, x passes) and radix stages (x, y, z axes)."""

@@ -125,3 +125,60 @@ def test_autotuned_schedule(tmp_path):
     with evpg.Job(c["input"], c["rho0"], precision=0, nr_mode=1) as j:
         assert j.tune() == 0.0  # cached
         assert j.schedule() == sched
+
+
+@pytest.mark.parametrize("grid,prec", [((16, 32, 32), 0), ((8, 64, 64), 0), ((8, 64, 64), 1),
+                                       ((4, 128, 128), 1)])
+def test_fused_plane_passes(tmp_path, grid, prec):
+    """The fused z+y plane kernels (warp-register FFTs) against the separate
+    Stockham passes on grids n1 == n2 = 32, 64, 128: FP64 within FFT rounding
+    with the same iterations; FP32 bulk within its tolerance."""
+    from conftest import rel_err
+    from srx_gb300 import rve
+    evpg = _evpg()
+    job = rve.Job(n=grid, load="tension", rate=1e-3, strain_per_step=2e-4, n_steps=2)
+    c = rve.make_case(str(tmp_path / "c"), grid, 6, 21, job, rho0=(0.5, 5.0))
+    res = []
+    for fused in (0, 1):
+        with evpg.Job(c["input"], c["rho0"], precision=prec, nr_mode=1) as j:
+            j.set_fused(fused)
+            assert (j.schedule()["pencils_zyx"][0] == 0) == bool(fused)
+            its = [j.increment(k) for k in range(2)]
+            res.append((its, j.download(evpg.F_SIG6), j.download(evpg.F_RHO_S), j.scalars()))
+    if prec == 0:
+        assert res[0][0] == res[1][0]
+        assert rel_err(res[1][1], res[0][1]) < 1e-9
+        assert rel_err(res[1][2], res[0][2]) < 1e-9
+    else:
+        assert abs(sum(res[0][0]) - sum(res[1][0])) <= 2
+        assert rel_err(res[1][3][7:16], res[0][3][7:16]) < 1e-5
+        l2 = np.linalg.norm(res[1][1] - res[0][1]) / np.linalg.norm(res[0][1])
+        assert l2 < 1e-4, l2
+
+
+def test_batch_with_fused_planes_equals_alone(tmp_path):
+    """Batched fused z+y kernels (every slot n1 == n2 == 32, FP32 bulk) give
+    the same bits as each RVE alone."""
+    from srx_gb300 import rve
+    evpg = _evpg()
+    cases = []
+    for i, (grid, load, sps) in enumerate((((8, 32, 32), "tension", 2e-4), ((16, 32, 32), "shear", 1e-4),
+                                           ((4, 32, 32), "compression", 2e-4))):
+        job = rve.Job(n=grid, load=load, rate=1e-3, strain_per_step=sps, n_steps=2)
+        cases.append(rve.make_case(str(tmp_path / ("f%d" % i)), grid, 5, 40 + i, job, rho0=(0.5, 5.0)))
+    ref = []
+    for c in cases:
+        with evpg.Job(c["input"], c["rho0"], precision=1, nr_mode=1) as j:
+            assert j.schedule()["pencils_zyx"][0] == 0  # fused by default
+            ref.append(([j.increment(k) for k in range(2)], _state(evpg, j)))
+    jobs = [evpg.Job(c["input"], c["rho0"], precision=1, nr_mode=1) for c in cases]
+    try:
+        its, _ = evpg.run_batched(jobs, [2, 2, 2], max_ticks=19)
+        assert its == [r[0] for r in ref]
+        for j, (_, st) in zip(jobs, ref):
+            got = _state(evpg, j)
+            for f, v in st.items():
+                assert np.array_equal(got[f], v), f
+    finally:
+        for j in jobs:
+            j.close()

@@ -142,3 +142,26 @@ def test_fp32_bulk_within_stated_error(tmp_path):
     for k in ("sig", "rho_s"):
         l2 = np.linalg.norm(f[k] - z[k]) / np.linalg.norm(z[k])
         assert l2 < 1e-3, (k, l2)
+
+
+def test_download_paths_agree(tmp_path):
+    """Device-packed downloads: pageable (pinned staging, chunked) and pinned
+    caller buffers give the same records; 72^3 voxels exceed one download
+    chunk for the 12- and 9-component fields."""
+    import torch
+    evpg = _evpg()
+    from srx_gb300 import rve
+    n = (72, 72, 72)
+    job = rve.Job(n=n, load="tension", n_steps=1)
+    c = rve.make_case(str(tmp_path / "c"), n, 12, 5, job)
+    with evpg.Job(c["input"], nr_mode=1, precision=1) as j:
+        j.increment(0)
+        for f in (evpg.F_SIG6, evpg.F_SIG, evpg.F_DISGRAD, evpg.F_RHO_S, evpg.F_EDOT, evpg.F_VELGRAD):
+            a = j.download(f)
+            pin = torch.empty(a.size, dtype=torch.float64, pin_memory=True)
+            b = j.download_into(f, pin.numpy())
+            assert np.array_equal(a.reshape(-1), b), f
+        sig9 = j.download(evpg.F_SIG).reshape(-1, 3, 3)
+        sig6 = j.download(evpg.F_SIG6)
+        assert np.array_equal(sig9[:, [0, 1, 2, 1, 0, 0], [0, 1, 2, 2, 2, 1]], sig6)
+        assert np.array_equal(sig9, np.transpose(sig9, (0, 2, 1)))

@@ -80,10 +80,11 @@ def test_served_results_equal_alone(tmp_path, precision):
 
 
 def test_admission_by_memory_budget(tmp_path):
-    """With room for one request at a time, solves run one after another."""
+    """With room for one request at a time (reservations 26, 19 and 20 MB in a
+    30 MB budget), solves run one after another."""
     evpg = _evpg()
     reqs = _requests(tmp_path)[:3]
-    with evpg.Server(precision=1, nr_mode=1, hbm_budget=100 << 20, max_slots=8, round_ticks=16,
+    with evpg.Server(precision=1, nr_mode=1, hbm_budget=30 << 20, max_slots=8, round_ticks=16,
                      loaders=3) as srv:
         ids = [srv.submit(c["input"], c["steps"], rho0=c["rho0"], switch_step=c["switch"],
                           switch_input=c["switch_input"]) for c in reqs]
