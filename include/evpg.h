@@ -214,6 +214,12 @@ int evpg_set_load(void *ctx, const int32_t velgrad_bc_flag[6], const int32_t str
  * radix stages of the x, y, z axes. */
 int evpg_tune(void *ctx, int32_t force, double *gain);
 int evpg_get_schedule(void *ctx, int32_t pencils[3], int32_t radix[3][12], int32_t nstages[3]);
+/* Relative stress-change tolerance and iteration cap of the per-voxel NR
+ * (the reference: 1e-10 and 500, evolution.c:217-218). The FP64 form
+ * defaults to those; the FP32-bulk loop defaults to 2e-6 (FP32 resolution)
+ * and its final FP64 refinement keeps 1e-10. The tolerance applies to the
+ * working-precision loop sweep, the cap to every sweep. */
+int evpg_set_nr_tolerance(void *ctx, double tol, int32_t itmax);
 /* Fused z+y passes (one x plane per CTA, warp-register FFTs along z and y;
  * n1 == n2 in {32, 64, 128} when the planes fit in shared memory): mode -1
  * default (on for FP32 bulk where eligible), 0 off, 1 on where eligible.

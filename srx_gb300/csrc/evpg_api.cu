@@ -754,6 +754,18 @@ int evpg_tune(void* ctx, int32_t force, double* gain) {
     return EVPG_OK;
 }
 
+int evpg_set_nr_tolerance(void* ctx, double tol, int32_t itmax) {
+    Ctx* c = (Ctx*)ctx;
+    if (!c || !(tol > 0.0) || itmax < 1) return fail(EVPG_ERR_ARG, "bad argument");
+    CK(cudaStreamSynchronize(c->stream));
+    if (c->precision == EVPG_FP32_BULK) c->nr_tol32 = tol;
+    else c->nr_tol64 = tol;
+    c->nr_itmax = itmax;
+    build_sets(*c);
+    c->version++;
+    return EVPG_OK;
+}
+
 int evpg_set_fused(void* ctx, int32_t mode) {
     Ctx* c = (Ctx*)ctx;
     if (!c || mode < -1 || mode > 1) return fail(EVPG_ERR_ARG, "bad argument");

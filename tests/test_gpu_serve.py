@@ -103,3 +103,32 @@ def test_request_larger_than_budget_fails(tmp_path):
         srv.wait(60)
         info = srv.request(rid)
         assert info.state == 5 and info.status == 3  # EVPG_ERR_NOMEM
+
+
+def test_failing_request_fails_alone(tmp_path):
+    """xy shear at 2e-4 per increment makes the Newton-Raphson fail in its
+    first iteration (the reference's own NR fails there too). In the server
+    that request ends with its error status; the requests around it finish
+    with the same results as alone."""
+    from srx_gb300 import rve
+    evpg = _evpg()
+    good = _requests(tmp_path)[:2]
+    n = (16, 16, 16)
+    job = rve.Job(n=n, load="shear", rate=1e-3, strain_per_step=2e-4, n_steps=2)
+    bad = rve.make_case(str(tmp_path / "bad"), n, 8, 7, job, rho0=(0.5, 5.0))
+    with evpg.Job(bad["input"], bad["rho0"], precision=1, nr_mode=1) as j:
+        with pytest.raises(evpg.EvpgError) as ei:
+            j.increment(0)
+        assert ei.value.status in (4, 5, 6)  # NaN, singular, line search
+    ref = [_alone(evpg, c, 1) for c in good]
+    with evpg.Server(precision=1, nr_mode=1, max_slots=4, round_ticks=11, keep_fields=True) as srv:
+        ids = [srv.submit(good[0]["input"], good[0]["steps"], rho0=good[0]["rho0"]),
+               srv.submit(bad["input"], 2, rho0=bad["rho0"]),
+               srv.submit(good[1]["input"], good[1]["steps"], rho0=good[1]["rho0"])]
+        srv.wait(600)
+        info = srv.request(ids[1])
+        assert info.state == 5 and info.status in (4, 5, 6)
+        for rid, c, (sig, rho, sc) in zip((ids[0], ids[2]), good, ref):
+            assert srv.request(rid).state == 4
+            gs, gr, gsc = srv.result(rid, c["N"])
+            assert np.array_equal(gs, sig) and np.array_equal(gr, rho) and np.array_equal(gsc, sc)
