@@ -81,6 +81,27 @@ enum { NI, NR, NSTR };
 typedef struct { const char *name; void *ptr; int type, len, status; } nlent;
 
 /* GetNameList, io.c:96-164 */
+/* Reentrant tokenizer with strtok_r semantics (loader threads of the server
+ * parse namelists concurrently; strtok keeps process-wide state). */
+static char *tok_next(char *str, const char *delim, char **save)
+{
+    char *s = str ? str : *save, *e;
+    if (!s) return NULL;
+    s += strspn(s, delim);
+    if (!*s) {
+        *save = s;
+        return NULL;
+    }
+    e = s + strcspn(s, delim);
+    if (*e) {
+        *e = 0;
+        *save = e + 1;
+    } else {
+        *save = e;
+    }
+    return s;
+}
+
 static int read_namelist(const char *path, evpg_namelist *nl)
 {
     nlent t[] = {
@@ -108,7 +129,7 @@ static int read_namelist(const char *path, evpg_namelist *nl)
         {"tau_DRX", &nl->tau_DRX, NR, 1, 0}, {"DeltaTau_DRX", &nl->DeltaTau_DRX, NR, 1, 0},
     };
     const int nt = (int)(sizeof t / sizeof t[0]);
-    char buff[200], *tok;
+    char buff[200], *tok, *save = NULL;
     FILE *fp = fopen(path, "r");
     int k, j;
     if (!fp) return -1;
@@ -117,14 +138,14 @@ static int read_namelist(const char *path, evpg_namelist *nl)
         if (!fgets(buff, 200, fp)) break;
         if (feof(fp)) break;
         if (buff[0] == '#' || buff[0] == '\n') continue;
-        tok = strtok(buff, " \t\n");
+        tok = tok_next(buff, " \t\n", &save);
         if (!tok) break;
         for (k = 0; k < nt; k++) {
             if (strcmp(tok, t[k].name) != 0) continue;
             if (t[k].status == 0) {
                 t[k].status = 1;
                 for (j = 0; j < t[k].len; j++) {
-                    tok = strtok(NULL, ", \t\n");
+                    tok = tok_next(NULL, ", \t\n", &save);
                     if (!tok) break;
                     if (t[k].type == NI) ((int *)t[k].ptr)[j] = (int)atol(tok);
                     else if (t[k].type == NR) ((double *)t[k].ptr)[j] = atof(tok);

@@ -40,3 +40,33 @@ def test_no_cpu_fallback_without_device(tmp_path):
     with pytest.raises(evpg.EvpgError) as e:
         evpg.Job(case["input"])
     assert e.value.status == 9  # EVPG_ERR_NO_DEVICE
+
+
+def test_namelist_parsing_is_thread_safe(tmp_path):
+    """The server's loader threads parse namelists concurrently: many threads
+    reading different files get their own grids (no shared tokenizer state)."""
+    import ctypes as C
+    import threading
+    from srx_gb300 import evpg, rve
+    L = evpg.lib()
+    L.evpg_job_grid.argtypes = [C.c_char_p, C.POINTER(C.c_int32)]
+    paths = []
+    for i in range(12):
+        n = (8 + i, 9 + 2 * i, 10 + 3 * i)
+        p = str(tmp_path / ("input%d" % i))
+        rve.write_namelist(p, rve.Job(n=n, load=["tension", "shear"][i % 2]), rve.Material(), "ms.txt", "cu.sx")
+        paths.append((p, n))
+    bad = []
+
+    def worker(k):
+        out = (C.c_int32 * 3)()
+        for r in range(200):
+            p, n = paths[(k + r) % len(paths)]
+            if L.evpg_job_grid(p.encode(), out) != 0 or tuple(out) != n:
+                bad.append((p, tuple(out), n))
+    ts = [threading.Thread(target=worker, args=(k,)) for k in range(8)]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    assert not bad, bad[:3]
