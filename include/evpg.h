@@ -216,7 +216,7 @@ int evpg_tune(void *ctx, int32_t force, double *gain);
 int evpg_get_schedule(void *ctx, int32_t pencils[3], int32_t radix[3][12], int32_t nstages[3]);
 /* Relative stress-change tolerance and iteration cap of the per-voxel NR
  * (the reference: 1e-10 and 500, evolution.c:217-218). The FP64 form
- * defaults to those; the FP32-bulk loop defaults to 2e-6 (FP32 resolution)
+ * defaults to those; the FP32-bulk loop defaults to 1e-5
  * and its final FP64 refinement keeps 1e-10. The tolerance applies to the
  * working-precision loop sweep, the cap to every sweep. */
 int evpg_set_nr_tolerance(void *ctx, double tol, int32_t itmax);

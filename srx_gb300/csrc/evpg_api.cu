@@ -314,7 +314,7 @@ int evpg_create(const evpg_rve_desc* d, void** out) {
     c->n_orient = d->n_orient;
     c->nr_itmax = 500;
     c->nr_tol64 = 1E-10;
-    c->nr_tol32 = 2E-6;
+    c->nr_tol32 = 1E-5;  // FP32: same iteration counts and errors as 2e-6 at 64^3 and 128^3, 6 % faster
     c->delta_tau_drx = d->delta_tau_drx;
     c->tau_drx = d->tau_drx;
     memcpy(c->udot_a, d->udot_a, sizeof c->udot_a);
