@@ -7,7 +7,9 @@
  * the same macros with one change: DD_CU is left undefined, so the elastic
  * constants come from the namelist's ElastConst_PhaseI instead of the
  * temperature formula at init.c:822-826 (the reference README.txt:2 allows
- * this). Every other flag matches evpFlags.h as shipped.
+ * this). Every other flag matches evpFlags.h as shipped; the optional
+ * flavours switch on NR_MODIFIED (SRX_ORACLE_NR_MODIFIED) and DD_POWER_LAW
+ * (SRX_ORACLE_POWER_LAW), both commented-out options of evpFlags.h.
  */
 #ifndef EVPFLAGS_H
 #define EVPFLAGS_H
@@ -21,6 +23,9 @@
 #define FORWARD_PLUS_BACKWARD
 #ifdef SRX_ORACLE_NR_MODIFIED
 #define NR_MODIFIED /* line-search NR of the FFTW3 variant */
+#endif
+#ifdef SRX_ORACLE_POWER_LAW
+#define DD_POWER_LAW /* power-law flow rule instead of the sinh law (evpFlags.h:24) */
 #endif
 #define PF_DRX
 #ifdef PF_DRX
