@@ -40,6 +40,7 @@ template <typename T> struct GreenK {
     T c0[3][3][3][3];
     T s0[3][3][3][3];
     int elast_bc;
+    T rn[3];   // (T)(1.0 / n_a), the reference's k-vector scaling (init.c:780-797)
 };
 
 template <typename T> struct ZArgs {

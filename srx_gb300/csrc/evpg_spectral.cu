@@ -118,7 +118,7 @@ __device__ __forceinline__ void x_green_body(const XArgs<T>& a, const GreenK<T>&
             green_k0<T>(gk.s0, gk.elast_bc, sb, du);
         } else {
             T nv[3];
-            kvec<T>(kx, ky, kz, g, nv);
+            kvec<T>(kx, ky, kz, gk.rn, nv);
             green_du<T>(gk.c0, nv, sb, du);
             const bool nyq = ((g.n0 & 1) == 0 && 2 * kx == g.n0) ||
                              ((g.n1 & 1) == 0 && 2 * ky == g.n1) ||
@@ -129,7 +129,7 @@ __device__ __forceinline__ void x_green_body(const XArgs<T>& a, const GreenK<T>&
 #pragma unroll
                 for (int c = 0; c < 6; c++) sm[c] = cconj<T>(sb[c]);
                 const int mx = (g.n0 - kx) % g.n0, my = (g.n1 - ky) % g.n1, mz = (g.n2 - kz) % g.n2;
-                kvec<T>(mx, my, mz, g, nv);
+                kvec<T>(mx, my, mz, gk.rn, nv);
                 green_du<T>(gk.c0, nv, sm, dm);
 #pragma unroll
                 for (int c = 0; c < 9; c++)
@@ -458,7 +458,12 @@ __global__ void __launch_bounds__(SPEC_THREADS) kb_x_green(const XArgs<T>* __res
     const T* src = &a.gk.c0[0][0][0][0];
     T* dst = &gks.c0[0][0][0][0];
     for (int i = threadIdx.x; i < 162; i += blockDim.x) dst[i] = src[i];
-    if (threadIdx.x == 0) gks.elast_bc = a.gk.elast_bc;
+    if (threadIdx.x == 0) {
+        gks.elast_bc = a.gk.elast_bc;
+        gks.rn[0] = a.gk.rn[0];
+        gks.rn[1] = a.gk.rn[1];
+        gks.rn[2] = a.gk.rn[2];
+    }
     __syncthreads();
     x_green_body<T>(a, gks, m.y, smem);
 }
@@ -568,6 +573,9 @@ static void fill_spec_t(Ctx& c, SpecSet<T>& s, const int P[3], const FftPlan pl[
         (&xa.gk.s0[0][0][0][0])[i] = (&m.s0[0][0][0][0])[i];
     }
     xa.gk.elast_bc = m.elast_bc;
+    xa.gk.rn[0] = (T)(1.0 / g.n0);
+    xa.gk.rn[1] = (T)(1.0 / g.n1);
+    xa.gk.rn[2] = (T)(1.0 / g.n2);
     s.grid_x = g.n1 * ((g.nh + xa.P - 1) / xa.P);
     s.sm_x = (size_t)(g.n0 + 18 * xa.P * (g.n0 + 1)) * es;
     s.epl = fused ? plane_epl(g, es) : 0;
@@ -1085,6 +1093,9 @@ extern "C" int evpg_green_correction_noalloc(const double* sig6, double* du9, in
         (&xa.gk.s0[0][0][0][0])[i] = s0[i];
     }
     xa.gk.elast_bc = elast_bc;
+    xa.gk.rn[0] = 1.0 / n0;
+    xa.gk.rn[1] = 1.0 / n1;
+    xa.gk.rn[2] = 1.0 / n2;
     const size_t smx = (size_t)(n0 + 18 * xa.P * (n0 + 1)) * es;
     const int ntile_x = (g.nh + xa.P - 1) / xa.P;
     set_kernel_attributes();

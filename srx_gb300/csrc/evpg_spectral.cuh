@@ -22,12 +22,13 @@
 namespace evpg {
 
 // k-space unit vector, init.c:780-797 (TWO_PI as the reference writes it).
+// rn: (T)(1.0/n_a) of the three axes, rounded once on the host.
 template <typename T>
-__device__ __forceinline__ void kvec(int kx, int ky, int kz, const Grid& g, T n[3]) {
+__device__ __forceinline__ void kvec(int kx, int ky, int kz, const T rn[3], T n[3]) {
     T t[3];
-    t[0] = (T)kx * (T)(1.0 / g.n0);
-    t[1] = (T)ky * (T)(1.0 / g.n1);
-    t[2] = (T)kz * (T)(1.0 / g.n2);
+    t[0] = (T)kx * rn[0];
+    t[1] = (T)ky * rn[1];
+    t[2] = (T)kz * rn[2];
 #pragma unroll
     for (int m = 0; m < 3; m++) {
         t[m] -= round(t[m]);
