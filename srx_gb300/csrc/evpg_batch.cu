@@ -93,7 +93,6 @@ struct Batch {
     void* dtab[BL_COUNT] = {};
     int2* dmap[BL_COUNT] = {};
     BatchLaunch L[BL_COUNT] = {};
-    Macro** dmacros = nullptr;
     int* dtk = nullptr;        // [0] tick, [1] kmax
     int* htk = nullptr;        // pinned mirror
     IncrCtl* hctl = nullptr;   // pinned, one per slot
@@ -115,8 +114,6 @@ static void free_tables(Batch& b) {
         b.dmap[k] = nullptr;
         memset(&b.L[k], 0, sizeof(BatchLaunch));
     }
-    if (b.dmacros) cudaFree(b.dmacros);
-    b.dmacros = nullptr;
 }
 
 static void free_graph(Batch& b) {
@@ -257,7 +254,6 @@ static cudaError_t build_tables_t(Batch& b) {
         if (e == cudaSuccess) e = put_table(b, BL_MBEGIN, mp, g1, 0);
         // BL_MBEGIN: nblk counts the slots
         b.L[BL_MBEGIN].nblk = (int)n;
-        b.dmacros = nullptr;
     }
     return e;
 }

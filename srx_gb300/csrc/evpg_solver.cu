@@ -85,13 +85,15 @@ __device__ __forceinline__ void set_status(Macro* m, int st) { atomicCAS(&m->sta
 
 
 __device__ __forceinline__ void sinh_cosh(double x, double& sh, double& ch) {
+    const double e = exp(x);
     if (x < 700.0) {
-        const double e = exp(x), ei = 1.0 / e;
+        const double ei = 1.0 / e;
         sh = 0.5 * (e - ei);
         ch = 0.5 * (e + ei);
     } else {
-        sh = sinh(x);
-        ch = cosh(x);
+        // e^-x is below 1e-304 here: sinh = cosh = e^x / 2 (inf past ~710)
+        sh = 0.5 * e;
+        ch = sh;
     }
 }
 // FP32 overflows at x ~ 89 (FP64 at ~710): the argument is capped at 85,
@@ -146,7 +148,7 @@ __device__ __forceinline__ void flow_eval(const NrArgs<T>& a, int nsys, int v, c
                 for (int q = p; q < 5; q++) dd[k++] += w * sc[q];
             }
         }
-        gam[i * NR_BLOCK] = g;
+        if (gam) gam[i * NR_BLOCK] = g;  // only sweeps that output gamdot keep them
     }
     bool nan = false;
 #pragma unroll
@@ -325,7 +327,7 @@ __device__ __forceinline__ void nr_body(const NrArgs<T>& a, int bid, unsigned ch
 #pragma unroll
                 for (int c = 0; c < 6; c++) old[c] = sig[c];
             }
-            if (!have) flow_eval<T>(a, nsys, v, stg, sig, !trial && stale0 && it == 1, ed, dd, gam, bad);
+            if (!have) flow_eval<T>(a, nsys, v, stg, sig, !trial && stale0 && it == 1, ed, dd, a.gamdot ? gam : nullptr, bad);
             have = false;
             if (bad) break;
             bool finish = false;

@@ -89,7 +89,7 @@ __device__ __forceinline__ void y_body(const YArgs<T>& a, int bid, unsigned char
 }
 
 // Forward x, Green contraction, inverse x on pencils (y, kz..kz+P).
-template <typename T>
+template <typename T, bool SHARED_C0>
 __device__ __forceinline__ void x_green_body(const XArgs<T>& a, const GreenK<T>& gk, int bid,
                                              unsigned char* smem) {
     const Grid& g = a.g;
@@ -100,6 +100,7 @@ __device__ __forceinline__ void x_green_body(const XArgs<T>& a, const GreenK<T>&
     const int ntile = (nh + P - 1) / P;
     const int y = bid / ntile, kz0 = (bid % ntile) * P, np = min(P, nh - kz0);
     const size_t xs = (size_t)g.n1 * nh;
+    const T rn[3] = {gk.rn[0], gk.rn[1], gk.rn[2]};
     load_tw<T>(tw, a.tw, n);
     for (int i = threadIdx.x; i < 6 * n * np; i += blockDim.x) {
         const int c = i / (n * np), rem = i - c * n * np, x = rem / np, kk = rem - x * np;
@@ -118,8 +119,9 @@ __device__ __forceinline__ void x_green_body(const XArgs<T>& a, const GreenK<T>&
             green_k0<T>(gk.s0, gk.elast_bc, sb, du);
         } else {
             T nv[3];
-            kvec<T>(kx, ky, kz, gk.rn, nv);
-            green_du<T>(gk.c0, nv, sb, du);
+            kvec<T>(kx, ky, kz, g, rn, nv);
+            if (SHARED_C0) green_du<T>(C0Shared<T>{&gk.c0[0][0][0][0]}, nv, sb, du);
+            else green_du<T>(C0Param<T>{gk.c0}, nv, sb, du);
             const bool nyq = ((g.n0 & 1) == 0 && 2 * kx == g.n0) ||
                              ((g.n1 & 1) == 0 && 2 * ky == g.n1) ||
                              ((g.n2 & 1) == 0 && 2 * kz == g.n2);
@@ -129,8 +131,9 @@ __device__ __forceinline__ void x_green_body(const XArgs<T>& a, const GreenK<T>&
 #pragma unroll
                 for (int c = 0; c < 6; c++) sm[c] = cconj<T>(sb[c]);
                 const int mx = (g.n0 - kx) % g.n0, my = (g.n1 - ky) % g.n1, mz = (g.n2 - kz) % g.n2;
-                kvec<T>(mx, my, mz, gk.rn, nv);
-                green_du<T>(gk.c0, nv, sm, dm);
+                kvec<T>(mx, my, mz, g, rn, nv);
+                if (SHARED_C0) green_du<T>(C0Shared<T>{&gk.c0[0][0][0][0]}, nv, sm, dm);
+                else green_du<T>(C0Param<T>{gk.c0}, nv, sm, dm);
 #pragma unroll
                 for (int c = 0; c < 9; c++)
                     du[c] = mk<T>((T)0.5 * (du[c].x + dm[c].x), (T)0.5 * (du[c].y - dm[c].y));
@@ -413,7 +416,7 @@ template <typename T>
 __global__ void __launch_bounds__(SPEC_THREADS) k_x_green(const __grid_constant__ XArgs<T> a) {
     extern __shared__ __align__(16) unsigned char smem[];
     if (!gate_open(a.macro, a.gate)) return;
-    x_green_body<T>(a, a.gk, blockIdx.x, smem);
+    x_green_body<T, false>(a, a.gk, blockIdx.x, smem);
 }
 
 template <typename T>
@@ -465,7 +468,7 @@ __global__ void __launch_bounds__(SPEC_THREADS) kb_x_green(const XArgs<T>* __res
         gks.rn[2] = a.gk.rn[2];
     }
     __syncthreads();
-    x_green_body<T>(a, gks, m.y, smem);
+    x_green_body<T, true>(a, gks, m.y, smem);
 }
 
 template <typename T>

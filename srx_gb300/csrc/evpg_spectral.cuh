@@ -22,13 +22,20 @@
 namespace evpg {
 
 // k-space unit vector, init.c:780-797 (TWO_PI as the reference writes it).
-// rn: (T)(1.0/n_a) of the three axes, rounded once on the host.
+// rn: (T)(1.0/n_a) of the three axes, rounded once on the host; used by the
+// FP32 kernels (no FP64 division there), the FP64 kernels divide as written.
 template <typename T>
-__device__ __forceinline__ void kvec(int kx, int ky, int kz, const T rn[3], T n[3]) {
+__device__ __forceinline__ void kvec(int kx, int ky, int kz, const Grid& g, const T rn[3], T n[3]) {
     T t[3];
-    t[0] = (T)kx * rn[0];
-    t[1] = (T)ky * rn[1];
-    t[2] = (T)kz * rn[2];
+    if (sizeof(T) == 8) {
+        t[0] = (T)kx * (T)(1.0 / g.n0);
+        t[1] = (T)ky * (T)(1.0 / g.n1);
+        t[2] = (T)kz * (T)(1.0 / g.n2);
+    } else {
+        t[0] = (T)kx * rn[0];
+        t[1] = (T)ky * rn[1];
+        t[2] = (T)kz * rn[2];
+    }
 #pragma unroll
     for (int m = 0; m < 3; m++) {
         t[m] -= round(t[m]);
@@ -43,8 +50,20 @@ __device__ __forceinline__ void kvec(int kx, int ky, int kz, const T rn[3], T n[
 // du = Gamma(k) : sig_hat, returned as 6 B-basis components of its symmetric
 // part and A12, A13, A23 of its antisymmetric part. Gamma_ijkl = -Omega_ik n_j n_l
 // with Omega = (C0_ijkl n_j n_l)^-1, so du_ij = -n_j (Omega (sig n))_i.
-template <typename T>
-__device__ __forceinline__ void green_du(const T c0[3][3][3][3], const T n[3], const C2<T> sb[6],
+// C0 element access: from the kernel's constant bank (single-RVE kernels) or
+// from shared memory re-read at every use (batched kernels; a cached copy
+// would pin 81 values in registers).
+template <typename T> struct C0Param {
+    const T (&c)[3][3][3][3];
+    __device__ __forceinline__ T operator()(int i, int j, int k, int l) const { return c[i][j][k][l]; }
+};
+template <typename T> struct C0Shared {
+    const volatile T* c;
+    __device__ __forceinline__ T operator()(int i, int j, int k, int l) const { return c[((i * 3 + j) * 3 + k) * 3 + l]; }
+};
+
+template <typename T, typename C0>
+__device__ __forceinline__ void green_du(const C0& c0, const T n[3], const C2<T> sb[6],
                                          C2<T> out[9]) {
     T sr[3][3], si[3][3];
     {
@@ -67,7 +86,7 @@ __device__ __forceinline__ void green_du(const T c0[3][3][3][3], const T n[3], c
 #pragma unroll
             for (int j = 0; j < 3; j++)
 #pragma unroll
-                for (int l = 0; l < 3; l++) s += c0[i][j][k][l] * nn[j][l];
+                for (int l = 0; l < 3; l++) s += c0(i, j, k, l) * nn[j][l];
             a[i][k] = s;
             a[k][i] = s;
         }
