@@ -101,7 +101,6 @@ struct Batch {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     int prologue_kernels = 0, body_kernels = 0;
-    int epl = 0;               // fused z+y passes in the batched launches
     long long launches = 0;
     long long rounds = 0;
 };
@@ -127,6 +126,10 @@ static void free_graph(Batch& b) {
 template <typename A>
 static cudaError_t put_table(Batch& b, int kind, const std::vector<A>& args, const std::vector<int>& grids,
                              size_t smem) {
+    if (args.empty()) {
+        memset(&b.L[kind], 0, sizeof(BatchLaunch));
+        return cudaSuccess;
+    }
     std::vector<int2> map;
     for (size_t i = 0; i < args.size(); i++)
         for (int q = 0; q < grids[i]; q++) map.push_back(make_int2((int)i, q));
@@ -165,36 +168,35 @@ static cudaError_t build_tables_t(Batch& b) {
         std::vector<XArgs<T>> x;
         std::vector<int> gz, gy, gx;
         size_t smz = 0, smy = 0, smx = 0;
+        // every slot runs the spectral variant it runs alone: the fused z+y
+        // plane kernels (one table per lane layout) or the separate passes
+        std::vector<PlaneArgs<T>> pa[3];
+        std::vector<int> gf[3], gi[3];
+        size_t smp[3] = {0, 0, 0};
         for (Ctx* c : b.slots) {
             const SpecSet<T>& s = sset<T>(*c);
+            x.push_back(s.x); x.back().gate = GATE_RUNNING;
+            gx.push_back(s.grid_x);
+            if (s.sm_x > smx) smx = s.sm_x;
+            if (s.epl) {
+                const int q = s.epl == 1 ? 0 : s.epl == 2 ? 1 : 2;
+                pa[q].push_back(s.pl);
+                pa[q].back().gate = GATE_RUNNING;
+                gf[q].push_back(s.grid_pf);
+                gi[q].push_back(s.grid_pi);
+                if (s.sm_p > smp[q]) smp[q] = s.sm_p;
+                continue;
+            }
             z.push_back(s.z); z.back().gate = GATE_RUNNING;
             yf.push_back(s.yf); yf.back().gate = GATE_RUNNING;
             yi.push_back(s.yi); yi.back().gate = GATE_RUNNING;
-            x.push_back(s.x); x.back().gate = GATE_RUNNING;
-            gz.push_back(s.grid_z); gy.push_back(s.grid_y); gx.push_back(s.grid_x);
+            gz.push_back(s.grid_z); gy.push_back(s.grid_y);
             if (s.sm_z > smz) smz = s.sm_z;
             if (s.sm_y > smy) smy = s.sm_y;
-            if (s.sm_x > smx) smx = s.sm_x;
         }
-        // fused z+y passes only when every slot uses them with one lane layout
-        int epl = sset<T>(*b.slots[0]).epl;
-        for (Ctx* c : b.slots)
-            if (sset<T>(*c).epl != epl) epl = 0;
-        b.epl = epl;
-        if (epl) {
-            std::vector<PlaneArgs<T>> pa;
-            std::vector<int> gf, gi;
-            size_t smp = 0;
-            for (Ctx* c : b.slots) {
-                const SpecSet<T>& s = sset<T>(*c);
-                pa.push_back(s.pl);
-                pa.back().gate = GATE_RUNNING;
-                gf.push_back(s.grid_pf);
-                gi.push_back(s.grid_pi);
-                if (s.sm_p > smp) smp = s.sm_p;
-            }
-            if (e == cudaSuccess) e = put_table(b, BL_PF, pa, gf, smp);
-            if (e == cudaSuccess) e = put_table(b, BL_PI, pa, gi, smp);
+        for (int q = 0; q < 3 && e == cudaSuccess; q++) {
+            e = put_table(b, BL_PF1 + q, pa[q], gf[q], smp[q]);
+            if (e == cudaSuccess) e = put_table(b, BL_PI1 + q, pa[q], gi[q], smp[q]);
         }
         if (e == cudaSuccess) e = put_table(b, BL_Z, z, gz, smz);
         if (e == cudaSuccess) e = put_table(b, BL_YF, yf, gy, smy);
@@ -328,10 +330,9 @@ static int build_graph(Batch& b) {
         nb += 2;
         c0->stream = cs;
     } else {
-        launch_spectral_batch(b.precision, b.L, b.stream, b.epl);
+        nb = launch_spectral_batch(b.precision, b.L, b.stream) + 2;
         launch_nr_batch(b.precision, b.nr_mode, b.L[BL_NR], b.stream);
         launch_macro_batch(b.L[BL_MACRO], b.stream);
-        nb = b.epl ? 5 : 7;
         launch_end_batch(b.precision, b.nr_mode, b.L, b.stream);
         nb += (b.precision != 0) ? 4 : 2;
     }

@@ -116,10 +116,13 @@ struct BatchLaunch {
     size_t smem;
 };
 enum BatchKind { BL_Z, BL_YF, BL_X, BL_YI, BL_NR, BL_MACRO, BL_MBEGIN, BL_BEGIN, BL_FOLD,
-                 BL_REFINE, BL_END, BL_ENDR, BL_PF, BL_PI, BL_COUNT };
-// epl > 0: the fused z+y plane kernels (tables BL_PF, BL_PI) with that many
-// elements per lane, else the separate z and y passes
-cudaError_t launch_spectral_batch(int precision, const BatchLaunch* L, cudaStream_t st, int epl);
+                 BL_REFINE, BL_END, BL_ENDR, BL_PF1, BL_PF2, BL_PF4, BL_PI1, BL_PI2, BL_PI4,
+                 BL_COUNT };
+// Spectral chain of a batch: the separate z and y passes over the slots in
+// BL_Z/BL_YF/BL_YI, the fused plane kernels over the slots in BL_PF*/BL_PI*
+// (1, 2, 4 elements per lane), the X pass over all; launches with no slot are
+// skipped. Returns the number of kernels launched.
+int launch_spectral_batch(int precision, const BatchLaunch* L, cudaStream_t st);
 int plane_epl(const Grid& g, size_t elem_bytes);
 // NR sweep, macro update for every slot
 cudaError_t launch_nr_batch(int precision, int nr_mode, const BatchLaunch& L, cudaStream_t st);

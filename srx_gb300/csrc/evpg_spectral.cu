@@ -716,27 +716,39 @@ cudaError_t launch_spectral(Ctx& c, int gate) {
     return c.precision == 0 ? spectral_t<double>(c, gate) : spectral_t<float>(c, gate);
 }
 
-// One pass of the spectral chain for a batch: the five launches, each over
-// every RVE of the batch (BL_Z: fwd and inv z, BL_YF, BL_X, BL_YI).
+// One pass of the spectral chain for a batch (see launch_spectral_batch).
 template <typename T>
-static cudaError_t spectral_batch_t(const BatchLaunch* L, cudaStream_t st, int epl) {
+static int spectral_batch_t(const BatchLaunch* L, cudaStream_t st) {
     const BatchLaunch &z = L[BL_Z], &yf = L[BL_YF], &x = L[BL_X], &yi = L[BL_YI];
-    if (epl) {
-        plane_launch_batch<T>(1, epl, L[BL_PF], st);
-        kb_x_green<T><<<x.nblk, SPEC_THREADS, x.smem, st>>>((const XArgs<T>*)x.tab, x.map);
-        plane_launch_batch<T>(0, epl, L[BL_PI], st);
-        return cudaGetLastError();
+    const int E[3] = {1, 2, 4};
+    int n = 0;
+    for (int q = 0; q < 3; q++)
+        if (L[BL_PF1 + q].nblk) {
+            plane_launch_batch<T>(1, E[q], L[BL_PF1 + q], st);
+            n++;
+        }
+    if (z.nblk) {
+        kb_fwd_z<T><<<z.nblk, SPEC_THREADS, z.smem, st>>>((const ZArgs<T>*)z.tab, z.map);
+        kb_y<T, -1><<<yf.nblk, SPEC_THREADS, yf.smem, st>>>((const YArgs<T>*)yf.tab, yf.map);
+        n += 2;
     }
-    kb_fwd_z<T><<<z.nblk, SPEC_THREADS, z.smem, st>>>((const ZArgs<T>*)z.tab, z.map);
-    kb_y<T, -1><<<yf.nblk, SPEC_THREADS, yf.smem, st>>>((const YArgs<T>*)yf.tab, yf.map);
     kb_x_green<T><<<x.nblk, SPEC_THREADS, x.smem, st>>>((const XArgs<T>*)x.tab, x.map);
-    kb_y<T, 1><<<yi.nblk, SPEC_THREADS, yi.smem, st>>>((const YArgs<T>*)yi.tab, yi.map);
-    kb_inv_z<T><<<z.nblk, SPEC_THREADS, z.smem, st>>>((const ZArgs<T>*)z.tab, z.map);
-    return cudaGetLastError();
+    n++;
+    if (z.nblk) {
+        kb_y<T, 1><<<yi.nblk, SPEC_THREADS, yi.smem, st>>>((const YArgs<T>*)yi.tab, yi.map);
+        kb_inv_z<T><<<z.nblk, SPEC_THREADS, z.smem, st>>>((const ZArgs<T>*)z.tab, z.map);
+        n += 2;
+    }
+    for (int q = 0; q < 3; q++)
+        if (L[BL_PI1 + q].nblk) {
+            plane_launch_batch<T>(0, E[q], L[BL_PI1 + q], st);
+            n++;
+        }
+    return n;
 }
 
-cudaError_t launch_spectral_batch(int precision, const BatchLaunch* L, cudaStream_t st, int epl) {
-    return precision == 0 ? spectral_batch_t<double>(L, st, epl) : spectral_batch_t<float>(L, st, epl);
+int launch_spectral_batch(int precision, const BatchLaunch* L, cudaStream_t st) {
+    return precision == 0 ? spectral_batch_t<double>(L, st) : spectral_batch_t<float>(L, st);
 }
 
 // ------------------------------------------------------------- autotuner

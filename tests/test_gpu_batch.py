@@ -182,3 +182,39 @@ def test_batch_with_fused_planes_equals_alone(tmp_path):
     finally:
         for j in jobs:
             j.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_batch_mixing_fused_and_separate_passes(tmp_path, precision):
+    """Slots with fused plane kernels of two lane layouts (32 and 64 planes)
+    next to slots with the separate passes: each runs its own variant, so the
+    batch gives the same bits as every RVE alone. FP64 contexts are switched
+    to the fused kernels where eligible."""
+    from srx_gb300 import rve
+    evpg = _evpg()
+    cases = []
+    for i, (grid, load, sps) in enumerate((((8, 32, 32), "tension", 2e-4), ((4, 64, 64), "shear", 1e-4),
+                                           ((12, 10, 9), "compression", 2e-4), ((16, 16, 16), "tension", 2e-4))):
+        job = rve.Job(n=grid, load=load, rate=1e-3, strain_per_step=sps, n_steps=2)
+        cases.append(rve.make_case(str(tmp_path / ("m%d" % i)), grid, 5, 60 + i, job, rho0=(0.5, 5.0)))
+
+    def open_job(c):
+        j = evpg.Job(c["input"], c["rho0"], precision=precision, nr_mode=1)
+        j.set_fused(1)
+        return j
+    ref = []
+    for c in cases:
+        with open_job(c) as j:
+            ref.append(([j.increment(k) for k in range(2)], _state(evpg, j)))
+    jobs = [open_job(c) for c in cases]
+    try:
+        assert [j.schedule()["pencils_zyx"][0] == 0 for j in jobs] == [True, True, False, False]
+        its, _ = evpg.run_batched(jobs, [2] * len(jobs), max_ticks=17)
+        assert its == [r[0] for r in ref]
+        for j, (_, st) in zip(jobs, ref):
+            got = _state(evpg, j)
+            for f, v in st.items():
+                assert np.array_equal(got[f], v), f
+    finally:
+        for j in jobs:
+            j.close()
