@@ -42,7 +42,10 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "voxel-iters/s 128^3 FP32-bulk vs FP64 (<=1e-4 sigma err)"
-NR_DRAM_BYTES_PER_VOXEL = 488.6
+# dram__bytes_read.sum + dram__bytes_write.sum of one FP32 NR sweep per voxel, from an
+# ncu capture of the 96^3 / 422-grain case (traffic grows with N: every voxel's state is
+# read and written once); scaled by N for the roofline's "traffic".
+NR_DRAM_BYTES_PER_VOXEL = 488.5
 UNIT = "voxel-iterations/s"
 
 

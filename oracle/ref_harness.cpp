@@ -11,7 +11,7 @@
  *       GetNameList, MPI_Init, PrintNameList, OpenFiles, SetupJob,
  *       [per-voxel initial SSD density from FILE: N doubles, 1e12 m^-2,
  *        the same value on every slip system], Evolution,
- *       [final state dump], DestroyJob, CloseFiles.
+ *       [final state dump, GND densities last], DestroyJob, CloseFiles.
  *
  *   srx_ref <input> --setup FILE
  *       SetupJob, update_schmid() (as the first increment does,
@@ -85,6 +85,8 @@ static void dump_final(const char *path)
     double sc[13] = {e_vm, d_vm, s_vm, s_vm1, TimeTot, rho_F_avg, rho_P_avg, rho_s_avg,
                      rho_m_avg, rho_g_avg, rho_dipole_avg, rho_forest_avg, rho_inplane_avg};
     put(f, sc, sizeof sc);
+    /* GND densities (zero unless built with DD_GND) */
+    put_sys(f, rho_g1); put_sys(f, rho_g2); put_sys(f, rho_g3);
     fclose(f);
 }
 

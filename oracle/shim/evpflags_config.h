@@ -8,8 +8,9 @@
  * constants come from the namelist's ElastConst_PhaseI instead of the
  * temperature formula at init.c:822-826 (the reference README.txt:2 allows
  * this). Every other flag matches evpFlags.h as shipped; the optional
- * flavours switch on NR_MODIFIED (SRX_ORACLE_NR_MODIFIED) and DD_POWER_LAW
- * (SRX_ORACLE_POWER_LAW), both commented-out options of evpFlags.h.
+ * flavours switch on NR_MODIFIED (SRX_ORACLE_NR_MODIFIED), DD_POWER_LAW
+ * (SRX_ORACLE_POWER_LAW) and DD_GND with its DD_GND_FIRST_ORDER companion
+ * (SRX_ORACLE_GND), all commented-out options of evpFlags.h.
  */
 #ifndef EVPFLAGS_H
 #define EVPFLAGS_H
@@ -26,6 +27,10 @@
 #endif
 #ifdef SRX_ORACLE_POWER_LAW
 #define DD_POWER_LAW /* power-law flow rule instead of the sinh law (evpFlags.h:24) */
+#endif
+#ifdef SRX_ORACLE_GND
+#define DD_GND /* geometrically necessary dislocations (evpFlags.h:29-32) */
+#define DD_GND_FIRST_ORDER
 #endif
 #define PF_DRX
 #ifdef PF_DRX
