@@ -14,6 +14,11 @@
  *  - error and average sums are accumulated into per-voxel slots and summed
  *    serially in voxel order, which equals the reference's serial order for
  *    any thread count;
+ *  - with GND densities on (evo_set_gnd, the reference's DD_GND with
+ *    DD_GND_FIRST_ORDER) the slip-rate gradient of each voxel is formed where
+ *    the densities are updated, from the neighbours' shear rates, instead of
+ *    in a separate pass over all voxels (Gradient_ShearRate,
+ *    constitutive.c:881-1112): the shear rates are not changed in between;
  *  - the displacement post-step (evolution.c:1401-1425) is restated by what
  *    it computes as written: its per-frequency sums go into scalars and one
  *    element past fft_data, so the inverse transform acts on the forward
@@ -177,6 +182,13 @@ struct evo_job {
         (*gam_acum)[NS], (*trial_gam_acum)[NS], (*rho_dipole)[NS], (*rho_forest)[NS],
         (*rho_inplane)[NS], (*rho_dot_s)[NS];
     double *rho_tot;
+    /* first-order GND densities (DD_GND): rho_g1 screw, rho_g2 edge type I; the
+     * edge type II density stays zero to first order (constitutive.c:1494-1518) */
+    int gnd;
+    double (*rho_g1)[NS], (*rho_g2)[NS];
+    unsigned char *gb;    /* same-grain neighbour bits, see gb_masks() */
+    double bp[NPH][NS][3];                       /* b x n, init.c:198-203 */
+    double cos_g1[NPH][NS][NS], sin_g1[NPH][NS][NS], cos_g2[NPH][NS][NS], sin_g2[NPH][NS][NS];
     double *kr, *ki;      /* kSig_r/kSig_i, [N][9] */
     double *fft;          /* N complex */
     double *vox_e, *vox_s;
@@ -482,6 +494,10 @@ static int plastic_init(evo_job *j, const char *path, int phase)
             norm = 0.0;
             for (mx = 0; mx < 3; mx++) norm += j->bn[phase][k][mx] * j->bb[phase][k][mx];
             if (norm > 1E-3) return -4;
+            /* sense vector p = b x n, init.c:198-203 */
+            j->bp[phase][k][0] = j->bb[phase][k][1] * j->bn[phase][k][2] - j->bb[phase][k][2] * j->bn[phase][k][1];
+            j->bp[phase][k][1] = j->bb[phase][k][2] * j->bn[phase][k][0] - j->bb[phase][k][0] * j->bn[phase][k][2];
+            j->bp[phase][k][2] = j->bb[phase][k][0] * j->bn[phase][k][1] - j->bb[phase][k][1] * j->bn[phase][k][0];
             for (a = 0; a < 3; a++)
                 for (b = 0; b < 3; b++)
                     aux[a][b] = (j->bn[phase][k][a] * j->bb[phase][k][b] +
@@ -511,6 +527,7 @@ static int alloc_fields(evo_job *j)
     ok &= ALLOC(j->rho_dipole, N) != 0; ok &= ALLOC(j->rho_forest, N) != 0;
     ok &= ALLOC(j->rho_inplane, N) != 0; ok &= ALLOC(j->rho_dot_s, N) != 0;
     ok &= ALLOC(j->rho_tot, N) != 0;
+    ok &= ALLOC(j->rho_g1, N) != 0; ok &= ALLOC(j->rho_g2, N) != 0; ok &= ALLOC(j->gb, N) != 0;
     ok &= ALLOC(j->kr, 9 * (size_t)N) != 0; ok &= ALLOC(j->ki, 9 * (size_t)N) != 0;
     ok &= ALLOC(j->fft, 2 * (size_t)N) != 0;
     ok &= ALLOC(j->vox_e, N) != 0; ok &= ALLOC(j->vox_s, N) != 0; ok &= ALLOC(j->vox_flag, N) != 0;
@@ -616,6 +633,33 @@ static double shear_modulus(const double *ec)
            (0.5) * (5 * (ec[0] - ec[1]) * ec[2]) / (4 * ec[2] + 3 * (ec[0] - ec[1]));
 }
 
+/* Gradient_ExchangeGrainID, constitutive.c:731-879, on one rank (periodic
+ * neighbours): bit 0/1 x+/x- neighbour in the same grain, 2/3 y+/y-, 4 z+,
+ * 5 the "z-" check, which compares with the y- neighbour as the reference
+ * does (GB_checkZ[pIDX][1], constitutive.c:821, 842, 859). */
+static void gb_masks(evo_job *j)
+{
+    const int n0 = j->n0, n1 = j->n1, n2 = j->n2;
+    int x, y, z;
+    for (x = 0; x < n0; x++)
+        for (y = 0; y < n1; y++)
+            for (z = 0; z < n2; z++) {
+                const int xp = (x + 1) % n0, xm = (x + n0 - 1) % n0, yp = (y + 1) % n1,
+                          ym = (y + n1 - 1) % n1, zp = (z + 1) % n2;
+                const int v = (x * n1 + y) * n2 + z, g = j->grain_f[v];
+                unsigned char m = 0;
+                m |= (g == j->grain_f[(xp * n1 + y) * n2 + z]) << 0;
+                m |= (g == j->grain_f[(xm * n1 + y) * n2 + z]) << 1;
+                m |= (g == j->grain_f[(x * n1 + yp) * n2 + z]) << 2;
+                m |= (g == j->grain_f[(x * n1 + ym) * n2 + z]) << 3;
+                m |= (g == j->grain_f[(x * n1 + y) * n2 + zp]) << 4;
+                m |= (g == j->grain_f[(x * n1 + ym) * n2 + z]) << 5;
+                j->gb[v] = m;
+            }
+}
+
+void evo_set_gnd(evo_job *j, int on) { j->gnd = on ? 1 : 0; }
+
 evo_job *evo_open(const char *input_path, const char *rho0_path, char *err, int errlen)
 {
     evo_job *j = calloc(1, sizeof(evo_job));
@@ -710,6 +754,23 @@ evo_job *evo_open(const char *input_path, const char *rho0_path, char *err, int 
         interaction(0.0, 0.0, j->nl.CrossSlip0[ph], j->nl.GlissileJunction0[ph],
                     j->nl.HirthLock0[ph], j->nl.LomerCottrellLock0[ph], j->Chi_1[ph]);
     }
+    /* projection angles of the GND densities, init.c:1119-1140 */
+    for (ph = 0; ph < NPH; ph++)
+        for (i = 0; i < j->nSYS[ph]; i++)
+            for (a = 0; a < j->nSYS[ph]; a++) {
+                const double *ni = j->bn[ph][i], *nj = j->bn[ph][a], *bj = j->bb[ph][a];
+                double sv[3], cs, c1;
+                sv[0] = nj[1] * bj[2] - nj[2] * bj[1];
+                sv[1] = nj[2] * bj[0] - nj[0] * bj[2];
+                sv[2] = nj[0] * bj[1] - nj[1] * bj[0];
+                cs = fabs(ni[0] * sv[0] + ni[1] * sv[1] + ni[2] * sv[2]);
+                c1 = fabs(ni[0] * bj[0] + ni[1] * bj[1] + ni[2] * bj[2]);
+                j->cos_g1[ph][i][a] = c1;
+                j->sin_g1[ph][i][a] = fabs(sqrt(fabs(1.0 - c1 * c1)));
+                j->cos_g2[ph][i][a] = cs;
+                j->sin_g2[ph][i][a] = fabs(sqrt(fabs(1.0 - cs * cs)));
+            }
+    gb_masks(j);
     /* InitFields, init.c:444-516 */
     for (a = 0; a < 3; a++)
         for (b = 0; b < 3; b++) j->DisGradAvg[a][b] = j->Udot[a][b] * j->nl.TimeStep;
@@ -740,7 +801,7 @@ void evo_close(evo_job *j)
     free(j->VelGrad); free(j->TranMat); free(j->fluct); free(j->disp); free(j->Schm_gr); free(j->rho_s);
     free(j->rho_m); free(j->rho_F); free(j->rho_P); free(j->gamdot); free(j->gam_acum);
     free(j->trial_gam_acum); free(j->rho_dipole); free(j->rho_forest); free(j->rho_inplane);
-    free(j->rho_dot_s); free(j->rho_tot); free(j->kr); free(j->ki); free(j->fft);
+    free(j->rho_dot_s); free(j->rho_tot); free(j->rho_g1); free(j->rho_g2); free(j->gb); free(j->kr); free(j->ki); free(j->fft);
     free(j->vox_e); free(j->vox_s); free(j->vox_flag);
     free(j);
 }
@@ -764,6 +825,8 @@ double *evo_field(evo_job *j, const char *n)
     if (!strcmp(n, "rho_forest")) return &j->rho_forest[0][0];
     if (!strcmp(n, "rho_inplane")) return &j->rho_inplane[0][0];
     if (!strcmp(n, "rho_tot")) return j->rho_tot;
+    if (!strcmp(n, "rho_g1")) return &j->rho_g1[0][0];
+    if (!strcmp(n, "rho_g2")) return &j->rho_g2[0][0];
     if (!strcmp(n, "Schm_gr")) return &j->Schm_gr[0][0][0];
     if (!strcmp(n, "C066")) return &j->C066[0][0];
     if (!strcmp(n, "S066")) return &j->S066[0][0];
@@ -818,8 +881,9 @@ void evo_update_schmid(evo_job *j)
 /* kT (evp.h:93) and the reduced activation energy (constitutive.c:543) */
 static double kT_of(const evo_job *j) { return (j->nl.T__K * BOLZ * (1.0 / EV_IN_J)); }
 
-/* StrainRate_Orowan, constitutive.c:507-728 (FORWARD_PLUS_BACKWARD, DD_GND
- * off, so every GND density is zero and rho_F == rho_f). Returns 1 on NaN. */
+/* StrainRate_Orowan, constitutive.c:507-728 (FORWARD_PLUS_BACKWARD; rho_F ==
+ * rho_f). The GND densities enter rho_F and rho_P through their projections
+ * (constitutive.c:558-577); with DD_GND off they are zero. Returns 1 on NaN. */
 static int strain_rate(evo_job *j, const double *stress, double *edot, double d_edot[6][6],
                        int idx, int jph)
 {
@@ -834,16 +898,33 @@ static int strain_rate(evo_job *j, const double *stress, double *edot, double d_
     double(*sc)[5] = j->Schm_gr[idx];
     int i, k, m, bad = 0;
     for (i = 0; i < ns; i++) rhoS[i] = j->rho_s[idx][i]; /* trial_rho_s == rho_s */
-    for (i = 0; i < ns; i++) {
-        double F = 0.0, P = 0.0, f = 0.0;
-        for (k = 0; k < ns; k++) {
-            F += j->Chi_1[p][i][k] * (rhoS[k] + 0.0 + 0.0 + 0.0);
-            f += j->Chi_1[p][i][k] * (rhoS[k] + 0.0 + 0.0 + 0.0);
-            P += j->Chi[p][i][k] * (rhoS[k] + 0.0 + 0.0 + 0.0);
+    if (j->gnd) {
+        /* trial_rho_g == rho_g; rho_g3 == 0 (first order) */
+        const double *g1 = j->rho_g1[idx], *g2 = j->rho_g2[idx];
+        for (i = 0; i < ns; i++) {
+            double F = 0.0, P = 0.0;
+            for (k = 0; k < ns; k++) {
+                F += j->Chi_1[p][i][k] * (rhoS[k] + fabs(g1[k] * j->cos_g1[p][i][k]) +
+                                          fabs(g2[k] * j->cos_g2[p][i][k]) + 0.0);
+                P += j->Chi[p][i][k] * (rhoS[k] + fabs(g1[k] * j->sin_g1[p][i][k]) +
+                                        fabs(g2[k] * j->sin_g2[p][i][k]) + 0.0);
+            }
+            j->rho_F[idx][i] = F;
+            j->rho_P[idx][i] = P;
+            rho_f[i] = F;
         }
-        j->rho_F[idx][i] = F;
-        j->rho_P[idx][i] = P;
-        rho_f[i] = f;
+    } else {
+        for (i = 0; i < ns; i++) {
+            double F = 0.0, P = 0.0, f = 0.0;
+            for (k = 0; k < ns; k++) {
+                F += j->Chi_1[p][i][k] * (rhoS[k] + 0.0 + 0.0 + 0.0);
+                f += j->Chi_1[p][i][k] * (rhoS[k] + 0.0 + 0.0 + 0.0);
+                P += j->Chi[p][i][k] * (rhoS[k] + 0.0 + 0.0 + 0.0);
+            }
+            j->rho_F[idx][i] = F;
+            j->rho_P[idx][i] = P;
+            rho_f[i] = f;
+        }
     }
     for (i = 0; i < ns; i++) {
         tau_pass = c_1 * shear_G * j->bb_B[p][i] * sqrt(fabs(j->rho_P[idx][i] + j->rho_m[idx][i])) *
@@ -1308,9 +1389,40 @@ static void reorient_voxel(evo_job *j, int v)
     memcpy(j->TranMat[v], tn, sizeof(t2));
 }
 
+/* One directional derivative of Gradient_ShearRate (constitutive.c:881-1112)
+ * from the same-grain bits of the plus and minus neighbours: backward, forward
+ * or central difference, or zero with no same-grain neighbour. */
+static double gb_diff(double c, double vp, double vm, int same_p, int same_m)
+{
+    if (!same_p && same_m) return c - vm;
+    if (same_p && !same_m) return vp - c;
+    if (same_p && same_m) return (vp - vm) / 2.0;
+    return 0.0;
+}
+
+/* gadot_grad[v][i] (constitutive.c:881-1112, one rank: periodic neighbours) */
+static void shear_rate_gradient(const evo_job *j, int v, int i, double gr[3])
+{
+    const int n0 = j->n0, n1 = j->n1, n2 = j->n2;
+    const int x = v / (n1 * n2), y = (v / n2) % n1, z = v % n2;
+    const int xp = (x + 1) % n0, xm = (x + n0 - 1) % n0, yp = (y + 1) % n1, ym = (y + n1 - 1) % n1,
+              zp = (z + 1) % n2, zm = (z + n2 - 1) % n2;
+    const unsigned m = j->gb[v];
+    const double c = j->gamdot[v][i];
+    gr[0] = gb_diff(c, j->gamdot[(xp * n1 + y) * n2 + z][i], j->gamdot[(xm * n1 + y) * n2 + z][i],
+                    m & 1, (m >> 1) & 1);
+    gr[1] = gb_diff(c, j->gamdot[(x * n1 + yp) * n2 + z][i], j->gamdot[(x * n1 + ym) * n2 + z][i],
+                    (m >> 2) & 1, (m >> 3) & 1);
+    gr[2] = gb_diff(c, j->gamdot[(x * n1 + y) * n2 + zp][i], j->gamdot[(x * n1 + y) * n2 + zm][i],
+                    (m >> 4) & 1, (m >> 5) & 1);
+}
+
 /* DislocationEvolution, constitutive.c:1353-1529 (istep <= 2000000 branch;
- * DD_GND off). Uses rho_F, rho_m and gamdot of the last flow-rule call. */
-static void dislocation_voxel(evo_job *j, int v)
+ * GND part first order, constitutive.c:1428-1522). Uses rho_F, rho_m and
+ * gamdot of the last flow-rule call. `grad`: the slip-rate gradients were
+ * formed this increment (Hard_Flag == 1 && istep > 1, evolution.c:1348-1357);
+ * otherwise gadot_grad still holds its initial zeros. */
+static void dislocation_voxel(evo_job *j, int v, int grad)
 {
     const int jph = j->phase_f[v], p = jph - 1;
     const double kT = kT_of(j), dt = j->nl.TimeStep, T__K = j->nl.T__K;
@@ -1341,6 +1453,17 @@ static void dislocation_voxel(evo_job *j, int v)
         j->rho_s[v][i] += dot * dt;
         j->rho_dot_s[v][i] = dot;
         j->gam_acum[v][i] = j->trial_gam_acum[v][i];
+        if (j->gnd) {
+            double gr[3] = {0.0, 0.0, 0.0}, gnd1, dot_g;
+            const double *bp = j->bp[p][i], *bb = j->bb[p][i];
+            if (grad) shear_rate_gradient(j, v, i, gr);
+            gnd1 = gr[0] * bp[0] + gr[1] * bp[1] + gr[2] * bp[2];
+            dot_g = gnd1 / b / j->nl.L0;
+            j->rho_g1[v][i] += dot_g * dt;
+            gnd1 = gr[0] * bb[0] + gr[1] * bb[1] + gr[2] * bb[2];
+            dot_g = -1.0 * gnd1 / b / j->nl.L0;
+            j->rho_g2[v][i] += dot_g * dt;
+        }
     }
 }
 
@@ -1355,7 +1478,10 @@ static void avg_dislocation(evo_job *j)
         for (v = 0; v < j->N; v++) {
             const int p = j->phase_f[v] - 1;
             if (j->nl.Type_phases[p]) continue;
-            for (i = 0; i < j->nSYS[p]; i++) s += arr[q] ? arr[q][v][i] : sqrt(0.0 + 0.0 + 0.0);
+            for (i = 0; i < j->nSYS[p]; i++)
+                s += arr[q] ? arr[q][v][i]
+                            : sqrt(j->rho_g1[v][i] * j->rho_g1[v][i] + j->rho_g2[v][i] * j->rho_g2[v][i] +
+                                   0.0 * 0.0);
         }
         j->rho_avg[q] = s;
         j->rho_avg[q] *= 1.0 / j->N;
@@ -1410,7 +1536,8 @@ int evo_increment(evo_job *j, int istep, int *iters)
         int i;
         j->rho_tot[v] = 0.0;
         for (i = 0; i < j->nSYS[p]; i++)
-            j->rho_tot[v] += j->rho_s[v][i] + j->rho_m[v][i] + sqrt(pow(0.0, 2.0) + pow(0.0, 2.0) + pow(0.0, 2.0));
+            j->rho_tot[v] += j->rho_s[v][i] + j->rho_m[v][i] +
+                             sqrt(pow(j->rho_g1[v][i], 2.0) + pow(j->rho_g2[v][i], 2.0) + pow(0.0, 2.0));
     }
     /* evolution.c:1115-1128 */
     for (v = 0; v < N; v++)
@@ -1488,8 +1615,11 @@ int evo_increment(evo_job *j, int istep, int *iters)
 #pragma omp parallel for num_threads(g_threads) schedule(static)
         for (v = 0; v < N; v++) reorient_voxel(j, v);
     }
+    {
+        const int grad = (j->nl.Hard_Flag == 1) && (istep > 1);
 #pragma omp parallel for num_threads(g_threads) schedule(static)
-    for (v = 0; v < N; v++) dislocation_voxel(j, v);
+        for (v = 0; v < N; v++) dislocation_voxel(j, v, grad);
+    }
     avg_dislocation(j);
     /* evolution.c:1401-1425: displacement_fluct[mi] = -Re(IFFT(FFT(fluct[mi][2])))/N */
     for (a = 0; a < 3; a++) {
@@ -1648,7 +1778,7 @@ int evo_run(evo_job *j, const char *outdir, int nsteps, int write_iout_flag)
 int main(int argc, char **argv)
 {
     const char *input = 0, *outdir = ".", *rho0 = 0;
-    int steps = -1, threads = 1, iout = 0, a, st, nrmode = 0;
+    int steps = -1, threads = 1, iout = 0, a, st, nrmode = 0, gnd = 0;
     char err[512];
     evo_job *j;
     for (a = 1; a < argc; a++) {
@@ -1658,16 +1788,18 @@ int main(int argc, char **argv)
         else if (!strcmp(argv[a], "--rho0") && a + 1 < argc) rho0 = argv[++a];
         else if (!strcmp(argv[a], "--iout")) iout = 1;
         else if (!strcmp(argv[a], "--line-search")) nrmode = 1;
+        else if (!strcmp(argv[a], "--gnd")) gnd = 1;
         else input = argv[a];
     }
     if (!input) {
-        fprintf(stderr, "usage: evp_oracle <input> [--outdir D] [--steps K] [--threads T] [--rho0 F] [--iout] [--line-search]\n");
+        fprintf(stderr, "usage: evp_oracle <input> [--outdir D] [--steps K] [--threads T] [--rho0 F] [--iout] [--line-search] [--gnd]\n");
         return 2;
     }
     evo_set_threads(threads);
     j = evo_open(input, rho0, err, sizeof err);
     if (!j) { fprintf(stderr, "evp_oracle: %s\n", err); return 1; }
     evo_set_nr_mode(j, nrmode);
+    evo_set_gnd(j, gnd);
     st = evo_run(j, outdir, steps, iout);
     evo_close(j);
     return st;

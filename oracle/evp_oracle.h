@@ -38,6 +38,14 @@ int evo_nvox(const evo_job *j);
 void evo_set_nr_mode(evo_job *j, int mode);
 int evo_nsteps(const evo_job *j);
 
+/* First-order GND densities (the reference built with DD_GND, which implies
+ * DD_GND_FIRST_ORDER, evpFlags.h:29-32): slip-rate gradients with grain-
+ * boundary stencils (constitutive.c:731-1112), GND rates in the dislocation
+ * update (constitutive.c:1428-1522), their projections in the flow rule
+ * (constitutive.c:558-577) and rho_tot (evolution.c:1041-1045). Set before
+ * the first increment; off by default (the shipped configuration). */
+void evo_set_gnd(evo_job *j, int on);
+
 /* One increment of Evolution() (evolution.c:726-1520) without file output.
  * Returns 0, or a nonzero status: 1 NaN in the flow rule, 2 singular LU. */
 int evo_increment(evo_job *j, int istep, int *iters);
@@ -52,7 +60,7 @@ int evo_run(evo_job *j, const char *outdir, int nsteps, int write_iout);
 /* Raw pointers into the AoS state (reference layout, evp.h:429-456):
  * "Sig","DisGrad","Eps","Edot","VelGrad","TranMat" ([N][3][3]);
  * "rho_s","rho_m","rho_F","rho_P","gamdot","gam_acum","trial_gam_acum",
- * "rho_dipole","rho_forest","rho_inplane" ([N][12]); "rho_tot" ([N]);
+ * "rho_dipole","rho_forest","rho_inplane","rho_g1","rho_g2" ([N][12]); "rho_tot" ([N]);
  * "Schm_gr" ([N][12][5]); set-up arrays "C066","S066" (6x6), "S0" (3^4),
  * "Chi","Chi_1" ([2][12][12]), "Shear_G" ([2]), "bb_B" ([2][12]),
  * "Schm_xt" ([2][12][5]); "scalars" (see evp_oracle.c). */

@@ -48,6 +48,7 @@ class Oracle:
         L.evo_update_schmid.argtypes = [C.c_void_p]
         L.evo_update_stress.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.evo_set_threads.argtypes = [C.c_int]
+        L.evo_set_gnd.argtypes = [C.c_void_p, C.c_int]
         self.L = L
 
     def open(self, input_path, rho0=None, nr_mode=0, threads=None):

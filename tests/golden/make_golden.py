@@ -1,8 +1,8 @@
 """Generate the golden fixtures under tests/golden/ from the reference itself.
 
 Runs the reference's own sources compiled with single-rank shims
-(oracle/_ref/srx_ref and srx_ref_nrmod, built by ``make -C oracle ref`` from
-the reference tree) on small cases and stores what it writes:
+(oracle/_ref/srx_ref, srx_ref_nrmod and srx_ref_gnd, built by ``make -C oracle
+ref`` from the reference tree) on small cases and stores what it writes:
 
 * ``bicrystal8``   the reference's 8^3 regression case (restated by
                    ``srx_gb300.rve.bicrystal8_case``), plain NR, 10 increments:
@@ -13,6 +13,11 @@ the reference tree) on small cases and stores what it writes:
                    NR_MODIFIED line search, 2 increments, full final fields;
 * ``cfg0_32_ls``   the 32^3 / 27-grain configuration, line search, first
                    increment, fields on every 7th voxel;
+* ``gnd12_ls``     12^3, 6 Voronoi grains, line search with first-order GND
+                   densities (srx_ref_gnd: DD_GND), 5 increments -- the slip-rate
+                   gradients start in the third increment (istep > 1) and reach
+                   the flow rule in the fourth; full final fields including
+                   the GND densities;
 * ``setup16``      the set-up state of ``voronoi16_ls`` (C066, S066, Schmid
                    tensors, interaction matrices, shear modulus, Burgers length);
 * ``nrprobe8``     one UpdateStress sweep of the reference on the bicrystal
@@ -38,6 +43,7 @@ from srx_gb300 import rve  # noqa: E402
 
 REF = os.path.join(ROOT, "oracle", "_ref", "srx_ref")
 REF_LS = os.path.join(ROOT, "oracle", "_ref", "srx_ref_nrmod")
+REF_GND = os.path.join(ROOT, "oracle", "_ref", "srx_ref_gnd")
 
 # .iout component order 11,22,33,23,13,12 (io.c:409-421)
 
@@ -50,6 +56,11 @@ def voronoi16_spec():
 def cfg0_32_spec():
     return dict(kind="voronoi", n=[32, 32, 32], grains=27, seed=1027, steps=1, nr="ls",
                 rho0=None)
+
+
+def gnd12_spec():
+    return dict(kind="voronoi", n=[12, 12, 12], grains=6, seed=1212, steps=5, nr="ls",
+                rho0=None, gnd=True)
 
 
 def make_input(spec: dict, d: str, print_every: int = 1) -> dict:
@@ -119,7 +130,8 @@ def gen_bicrystal8(out: str) -> None:
 def gen_voronoi(spec: dict, out: str, stride: int = 1) -> None:
     with tempfile.TemporaryDirectory() as t:
         case = make_input(spec, t)
-        iters = run_ref(REF_LS if spec["nr"] == "ls" else REF, case, ["--final", "final.bin"])
+        binary = REF_GND if spec.get("gnd") else (REF_LS if spec["nr"] == "ls" else REF)
+        iters = run_ref(binary, case, ["--final", "final.bin"])
         N = int(np.prod(spec["n"]))
         last = spec["steps"] - 1
         f = read_fields(t, last, N)
@@ -129,7 +141,10 @@ def gen_voronoi(spec: dict, out: str, stride: int = 1) -> None:
         for k, v in f.items():
             data[k] = v[idx]
         fin = final_state(os.path.join(t, "final.bin"))
-        for k in ("rho_m", "gamdot", "TranMat", "DisGrad", "Edot"):
+        keys = ["rho_m", "gamdot", "TranMat", "DisGrad", "Edot"]
+        if spec.get("gnd"):
+            keys += ["Sig", "rho_s", "rho_g1", "rho_g2"]
+        for k in keys:
             data["final_" + k] = fin[k][idx]
     np.savez_compressed(out, spec=json.dumps(spec), **data)
 
@@ -153,6 +168,11 @@ def final_state(p: str) -> dict:
         take(k, 12 * N)
         out[k] = out[k].reshape(N, 12)
     take("rho_tot", N)
+    off += 8 * (4 * 9 + 13)  # SigAvg, SigAvg1, dDisGradAvg_acum, DisGradAvg, scalars
+    if len(b) >= off + 3 * 8 * 12 * N:  # GND densities (harness builds that dump them)
+        for k in ("rho_g1", "rho_g2", "rho_g3"):
+            take(k, 12 * N)
+            out[k] = out[k].reshape(N, 12)
     return out
 
 
@@ -224,13 +244,14 @@ GENS = {
     "bicrystal8": lambda o: gen_bicrystal8(o),
     "voronoi16_ls": lambda o: gen_voronoi(voronoi16_spec(), o),
     "cfg0_32_ls": lambda o: gen_voronoi(cfg0_32_spec(), o, stride=7),
+    "gnd12_ls": lambda o: gen_voronoi(gnd12_spec(), o),
     "setup16": lambda o: gen_setup16(o),
     "nrprobe8": lambda o: gen_nrprobe8(o),
 }
 
 
 def main(argv):
-    if not (os.path.exists(REF) and os.path.exists(REF_LS)):
+    if not all(os.path.exists(p) for p in (REF, REF_LS, REF_GND)):
         raise SystemExit("build the reference oracle first: make -C oracle ref")
     names = argv or list(GENS)
     for n in names:

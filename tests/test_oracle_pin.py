@@ -20,13 +20,15 @@ def _close(a, b):
     return rel_err(a, b) <= TOL
 
 
-def _run(case, out, steps, line_search=False, threads=8):
+def _run(case, out, steps, line_search=False, threads=8, gnd=False):
     build_oracle()
     os.makedirs(out, exist_ok=True)
     cmd = [ORACLE_BIN, case["input"], "--outdir", str(out), "--iout", "--steps", str(steps),
            "--threads", str(threads)]
     if line_search:
         cmd.append("--line-search")
+    if gnd:
+        cmd.append("--gnd")
     if case.get("rho0"):
         cmd += ["--rho0", case["rho0"]]
     subprocess.run(cmd, check=True, capture_output=True)
@@ -45,11 +47,11 @@ def test_bicrystal8_matches_reference(tmp_path):
             assert _close(f[k], z["%s_%d" % (k, s)]), (k, s)
 
 
-@pytest.mark.parametrize("name", ["voronoi16_ls", "cfg0_32_ls"])
+@pytest.mark.parametrize("name", ["voronoi16_ls", "cfg0_32_ls", "gnd12_ls"])
 def test_line_search_cases_match_reference(tmp_path, name):
     z, spec = golden(name)
     case = write_spec_case(spec, tmp_path / "case")
-    _run(case, tmp_path / "out", spec["steps"], line_search=True)
+    _run(case, tmp_path / "out", spec["steps"], line_search=True, gnd=spec.get("gnd", False))
     assert read_iters(tmp_path / "out") == list(z["iters"])
     assert _close(read_table(tmp_path / "out" / "vm.out"), z["vm"])
     N = int(np.prod(spec["n"]))
@@ -101,3 +103,32 @@ def test_update_stress_sweep_matches_reference(oracle, tmp_path):
         assert _close([ee.value, es.value], z["err"])
     finally:
         oracle.L.evo_close(h)
+
+
+def test_gnd_densities_match_reference(oracle):
+    """First-order GND densities (the reference built with DD_GND): after five
+    increments the screw and edge densities, SSD and mobile densities, slip
+    rates and stress of every voxel equal the reference's final state."""
+    import tempfile
+    z, spec = golden("gnd12_ls")
+    N = int(np.prod(spec["n"]))
+    with tempfile.TemporaryDirectory() as d:
+        case = write_spec_case(spec, d)
+        h = oracle.open(case["input"], nr_mode=1)
+        try:
+            oracle.L.evo_set_gnd(h, 1)
+            import ctypes as C
+            its = []
+            for k in range(spec["steps"]):
+                it = C.c_int(0)
+                assert oracle.L.evo_increment(h, k, C.byref(it)) == 0
+                its.append(it.value)
+            assert its == list(z["iters"])
+            for name, key, w in (("rho_g1", "final_rho_g1", 12), ("rho_g2", "final_rho_g2", 12),
+                                 ("rho_s", "final_rho_s", 12), ("rho_m", "final_rho_m", 12),
+                                 ("gamdot", "final_gamdot", 12), ("Sig", "final_Sig", 9)):
+                got = oracle.field(h, name, N * w).reshape(N, w)
+                assert _close(got, z[key]), name
+            assert np.abs(z["final_rho_g1"]).max() > 0.1  # the densities did grow
+        finally:
+            oracle.L.evo_close(h)
