@@ -17,7 +17,8 @@
  *                                        -> evpg_equilibrium_iteration
  *   the whole while loop                 -> evpg_equilibrium_solve
  *   increment tail (evolution.c:1266-1362: VelGrad, Eps, averages,
- *   update_orient constitutive.c:196-273, DislocationEvolution
+ *   update_orient constitutive.c:196-273, the DD_GND slip-rate gradients
+ *   Gradient_ShearRate constitutive.c:881-1112, DislocationEvolution
  *   constitutive.c:1353-1529, AvgDislocation constitutive.c:1681-1808)
  *                                        -> evpg_increment_end
  *   Evolution() itself                   -> evpg_job_run
@@ -113,6 +114,16 @@ typedef struct evpg_rve_desc {
     int32_t iter_max;             /* IterMax */
     int32_t precision;            /* evpg_precision */
     int32_t nr_mode;              /* evpg_nr_mode */
+    /* First-order GND densities: the reference built with DD_GND (which
+     * implies DD_GND_FIRST_ORDER, evpFlags.h:29-32). Screw and edge densities
+     * per slip system grow from the slip-rate gradients across each grain
+     * (Gradient_ShearRate, constitutive.c:881-1112; DislocationEvolution,
+     * constitutive.c:1428-1522) and enter the forest and parallel densities
+     * of the flow rule (constitutive.c:558-577) and rho_tot
+     * (evolution.c:1041-1045). 0 leaves them out (the shipped build). */
+    int32_t gnd;                  /* 1: on */
+    double l0;                    /* L0 of the namelist (> 0 when gnd = 1) */
+    const int32_t *voxel_grain;   /* [N] grain ids (grain_f); read when gnd = 1 */
 } evpg_rve_desc;
 
 /* Macro quantities after an equilibrium iteration (all FP64). */
@@ -148,8 +159,19 @@ typedef enum evpg_field {
     EVPG_F_GAMDOT = 7,     /* [N][12] gamdot */
     EVPG_F_GAM_ACUM = 8,   /* [N][12] gam_acum */
     EVPG_F_VELGRAD = 9,    /* [N][3][3] VelGrad (valid after evpg_increment_end) */
-    EVPG_F_SIG6 = 10       /* [N][6] Sig in .iout order 11,22,33,23,13,12 */
+    EVPG_F_SIG6 = 10,      /* [N][6] Sig in .iout order 11,22,33,23,13,12 */
+    EVPG_F_RHO_G1 = 11,    /* [N][12] rho_g1, screw GND density (contexts with gnd = 1) */
+    EVPG_F_RHO_G2 = 12     /* [N][12] rho_g2, edge GND density (contexts with gnd = 1) */
 } evpg_field;
+
+/* Flags of the increment tail (evpg_increment_end, evpg_increment,
+ * evpg_batch_stage). */
+typedef enum evpg_tail_flag {
+    EVPG_TAIL_REORIENT = 1,    /* update_orient (Update_Flag == 1 && istep > 1) */
+    EVPG_TAIL_GND_GRADIENT = 2 /* slip-rate gradients for the GND densities this increment
+                                  (Hard_Flag == 1 && istep > 1, evolution.c:1348-1357);
+                                  otherwise the gradients stay at their initial zeros */
+} evpg_tail_flag;
 
 const char *evpg_version(void);
 const char *evpg_status_string(int status);
@@ -178,9 +200,10 @@ int evpg_equilibrium_iteration(void *ctx, double e_vm, evpg_iter_out *out);
  * (out->converged tells), as the reference does. */
 int evpg_equilibrium_solve(void *ctx, double e_vm, evpg_iter_out *out);
 
-/* Increment tail. update_orient runs when reorient != 0 (the reference:
- * Update_Flag == 1 && istep > 1). out may be NULL. */
-int evpg_increment_end(void *ctx, int32_t reorient, evpg_incr_out *out);
+/* Increment tail. tail: evpg_tail_flag bits (update_orient with
+ * EVPG_TAIL_REORIENT, the reference's Update_Flag == 1 && istep > 1). out
+ * may be NULL. */
+int evpg_increment_end(void *ctx, int32_t tail, evpg_incr_out *out);
 
 /* The whole increment -- head, equilibrium loop, tail -- as one CUDA graph
  * launch on the context's stream (captured on the first call, replayed
@@ -188,12 +211,12 @@ int evpg_increment_end(void *ctx, int32_t reorient, evpg_incr_out *out);
  * sets after every iteration, so no host round trip happens inside the
  * increment. Same results as evpg_increment_begin + evpg_equilibrium_solve +
  * evpg_increment_end (with the increment tail skipped when the loop stops on
- * an error). e_vm: strain-error normaliser; reorient as in
+ * an error). e_vm: strain-error normaliser; tail as in
  * evpg_increment_end. it/inc may be NULL. No counterpart in the reference,
  * whose loop is host-driven (evolution.c:1150). */
 int evpg_increment(void *ctx, const double udot_dt[3][3], int32_t creep,
                    const double disgrad_avg_actual[3][3], double time_tot, double e_vm,
-                   int32_t reorient, evpg_iter_out *it, evpg_incr_out *inc);
+                   int32_t tail, evpg_iter_out *it, evpg_incr_out *inc);
 
 /* Change the loading between increments (a mid-run BC switch, e.g.
  * tension then shear; the reference reads one BC set per run, init.c:865-901):
@@ -226,7 +249,8 @@ int evpg_set_nr_tolerance(void *ctx, double tol, int32_t itmax);
  * evpg_get_schedule then reports 0 pencils for the z and y passes. */
 int evpg_set_fused(void *ctx, int32_t mode);
 /* Device bytes evpg_create allocates for an n[0] x n[1] x n[2] RVE with
- * n_orient distinct orientations (for admission by HBM footprint). */
+ * n_orient distinct orientations (for admission by HBM footprint); GND
+ * densities add 193 bytes per voxel. */
 int evpg_estimate_bytes(const int32_t n[3], int32_t precision, int32_t n_orient, int64_t *bytes);
 
 int evpg_download(void *ctx, int32_t field, double *host, size_t count);
@@ -288,7 +312,7 @@ int evpg_batch_set(void *batch, void *const *ctxs, int32_t n);
 /* Controls of slot's next increment (as evpg_increment). */
 int evpg_batch_stage(void *batch, int32_t slot, const double udot_dt[3][3], int32_t creep,
                      const double disgrad_avg_actual[3][3], double time_tot, double e_vm,
-                     int32_t reorient);
+                     int32_t tail);
 int evpg_batch_round(void *batch, int32_t max_ticks, int32_t *ticks);
 /* After a round: phase (0 idle, 1 staged, 2 running, 3 ended), sticky
  * status (evpg_status of the slot's last error) and the macro outputs of
@@ -306,6 +330,11 @@ const char *evpg_batch_last_error(void);
  * to every slip system. precision: evpg_precision; nr_mode: evpg_nr_mode. */
 int evpg_job_open(const char *input_path, const char *rho0_path, int32_t precision,
                   int32_t nr_mode, void **job_out);
+/* evpg_job_open with options: EVPG_JOB_GND selects the first-order GND
+ * densities (the reference built with DD_GND; L0 from the namelist). */
+#define EVPG_JOB_GND 1
+int evpg_job_open_opts(const char *input_path, const char *rho0_path, int32_t precision,
+                       int32_t nr_mode, int32_t options, void **job_out);
 int evpg_job_close(void *job);
 void *evpg_job_ctx(void *job);
 int evpg_job_nvox(void *job, int32_t n[3]);

@@ -219,7 +219,7 @@ static void free_ctx(Ctx* c) {
                     c->gamdot64, c->gam_acum, c->tranmat, c->schm64, c->fc64, c->sgr64, c->orient,
                     c->phase, c->sig32, c->ddg32, c->b6_32, c->schm32, c->fc32, c->sgr32, c->spec,
                     c->part_nr, c->part_nr2, c->ticket, c->part_end, c->macro, c->tw64[0], c->tw64[1], c->tw64[2],
-                    c->tw32[0], c->tw32[1], c->tw32[2]};
+                    c->tw32[0], c->tw32[1], c->tw32[2], c->rho_g, c->gproj, c->gbm};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (c->macro_host) cudaFreeHost(c->macro_host);
@@ -276,6 +276,51 @@ const char* evpg_status_string(int st) {
     }
 }
 
+// Host-side GND constants: per phase the projection tables and sense vectors
+// of the GP_* row (init.c:198-203, 1119-1140), and per voxel the same-grain
+// bits of Gradient_ExchangeGrainID (constitutive.c:731-879) on one rank with
+// periodic neighbours: bit 0/1 x+/x-, 2/3 y+/y-, 4 z+, 5 the reference's
+// "z-" check, which compares with the y- neighbour (GB_checkZ[pIDX][1]).
+static void gnd_tables(const evpg_rve_desc* d, std::vector<double>& gp, std::vector<uint8_t>& m) {
+    gp.assign(2 * (size_t)GP_STRIDE, 0.0);
+    for (int p = 0; p < 2; p++) {
+        const evpg_phase_desc& P = d->phase[p];
+        double* row = gp.data() + (size_t)p * GP_STRIDE;
+        for (int i = 0; i < P.n_sys; i++) {
+            const double *ni = P.bn[i], *bi = P.bb[i];
+            row[GP_BP + 3 * i + 0] = bi[1] * ni[2] - bi[2] * ni[1];
+            row[GP_BP + 3 * i + 1] = bi[2] * ni[0] - bi[0] * ni[2];
+            row[GP_BP + 3 * i + 2] = bi[0] * ni[1] - bi[1] * ni[0];
+            for (int j = 0; j < P.n_sys; j++) {
+                const double *nj = P.bn[j], *bj = P.bb[j];
+                const double sv[3] = {nj[1] * bj[2] - nj[2] * bj[1], nj[2] * bj[0] - nj[0] * bj[2],
+                                      nj[0] * bj[1] - nj[1] * bj[0]};
+                const double cs = fabs(ni[0] * sv[0] + ni[1] * sv[1] + ni[2] * sv[2]);
+                const double c1 = fabs(ni[0] * bj[0] + ni[1] * bj[1] + ni[2] * bj[2]);
+                row[GP_COS1 + i * NS + j] = c1;
+                row[GP_SIN1 + i * NS + j] = fabs(sqrt(fabs(1.0 - c1 * c1)));
+                row[GP_COS2 + i * NS + j] = cs;
+                row[GP_SIN2 + i * NS + j] = fabs(sqrt(fabs(1.0 - cs * cs)));
+            }
+        }
+    }
+    const int n0 = d->n[0], n1 = d->n[1], n2 = d->n[2];
+    const int32_t* g = d->voxel_grain;
+    m.assign((size_t)n0 * n1 * n2, 0);
+    for (int x = 0; x < n0; x++)
+        for (int y = 0; y < n1; y++)
+            for (int z = 0; z < n2; z++) {
+                const int xp = (x + 1) % n0, xm = (x + n0 - 1) % n0, yp = (y + 1) % n1,
+                          ym = (y + n1 - 1) % n1, zp = (z + 1) % n2;
+                const size_t v = ((size_t)x * n1 + y) * n2 + z;
+                const int gv = g[v];
+                auto at = [&](int a, int b, int c) { return g[((size_t)a * n1 + b) * n2 + c]; };
+                m[v] = (uint8_t)((gv == at(xp, y, z)) | (gv == at(xm, y, z)) << 1 | (gv == at(x, yp, z)) << 2 |
+                                 (gv == at(x, ym, z)) << 3 | (gv == at(x, y, zp)) << 4 |
+                                 (gv == at(x, ym, z)) << 5);
+            }
+}
+
 int evpg_create(const evpg_rve_desc* d, void** out) {
     if (!d || !out) return fail(EVPG_ERR_ARG, "null argument");
     *out = nullptr;
@@ -293,6 +338,8 @@ int evpg_create(const evpg_rve_desc* d, void** out) {
     for (int p = 0; p < 2; p++)
         if (d->phase[p].n_sys < 0 || d->phase[p].n_sys > EVPG_NSYS)
             return fail(EVPG_ERR_ARG, "n_sys %d", d->phase[p].n_sys);
+    if (d->gnd && (!d->voxel_grain || !(d->l0 > 0.0)))
+        return fail(EVPG_ERR_ARG, "GND densities need voxel_grain and L0 > 0");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
         return fail(EVPG_ERR_NO_DEVICE, "no CUDA device");
@@ -361,6 +408,10 @@ int evpg_create(const evpg_rve_desc* d, void** out) {
         AL(sp, 9 * (size_t)c->g.Nh);
         c->spec = sp;
     }
+    if (d->gnd) {
+        AL(c->rho_g, 24 * n); AL(c->gproj, 2 * (size_t)GP_STRIDE); AL(c->gbm, n);
+        c->l0 = d->l0;
+    }
     AL(c->part_nr, (size_t)c->nb_nr * (NR_BLOCK / 32) * NPART_NR);
     AL(c->part_nr2, (size_t)MACRO_BLOCKS * NPART_NR);
     AL(c->ticket, 1);
@@ -427,6 +478,13 @@ int evpg_create(const evpg_rve_desc* d, void** out) {
             for (size_t i = 0; i < hf.size(); i++) hf[i] = (float)t[i];
             e = put(c->sgr32, hf.data(), hf.size() * sizeof(float));
         }
+    }
+    if (e == cudaSuccess && d->gnd) {
+        std::vector<double> gp;
+        std::vector<uint8_t> m;
+        gnd_tables(d, gp, m);
+        e = put(c->gproj, gp.data(), gp.size() * sizeof(double));
+        if (e == cudaSuccess) e = put(c->gbm, m.data(), m.size());
     }
     for (int a = 0; a < 3 && e == cudaSuccess; a++) {
         const int na = d->n[a];
@@ -554,7 +612,7 @@ __global__ void k_set_evm(Macro* m, double e_vm) {
     m->ctl.e_vm = e_vm;
 }
 
-__global__ void k_set_reorient(Macro* m, int r) { m->ctl.reorient = r; }
+__global__ void k_set_tail(Macro* m, int t) { m->ctl.tail = t; }
 
 // Field packing for downloads: SoA planes (B basis) -> voxel-major records
 // in the host layout of evpg_download, for voxels [v0, v0 + nv).
@@ -623,7 +681,7 @@ static int launch_iteration(Ctx* c) {
 
 // Controls of one increment into the context's pinned staging area.
 static void stage_ctl(Ctx* c, const double udot_dt[3][3], int creep, const double dgavg[3][3],
-                      double time_tot, double e_vm, int reorient) {
+                      double time_tot, double e_vm, int tail) {
     IncrCtl& k = *c->ctl_host;
     double u9[9], g9[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     tensor_to_9(udot_dt, u9);
@@ -637,7 +695,7 @@ static void stage_ctl(Ctx* c, const double udot_dt[3][3], int creep, const doubl
     k.e_vm = e_vm;
     k.err0 = 2. * c->cfg.err_tol;
     k.creep = creep ? 1 : 0;
-    k.reorient = reorient ? 1 : 0;
+    k.tail = tail & (EVPG_TAIL_REORIENT | EVPG_TAIL_GND_GRADIENT);
     k.phase = PH_BEGIN;
     k.pad = 0;
 }
@@ -698,10 +756,10 @@ int evpg_equilibrium_solve(void* ctx, double e_vm, evpg_iter_out* out) {
     return EVPG_OK;
 }
 
-int evpg_increment_end(void* ctx, int32_t reorient, evpg_incr_out* out) {
+int evpg_increment_end(void* ctx, int32_t tail, evpg_incr_out* out) {
     Ctx* c = (Ctx*)ctx;
     if (!c) return fail(EVPG_ERR_ARG, "null context");
-    k_set_reorient<<<1, 1, 0, c->stream>>>(c->macro, reorient ? 1 : 0);
+    k_set_tail<<<1, 1, 0, c->stream>>>(c->macro, tail & (EVPG_TAIL_REORIENT | EVPG_TAIL_GND_GRADIENT));
     c->launches++;
     if (c->precision == EVPG_FP32_BULK) {
         CK(launch_fold(*c, GATE_ALWAYS));
@@ -828,8 +886,11 @@ int evpg_download(void* ctx, int32_t field, double* host, size_t count) {
         case EVPG_F_GAMDOT: src = c->gamdot64; planes = 12; break;
         case EVPG_F_GAM_ACUM: src = c->gam_acum; planes = 12; break;
         case EVPG_F_VELGRAD: src = c->dg_old; planes = 9; kind = PK_TENSOR9; outw = 9; break;
+        case EVPG_F_RHO_G1: src = c->rho_g; planes = 12; break;
+        case EVPG_F_RHO_G2: src = c->rho_g ? c->rho_g + 12 * n : nullptr; planes = 12; break;
         default: return fail(EVPG_ERR_ARG, "unknown field %d", field);
     }
+    if (!src) return fail(EVPG_ERR_ARG, "field %d: GND densities are off for this context", field);
     if (count < (size_t)outw * n) return fail(EVPG_ERR_ARG, "buffer too small");
     // packed on the device in chunks, copied through a pinned staging buffer
     // (or straight into the caller's buffer when it is pinned)

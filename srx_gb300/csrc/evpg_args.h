@@ -8,8 +8,13 @@
 namespace evpg {
 
 constexpr int NPART_NR = 15;   // err_e, err_s, sig6 sum, sig6 phase-1 sum, NR iterations
-constexpr int NPART_END = 18;  // rho_F, rho_P, rho_s, rho_m, d_dipole, d_forest, d_inplane,
-                               // Eps (6), Edot (5)
+constexpr int NPART_END = 19;  // rho_F, rho_P, rho_s, rho_m, d_dipole, d_forest, d_inplane,
+                               // Eps (6), Edot (5), rho_g
+// Per-phase GND constants in one device row (first-order GND densities):
+// |n_i . b_j| and its sine, |n_i . (n_j x b_j)| and its sine (init.c:1119-1140)
+// as [NS][NS] tables, then the sense vectors b x n (init.c:198-203).
+constexpr int GP_COS1 = 0, GP_SIN1 = 144, GP_COS2 = 288, GP_SIN2 = 432, GP_BP = 576,
+              GP_STRIDE = 612;
 constexpr int NR_BLOCK = 128;
 constexpr int MACRO_BLOCKS = 64;
 constexpr int END_BLOCK = 128;
@@ -127,6 +132,9 @@ struct BeginArgs {
     float* b6_32;
     float* ddg32;
     const double* epsp;
+    // first-order GND densities (nullptr when off): [24][N] rho_g1, rho_g2
+    const double* rho_g;
+    const double* gproj;  // [2][GP_STRIDE]
 };
 
 struct FoldArgs {
@@ -142,7 +150,7 @@ struct FoldArgs {
 struct EndArgs {
     Material<double> mat;
     Grid g;
-    const Macro* macro;   // reorient flag in macro->ctl
+    const Macro* macro;   // tail flags in macro->ctl
     int gate;
     double udot_a[3][3];
     double* dg_old;       // in: DisGrad at increment start; out: VelGrad
@@ -159,6 +167,11 @@ struct EndArgs {
     const int32_t* phase;
     float* sig32;         // FP32 bulk: next increment starts from the refined stress
     double* part;
+    // first-order GND densities (nullptr when off)
+    double* rho_g;        // [24][N] rho_g1, rho_g2
+    const double* gproj;  // [2][GP_STRIDE]
+    const uint8_t* gbm;   // [N] same-grain neighbour bits (x+, x-, y+, y-, z+, "z-")
+    double l0;            // L0
 };
 
 struct EndReduceArgs {

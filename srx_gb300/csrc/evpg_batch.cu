@@ -386,7 +386,7 @@ static int set_slots(Batch& b, Ctx* const* ctxs, int n) {
 
 // Stage slot i's next increment (copied to the device when the round starts).
 static void stage(Batch& b, int i, const double udot_dt[3][3], int creep, const double dgavg[3][3],
-                  double time_tot, double e_vm, int reorient) {
+                  double time_tot, double e_vm, int tail) {
     Ctx* c = b.slots[i];
     IncrCtl& k = b.hctl[i];
     double g9[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
@@ -408,7 +408,7 @@ static void stage(Batch& b, int i, const double udot_dt[3][3], int creep, const 
     k.e_vm = e_vm;
     k.err0 = 2. * c->cfg.err_tol;
     k.creep = creep ? 1 : 0;
-    k.reorient = reorient ? 1 : 0;
+    k.tail = tail & (EVPG_TAIL_REORIENT | EVPG_TAIL_GND_GRADIENT);
     k.phase = PH_BEGIN;
     k.pad = 0;
     b.staged[i] = 1;
@@ -543,11 +543,11 @@ int evpg_batch_set(void* batch, void* const* ctxs, int32_t n) {
 }
 
 int evpg_batch_stage(void* batch, int32_t slot, const double udot_dt[3][3], int32_t creep,
-                     const double disgrad_avg_actual[3][3], double time_tot, double e_vm, int32_t reorient) {
+                     const double disgrad_avg_actual[3][3], double time_tot, double e_vm, int32_t tail) {
     Batch* b = (Batch*)batch;
     if (!b || !udot_dt || slot < 0 || slot >= (int)b->slots.size()) return bfail(EVPG_ERR_ARG, "bad argument");
     if (creep && !disgrad_avg_actual) return bfail(EVPG_ERR_ARG, "creep needs disgrad_avg_actual");
-    stage(*b, slot, udot_dt, creep, disgrad_avg_actual, time_tot, e_vm, reorient);
+    stage(*b, slot, udot_dt, creep, disgrad_avg_actual, time_tot, e_vm, tail);
     return EVPG_OK;
 }
 
@@ -577,7 +577,7 @@ int evpg_batch_launch_count(void* batch, int64_t* n) {
 }
 
 int evpg_increment(void* ctx, const double udot_dt[3][3], int32_t creep, const double disgrad_avg_actual[3][3],
-                   double time_tot, double e_vm, int32_t reorient, evpg_iter_out* it, evpg_incr_out* inc) {
+                   double time_tot, double e_vm, int32_t tail, evpg_iter_out* it, evpg_incr_out* inc) {
     Ctx* c = (Ctx*)ctx;
     if (!c || !udot_dt) return bfail(EVPG_ERR_ARG, "null argument");
     if (creep && !disgrad_avg_actual) return bfail(EVPG_ERR_ARG, "creep needs disgrad_avg_actual");
@@ -585,7 +585,7 @@ int evpg_increment(void* ctx, const double udot_dt[3][3], int32_t creep, const d
         // per-kernel timing needs the launch-by-launch path
         int st = evpg_increment_begin(ctx, udot_dt, creep, disgrad_avg_actual, time_tot);
         if (!st) st = evpg_equilibrium_solve(ctx, e_vm, it);
-        if (!st) st = evpg_increment_end(ctx, reorient, inc);
+        if (!st) st = evpg_increment_end(ctx, tail, inc);
         return st;
     }
     Batch* b = (Batch*)c->solo;
@@ -597,7 +597,7 @@ int evpg_increment(void* ctx, const double udot_dt[3][3], int32_t creep, const d
         st = set_slots(*b, &c, 1);
         if (st) return st;
     }
-    stage(*b, 0, udot_dt, creep, disgrad_avg_actual, time_tot, e_vm, reorient);
+    stage(*b, 0, udot_dt, creep, disgrad_avg_actual, time_tot, e_vm, tail);
     int ticks = 0;
     const int st = run_round(*b, c->cfg.iter_max + 1, &ticks);
     if (st) return st;

@@ -94,7 +94,7 @@ struct IncrCtl {
     double e_vm;        // strain-error normaliser of this increment
     double err0;        // initial error value (2*Err)
     int creep;
-    int reorient;       // update_orient in the increment tail
+    int tail;           // increment-tail flags: 1 update_orient, 2 GND slip-rate gradients
     int phase;          // 0 idle, 1 begin requested, 2 running, 3 ended
     int pad;
 };

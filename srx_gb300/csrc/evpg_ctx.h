@@ -42,6 +42,10 @@ struct Ctx {
     double *sig64, *dg64, *dg_old, *epsp, *edot64, *rho_s, *rho_m, *gamdot64, *gam_acum,
         *tranmat, *schm64, *fc64, *sgr64;
     int32_t *orient, *phase;
+    // first-order GND densities (gnd = 1 only)
+    double *rho_g, *gproj;
+    uint8_t* gbm;
+    double l0;
     // FP32 working set (FP32 bulk only)
     float *sig32, *ddg32, *b6_32, *schm32, *fc32, *sgr32;
     void* spec;  // 9 * Nh complex of the working precision

@@ -736,6 +736,35 @@ __global__ void k_phase(Macro* m, int from, int to) {
 
 // update_schmid (kinematics.c:430-463) and the rho-dependent products of the
 // flow rule that stay fixed during an increment (constitutive.c:559-633).
+// GND densities of voxel v: g1 = rho_g1 (screw), g2 = rho_g2 (edge type I),
+// zero past n_sys; rho_g3 stays zero to first order.
+__device__ __forceinline__ void load_gnd(const double* __restrict__ rho_g, int N, int v, int nsys,
+                                         double g1[NS], double g2[NS]) {
+#pragma unroll
+    for (int j = 0; j < NS; j++) {
+        g1[j] = (j < nsys) ? rho_g[(size_t)j * N + v] : 0.0;
+        g2[j] = (j < nsys) ? rho_g[(size_t)(NS + j) * N + v] : 0.0;
+    }
+}
+
+// rho_P and rho_F of system i with the projected GND densities
+// (constitutive.c:558-577): sum_j Chi (Chi_1) times rho_s + |rho_g1 sin (cos)
+// theta_g1| + |rho_g2 sin (cos) theta_g2|.
+__device__ __forceinline__ void forest_parallel_gnd(const PhaseK<double>& P, const double* __restrict__ gp,
+                                                    int i, const double rs[NS], const double g1[NS],
+                                                    const double g2[NS], double& rP, double& rf) {
+    rP = 0.0;
+    rf = 0.0;
+#pragma unroll
+    for (int j = 0; j < NS; j++) {
+        const int ij = i * NS + j;
+        const double tf = rs[j] + fabs(g1[j] * gp[GP_COS1 + ij]) + fabs(g2[j] * gp[GP_COS2 + ij]);
+        const double tp = rs[j] + fabs(g1[j] * gp[GP_SIN1 + ij]) + fabs(g2[j] * gp[GP_SIN2 + ij]);
+        rP += P.chi[i][j] * tp;
+        rf += P.chi1[i][j] * tf;
+    }
+}
+
 __device__ __forceinline__ void begin_body(const BeginArgs& a, int bid) {
     const int v = bid * 128 + threadIdx.x;
     const int N = a.g.N;
@@ -790,12 +819,19 @@ __device__ __forceinline__ void begin_body(const BeginArgs& a, int bid) {
     double rs[NS];
 #pragma unroll
     for (int i = 0; i < NS; i++) rs[i] = (i < P.n_sys) ? a.rho_s[(size_t)i * N + v] : 0.0;
+    double g1[NS], g2[NS];
+    const double* gp = a.rho_g ? a.gproj + (size_t)(ph - 1) * GP_STRIDE : nullptr;
+    if (gp) load_gnd(a.rho_g, N, v, P.n_sys, g1, g2);
     for (int i = 0; i < P.n_sys; i++) {
         double rP = 0.0, rf = 0.0;
+        if (gp) {
+            forest_parallel_gnd(P, gp, i, rs, g1, g2, rP, rf);
+        } else {
 #pragma unroll
-        for (int j = 0; j < NS; j++) {
-            rP += P.chi[i][j] * rs[j];
-            rf += P.chi1[i][j] * rs[j];
+            for (int j = 0; j < NS; j++) {
+                rP += P.chi[i][j] * rs[j];
+                rf += P.chi1[i][j] * rs[j];
+            }
         }
         const double rm_stale = a.rho_m[(size_t)i * N + v];
         const double rm = P.k_rhom[i] * sqrt(rP * rf);
@@ -874,9 +910,34 @@ __device__ void reorient(double tran[3][3], const double rot[3][3]) {
         for (int j = 0; j < 3; j++) tran[i][j] = tn[i][j];
 }
 
+// One directional derivative of Gradient_ShearRate (constitutive.c:881-1112)
+// from the same-grain bits of the plus and minus neighbours: backward,
+// forward or central difference, zero with no neighbour in the grain.
+__device__ __forceinline__ double gb_diff(double c, double vp, double vm, unsigned same_p, unsigned same_m) {
+    if (!same_p && same_m) return c - vm;
+    if (same_p && !same_m) return vp - c;
+    if (same_p && same_m) return (vp - vm) / 2.0;
+    return 0.0;
+}
+
+// gadot_grad of system i at voxel v (one rank: periodic neighbours).
+__device__ __forceinline__ void slip_rate_gradient(const EndArgs& a, int v, int i, double gr[3]) {
+    const int n0 = a.g.n0, n1 = a.g.n1, n2 = a.g.n2;
+    const int x = v / (n1 * n2), y = (v / n2) % n1, z = v % n2;
+    const int xp = x + 1 == n0 ? 0 : x + 1, xm = x == 0 ? n0 - 1 : x - 1;
+    const int yp = y + 1 == n1 ? 0 : y + 1, ym = y == 0 ? n1 - 1 : y - 1;
+    const int zp = z + 1 == n2 ? 0 : z + 1, zm = z == 0 ? n2 - 1 : z - 1;
+    const double* gd = a.gamdot + (size_t)i * a.g.N;
+    const unsigned m = a.gbm[v];
+    gr[0] = gb_diff(gd[v], gd[(xp * n1 + y) * n2 + z], gd[(xm * n1 + y) * n2 + z], m & 1u, m & 2u);
+    gr[1] = gb_diff(gd[v], gd[(x * n1 + yp) * n2 + z], gd[(x * n1 + ym) * n2 + z], m & 4u, m & 8u);
+    gr[2] = gb_diff(gd[v], gd[(x * n1 + y) * n2 + zp], gd[(x * n1 + y) * n2 + zm], m & 16u, m & 32u);
+}
+
 __device__ __forceinline__ void end_body(const EndArgs& a, int bid) {
     const int v = bid * END_BLOCK + threadIdx.x;
-    const int reorient_on = a.macro->ctl.reorient;
+    const int reorient_on = a.macro->ctl.tail & 1;
+    const int grad_on = a.macro->ctl.tail & 2;
     const int N = a.g.N;
     const double dt = a.mat.dt;
     double q[NPART_END];
@@ -940,17 +1001,27 @@ __device__ __forceinline__ void end_body(const EndArgs& a, int bid) {
             double rs[NS], rf[NS], rP[NS], rm[NS], rtot = 0.0;
 #pragma unroll
             for (int i = 0; i < NS; i++) rs[i] = (i < P.n_sys) ? a.rho_s[(size_t)i * N + v] : 0.0;
+            // GND densities before this increment's update (the flow rule's
+            // trial values and rho_tot, evolution.c:1041-1045)
+            double g1[NS], g2[NS];
+            const double* gp = a.rho_g ? a.gproj + (size_t)(ph - 1) * GP_STRIDE : nullptr;
+            if (gp) load_gnd(a.rho_g, N, v, P.n_sys, g1, g2);
             for (int i = 0; i < P.n_sys; i++) {
                 double x = 0.0, y = 0.0;
+                if (gp) {
+                    forest_parallel_gnd(P, gp, i, rs, g1, g2, x, y);
+                } else {
 #pragma unroll
-                for (int j = 0; j < NS; j++) {
-                    x += P.chi[i][j] * rs[j];
-                    y += P.chi1[i][j] * rs[j];
+                    for (int j = 0; j < NS; j++) {
+                        x += P.chi[i][j] * rs[j];
+                        y += P.chi1[i][j] * rs[j];
+                    }
                 }
                 rP[i] = x;
                 rf[i] = y;
                 rm[i] = P.k_rhom[i] * sqrt(x * y);
-                rtot += rs[i] + a.rho_m[(size_t)i * N + v];
+                rtot += gp ? rs[i] + a.rho_m[(size_t)i * N + v] + sqrt(g1[i] * g1[i] + g2[i] * g2[i])
+                           : rs[i] + a.rho_m[(size_t)i * N + v];
             }
             double s6[6];
 #pragma unroll
@@ -976,6 +1047,20 @@ __device__ __forceinline__ void end_body(const EndArgs& a, int bid) {
                 a.rho_s[(size_t)i * N + v] = rn;
                 a.rho_m[(size_t)i * N + v] = rm[i];
                 a.gam_acum[(size_t)i * N + v] += gd[i] * dt;
+                if (gp) {
+                    // first-order GND rates (constitutive.c:1428-1522): screw
+                    // grad(gamdot).p / b / L0, edge type I -grad(gamdot).b / b / L0
+                    double gr[3] = {0.0, 0.0, 0.0};
+                    if (grad_on) slip_rate_gradient(a, v, i, gr);
+                    const double* bp = gp + GP_BP + 3 * i;
+                    const double d1 = (gr[0] * bp[0] + gr[1] * bp[1] + gr[2] * bp[2]) / b / a.l0;
+                    const double d2 =
+                        -1.0 * (gr[0] * P.bb[i][0] + gr[1] * P.bb[i][1] + gr[2] * P.bb[i][2]) / b / a.l0;
+                    const double n1 = g1[i] + d1 * dt, n2 = g2[i] + d2 * dt;
+                    a.rho_g[(size_t)i * N + v] = n1;
+                    a.rho_g[(size_t)(NS + i) * N + v] = n2;
+                    q[18] += sqrt(n1 * n1 + n2 * n2);
+                }
                 q[0] += rf[i];
                 q[1] += rP[i];
                 q[2] += rn;
@@ -1022,7 +1107,7 @@ __device__ __forceinline__ void end_reduce_body(const EndReduceArgs& a) {
     m->rho_avg[1] = tot[1] * a.wgt;
     m->rho_avg[2] = tot[2] * a.wgt;
     m->rho_avg[3] = tot[3] * a.wgt;
-    m->rho_avg[4] = 0.0;
+    m->rho_avg[4] = tot[18] * a.wgt;
     m->rho_avg[5] = m->rho_dip_acc * a.wgt;
     m->rho_avg[6] = m->rho_for_acc * a.wgt;
     m->rho_avg[7] = m->rho_inp_acc * a.wgt;
@@ -1079,6 +1164,7 @@ void build_solver_sets(Ctx& c) {
     b.dg64 = c.dg64; b.dg_old = c.dg_old; b.tranmat = c.tranmat; b.rho_s = c.rho_s;
     b.rho_m = c.rho_m; b.phase = c.phase; b.schm64 = c.schm64; b.fc64 = c.fc64;
     b.schm32 = c.schm32; b.fc32 = c.fc32; b.b6_32 = c.b6_32; b.ddg32 = c.ddg32; b.epsp = c.epsp;
+    b.rho_g = c.rho_g; b.gproj = c.gproj;
     k.grid_begin = (c.g.N + 127) / 128;
     FoldArgs& f = k.fold;
     f.g = c.g; f.macro = c.macro; f.gate = GATE_ENDING; f.dg64 = c.dg64; f.ddg32 = c.ddg32;
@@ -1092,6 +1178,7 @@ void build_solver_sets(Ctx& c) {
     e.tranmat = c.tranmat; e.rho_s = c.rho_s; e.rho_m = c.rho_m; e.gamdot = c.gamdot64;
     e.gam_acum = c.gam_acum; e.sig64 = c.sig64; e.schm64 = c.schm64; e.phase = c.phase;
     e.sig32 = c.sig32; e.part = c.part_end;
+    e.rho_g = c.rho_g; e.gproj = c.gproj; e.gbm = c.gbm; e.l0 = c.l0;
     k.grid_end = c.nb_end;
     EndReduceArgs& r = k.endr;
     r.macro = c.macro; r.gate = GATE_ENDING; r.part = c.part_end; r.nblocks = c.nb_end; r.wgt = c.cfg.wgt;

@@ -42,7 +42,7 @@ typedef struct {
     double TimeStep, Err, VelGrad_BC[6], Stress_BC[6], ElastConst_PhaseI[4],
         ElastConst_PhaseII[4];
     char Slip_PhaseI[100], Slip_PhaseII[100], initial_ms[100];
-    double a0[2], T__K, Q_slip[2], Q_bulk[2], C_1[2], C_2[2], C_3[2], C_4[2], C_5[2], C_6[2],
+    double a0[2], L0, T__K, Q_slip[2], Q_bulk[2], C_1[2], C_2[2], C_3[2], C_4[2], C_5[2], C_6[2],
         Selfinter0[2], Coplanar0[2], CrossSlip0[2], GlissileJunction0[2], HirthLock0[2],
         LomerCottrellLock0[2], rho_SSD_initial, D_0, tau_DRX, DeltaTau_DRX;
 } evpg_namelist;
@@ -71,7 +71,7 @@ typedef struct evpg_job {
     double rho_avg[8];
     long long nr_iters;
     FILE *err_log;
-    int precision, nr_mode;
+    int precision, nr_mode, gnd;
     t2 dE_unapplied;  /* sum over increments of the last iteration's dDisGradAvg */
 } evpg_job;
 
@@ -117,6 +117,7 @@ static int read_namelist(const char *path, evpg_namelist *nl)
         {"ElastConst_PhaseII", nl->ElastConst_PhaseII, NR, 4, 0},
         {"Slip_PhaseI", nl->Slip_PhaseI, NSTR, 1, 0}, {"Slip_PhaseII", nl->Slip_PhaseII, NSTR, 1, 0},
         {"initial_ms", nl->initial_ms, NSTR, 1, 0}, {"a0", nl->a0, NR, 2, 0},
+        {"L0", &nl->L0, NR, 1, 0},
         {"T__K", &nl->T__K, NR, 1, 0}, {"Q_slip", nl->Q_slip, NR, 2, 0},
         {"Q_bulk", nl->Q_bulk, NR, 2, 0}, {"C_1", nl->C_1, NR, 2, 0}, {"C_2", nl->C_2, NR, 2, 0},
         {"C_3", nl->C_3, NR, 2, 0}, {"C_4", nl->C_4, NR, 2, 0}, {"C_5", nl->C_5, NR, 2, 0},
@@ -530,6 +531,12 @@ int evpg_job_close(void *jp)
 
 int evpg_job_open(const char *input, const char *rho0, int32_t precision, int32_t nr_mode, void **out)
 {
+    return evpg_job_open_opts(input, rho0, precision, nr_mode, 0, out);
+}
+
+int evpg_job_open_opts(const char *input, const char *rho0, int32_t precision, int32_t nr_mode,
+                       int32_t options, void **out)
+{
     evpg_job *j;
     char path[1024];
     int i, a, b, v, st, p;
@@ -697,6 +704,10 @@ int evpg_job_open(const char *input, const char *rho0, int32_t precision, int32_
         j->nr_mode = nr_mode;
         d.precision = precision;
         d.nr_mode = nr_mode;
+        j->gnd = (options & EVPG_JOB_GND) != 0;
+        d.gnd = j->gnd;
+        d.l0 = j->nl.L0;
+        d.voxel_grain = j->grain_f;
         st = evpg_create(&d, &j->ctx);
         free(cg);
         free(sg);
@@ -790,14 +801,17 @@ int evpg_job_grid(const char *input, int32_t n[3])
 
 /* Controls of increment istep (evolution.c:1115-1128): Udot*TimeStep,
  * creep, the applied average, TimeTot, the strain-error normaliser e_vm and
- * whether update_orient runs in the tail (Update_Flag == 1 && istep > 1). */
-static void job_controls(const evpg_job *j, int istep, t2 udt, int *reorient)
+ * the tail flags: update_orient when Update_Flag == 1 && istep > 1
+ * (evolution.c:1340-1343), the GND slip-rate gradients when Hard_Flag == 1
+ * && istep > 1 (evolution.c:1348-1357). */
+static void job_controls(const evpg_job *j, int istep, t2 udt, int *tail)
 {
     const double dt = j->nl.TimeStep;
     int a, b;
     for (a = 0; a < 3; a++)
         for (b = 0; b < 3; b++) udt[a][b] = j->Udot[a][b] * dt;
-    *reorient = (j->nl.Update_Flag == 1) && (istep > 1);
+    *tail = ((j->nl.Update_Flag == 1) && (istep > 1) ? EVPG_TAIL_REORIENT : 0) |
+            (j->gnd && (j->nl.Hard_Flag == 1) && (istep > 1) ? EVPG_TAIL_GND_GRADIENT : 0);
 }
 
 /* Increment bookkeeping after the tail (evolution.c:1273-1332). */
@@ -846,9 +860,9 @@ int evpg_job_increment(void *jp, int32_t istep, int32_t *iters)
     t2 udt;
     evpg_iter_out io;
     evpg_incr_out eo;
-    int st, reorient;
+    int st, tail;
     if (!j) return EVPG_ERR_ARG;
-    job_controls(j, istep, udt, &reorient);
+    job_controls(j, istep, udt, &tail);
     if (j->err_log) {
         st = evpg_increment_begin(j->ctx, (const double(*)[3])udt, j->CREEP_FLAG == 1,
                                   (const double(*)[3])j->DisGradAvg_actual, j->TimeTot);
@@ -859,12 +873,12 @@ int evpg_job_increment(void *jp, int32_t istep, int32_t *iters)
             if (st) return st;
             fprintf(j->err_log, "%d %d %.17g %.17g %.17g\n", istep, io.iter, io.err_e, io.err_s, io.s_vm);
         } while (!io.converged && io.iter < j->nl.IterMax);
-        st = evpg_increment_end(j->ctx, reorient, &eo);
+        st = evpg_increment_end(j->ctx, tail, &eo);
         if (st) return st;
     } else {
         /* the whole increment as one graph launch */
         st = evpg_increment(j->ctx, (const double(*)[3])udt, j->CREEP_FLAG == 1,
-                            (const double(*)[3])j->DisGradAvg_actual, j->TimeTot, j->e_vm, reorient, &io, &eo);
+                            (const double(*)[3])j->DisGradAvg_actual, j->TimeTot, j->e_vm, tail, &io, &eo);
         if (st) return st;
     }
     if (iters) *iters = io.iter;
@@ -877,11 +891,11 @@ int evpg_job_stage(void *jp, void *batch, int32_t slot, int32_t istep)
 {
     evpg_job *j = (evpg_job *)jp;
     t2 udt;
-    int reorient;
+    int tail;
     if (!j || !batch) return EVPG_ERR_ARG;
-    job_controls(j, istep, udt, &reorient);
+    job_controls(j, istep, udt, &tail);
     return evpg_batch_stage(batch, slot, (const double(*)[3])udt, j->CREEP_FLAG == 1,
-                            (const double(*)[3])j->DisGradAvg_actual, j->TimeTot, j->e_vm, reorient);
+                            (const double(*)[3])j->DisGradAvg_actual, j->TimeTot, j->e_vm, tail);
 }
 
 /* After a round: if the job's increment in `slot` ended, do its bookkeeping

@@ -19,8 +19,11 @@ FP64, FP32_BULK = 0, 1
 NR_PLAIN, NR_LINESEARCH = 0, 1
 F_SIG, F_DISGRAD, F_EPS, F_EDOT, F_TRANMAT = 0, 1, 2, 3, 4
 F_RHO_S, F_RHO_M, F_GAMDOT, F_GAM_ACUM, F_VELGRAD, F_SIG6 = 5, 6, 7, 8, 9, 10
+F_RHO_G1, F_RHO_G2 = 11, 12  # GND densities (jobs opened with gnd=True)
 FIELD_WIDTH = {F_SIG: 9, F_DISGRAD: 9, F_EPS: 9, F_EDOT: 9, F_TRANMAT: 9, F_RHO_S: 12,
-               F_RHO_M: 12, F_GAMDOT: 12, F_GAM_ACUM: 12, F_VELGRAD: 9, F_SIG6: 6}
+               F_RHO_M: 12, F_GAMDOT: 12, F_GAM_ACUM: 12, F_VELGRAD: 9, F_SIG6: 6,
+               F_RHO_G1: 12, F_RHO_G2: 12}
+JOB_GND = 1  # evpg_job_open_opts option: first-order GND densities (DD_GND)
 
 
 class EvpgError(RuntimeError):
@@ -58,6 +61,7 @@ def lib() -> C.CDLL:
         L.evpg_status_string.restype = C.c_char_p
         L.evpg_status_string.argtypes = [C.c_int]
         L.evpg_job_open.argtypes = [C.c_char_p, C.c_char_p, i32, i32, C.POINTER(vp)]
+        L.evpg_job_open_opts.argtypes = [C.c_char_p, C.c_char_p, i32, i32, i32, C.POINTER(vp)]
         L.evpg_job_close.argtypes = [vp]
         L.evpg_job_ctx.argtypes = [vp]
         L.evpg_job_ctx.restype = vp
@@ -102,14 +106,16 @@ def check(st: int) -> None:
 
 
 class Job:
-    """A job of the host driver: the reference's input files on the device."""
+    """A job of the host driver: the reference's input files on the device.
+    gnd=True adds the first-order GND densities (the reference built with
+    DD_GND)."""
 
     def __init__(self, input_path: str, rho0: Optional[str] = None, precision: int = FP64,
-                 nr_mode: int = NR_PLAIN):
+                 nr_mode: int = NR_PLAIN, gnd: bool = False):
         L = lib()
         h = C.c_void_p()
-        check(L.evpg_job_open(input_path.encode(), rho0.encode() if rho0 else None,
-                              precision, nr_mode, C.byref(h)))
+        check(L.evpg_job_open_opts(input_path.encode(), rho0.encode() if rho0 else None,
+                                   precision, nr_mode, JOB_GND if gnd else 0, C.byref(h)))
         self._h = h
         n = (C.c_int32 * 3)()
         check(L.evpg_job_nvox(h, n))

@@ -218,3 +218,41 @@ def test_batch_mixing_fused_and_separate_passes(tmp_path, precision):
     finally:
         for j in jobs:
             j.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_batch_with_gnd_slot_equals_alone(tmp_path, precision):
+    """A context with GND densities next to contexts without them in one
+    batch: every RVE, the GND densities included, keeps its solo bits."""
+    from srx_gb300 import rve
+    evpg = _evpg()
+    cases = []
+    for i, (grid, load, gnd) in enumerate((((12, 12, 12), "tension", True), ((12, 10, 9), "compression", False),
+                                           ((8, 8, 8), "tension", True))):
+        job = rve.Job(n=grid, load=load, rate=1e-3, strain_per_step=2e-4, n_steps=4)
+        c = rve.make_case(str(tmp_path / ("g%d" % i)), grid, 5, 80 + i, job, rho0=(0.5, 5.0))
+        c["gnd"] = gnd
+        cases.append(c)
+
+    def fields(j, gnd):
+        st = _state(evpg, j)
+        if gnd:
+            st[evpg.F_RHO_G1] = j.download(evpg.F_RHO_G1)
+            st[evpg.F_RHO_G2] = j.download(evpg.F_RHO_G2)
+        return st
+    ref = []
+    for c in cases:
+        with evpg.Job(c["input"], c["rho0"], precision=precision, nr_mode=1, gnd=c["gnd"]) as j:
+            ref.append(([j.increment(k) for k in range(4)], fields(j, c["gnd"])))
+    jobs = [evpg.Job(c["input"], c["rho0"], precision=precision, nr_mode=1, gnd=c["gnd"]) for c in cases]
+    try:
+        its, _ = evpg.run_batched(jobs, [4, 4, 4], max_ticks=29)
+        assert its == [r[0] for r in ref]
+        for j, c, (_, st) in zip(jobs, cases, ref):
+            got = fields(j, c["gnd"])
+            for f, v in st.items():
+                assert np.array_equal(got[f], v), f
+        assert np.abs(ref[0][1][evpg.F_RHO_G1]).max() > 0
+    finally:
+        for j in jobs:
+            j.close()

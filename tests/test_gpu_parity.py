@@ -61,6 +61,53 @@ def test_line_search_cases_match_reference(tmp_path, name):
         assert rel_err(f[k][idx], z[k]) < FIELD_TOL, k
 
 
+def test_gnd_densities_match_reference(tmp_path):
+    """First-order GND densities (the reference built with DD_GND), FP64
+    plain form, line search, 12^3: iteration counts of all five increments,
+    vm.out, the last increment's fields and the final screw and edge GND
+    densities of every voxel. The slip-rate gradients start in the third
+    increment and reach the flow rule in the fourth, where the iteration
+    counts differ from the run without GND densities."""
+    evpg = _evpg()
+    z, spec = golden("gnd12_ls")
+    case = write_spec_case(spec, tmp_path / "case")
+    N = int(np.prod(spec["n"]))
+    out = tmp_path / "out"
+    os.makedirs(out, exist_ok=True)
+    with evpg.Job(case["input"], None, precision=0, nr_mode=1, gnd=True) as j:
+        j.run(str(out), spec["steps"], iout=True)
+        g1 = j.download(evpg.F_RHO_G1)
+        g2 = j.download(evpg.F_RHO_G2)
+        rm = j.download(evpg.F_RHO_M)
+    assert read_iters(out) == list(z["iters"])
+    assert rel_err(read_table(out / "vm.out"), z["vm"]) < PRINT_TOL
+    f = read_iout_fields(out, spec["steps"] - 1, N)
+    for k in ("sig", "eps", "els", "rho_s", "gam_acum", "newpos"):
+        assert rel_err(f[k], z[k]) < FIELD_TOL, k
+    assert rel_err(g1, z["final_rho_g1"]) < FIELD_TOL
+    assert rel_err(g2, z["final_rho_g2"]) < FIELD_TOL
+    assert rel_err(rm, z["final_rho_m"]) < FIELD_TOL
+    assert np.abs(g1).max() > 0.1
+
+
+def test_gnd_fp32_bulk_within_stated_error(tmp_path):
+    """The FP32-bulk form with GND densities: macroscopic stress within 1e-4
+    of the reference's FP64 run, stress and GND fields within 1e-3 (L2)."""
+    evpg = _evpg()
+    z, spec = golden("gnd12_ls")
+    case = write_spec_case(spec, tmp_path / "case")
+    N = int(np.prod(spec["n"]))
+    with evpg.Job(case["input"], None, precision=1, nr_mode=1, gnd=True) as j:
+        for k in range(spec["steps"]):
+            j.increment(k)
+        sig = j.download(evpg.F_SIG6)
+        g1 = j.download(evpg.F_RHO_G1)
+    l2 = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))
+    assert l2(sig, z["sig"]) < 1e-3
+    assert l2(g1, z["final_rho_g1"]) < 1e-3
+    assert rel_err(sig.mean(axis=0), z["sig"].mean(axis=0)) < 1e-4
+
+
 def _oracle_case(tmp_path, gas=False, iter_max=1000, steps=3):
     """Non-power-of-two grid (radix 3 and 5 stages, odd length, Nyquist planes
     on two axes), z tension; with gas=True the sixth grain is a gas phase.
