@@ -107,12 +107,23 @@ __device__ __forceinline__ void sinh_cosh(float x, float& sh, float& ch) {
 // StrainRate_Orowan at stress s (constitutive.c:585-725): per slip system the
 // resolved shear stress and the sinh glide law with its derivative; returns
 // edot (5), the upper triangle of d_edot (15) and the shear rates (shared
-// memory column of this thread). The system loop stays rolled to keep the
-// kernel small. bad |= NaN seen (the reference asserts).
+// memory column of this thread). bad |= NaN seen (the reference asserts).
+// Two passes: the resolved shear stresses of all systems give the mask of
+// systems above their passing stress; the glide law then runs over the set
+// bits only, lowest first, so a warp iterates max(active per lane) times
+// instead of once per system any lane has active. The sums keep the system
+// order, so the results are those of one pass over all systems.
 // Per-voxel constants of the slip systems staged in shared memory for the
 // sweep (column of this thread, stride NR_BLOCK): Schmid vectors at
 // [5i+q], tau_pass at [60+i], 1/(tau0+tau_cut) at [72+i], gam_o at [84+i].
 constexpr int NSTAGE = 96;
+
+template <typename T>
+__device__ __forceinline__ T resolved_shear(const T* cs, const T* s, int i, T (&sc)[5]) {
+#pragma unroll
+    for (int q = 0; q < 5; q++) sc[q] = cs[(i * 5 + q) * NR_BLOCK];
+    return sc[0] * s[0] + sc[1] * s[1] + sc[2] * s[2] + sc[3] * s[3] + sc[4] * s[4];
+}
 
 template <typename T>
 __device__ __forceinline__ void flow_eval(const NrArgs<T>& a, int nsys, int v, const T* cs,
@@ -122,33 +133,39 @@ __device__ __forceinline__ void flow_eval(const NrArgs<T>& a, int nsys, int v, c
     for (int q = 0; q < 5; q++) ed[q] = (T)0;
 #pragma unroll
     for (int q = 0; q < 15; q++) dd[q] = (T)0;
+    unsigned act = 0;
 #pragma unroll 1
     for (int i = 0; i < nsys; i++) {
         T sc[5];
-#pragma unroll
-        for (int q = 0; q < 5; q++) sc[q] = cs[(i * 5 + q) * NR_BLOCK];
-        const T rss = sc[0] * s[0] + sc[1] * s[1] + sc[2] * s[2] + sc[3] * s[3] + sc[4] * s[4];
+        const T rss = resolved_shear<T>(cs, s, i, sc);
+        const T tp = stale ? __ldg(a.fc + (size_t)(36 + i) * N + v) : cs[(60 + i) * NR_BLOCK];
+        if (fabs(rss) > tp) act |= 1u << i;
+        if (gam) gam[i * NR_BLOCK] = (T)0;  // only sweeps that output gamdot keep them
+    }
+#pragma unroll 1
+    while (act) {
+        const int i = __ffs(act) - 1;
+        act &= act - 1;
+        T sc[5];
+        const T rss = resolved_shear<T>(cs, s, i, sc);
         const T tp = stale ? __ldg(a.fc + (size_t)(36 + i) * N + v) : cs[(60 + i) * NR_BLOCK];
         const T ar = fabs(rss);
-        T g = (T)0;
-        if (ar > tp) {
-            const T itc = cs[(72 + i) * NR_BLOCK];
-            const T go = cs[(84 + i) * NR_BLOCK];
-            T sh, ch;
-            sinh_cosh((ar - tp) * itc, sh, ch);
-            g = (rss > (T)0) ? go * sh : -(go * sh);
-            const T g2 = go * ch * itc;
+        const T itc = cs[(72 + i) * NR_BLOCK];
+        const T go = cs[(84 + i) * NR_BLOCK];
+        T sh, ch;
+        sinh_cosh((ar - tp) * itc, sh, ch);
+        const T g = (rss > (T)0) ? go * sh : -(go * sh);
+        const T g2 = go * ch * itc;
 #pragma unroll
-            for (int q = 0; q < 5; q++) ed[q] += sc[q] * g;
-            int k = 0;
+        for (int q = 0; q < 5; q++) ed[q] += sc[q] * g;
+        int k = 0;
 #pragma unroll
-            for (int p = 0; p < 5; p++) {
-                const T w = sc[p] * g2;
+        for (int p = 0; p < 5; p++) {
+            const T w = sc[p] * g2;
 #pragma unroll
-                for (int q = p; q < 5; q++) dd[k++] += w * sc[q];
-            }
+            for (int q = p; q < 5; q++) dd[k++] += w * sc[q];
         }
-        if (gam) gam[i * NR_BLOCK] = g;  // only sweeps that output gamdot keep them
+        if (gam) gam[i * NR_BLOCK] = g;
     }
     bool nan = false;
 #pragma unroll
@@ -390,7 +407,27 @@ __device__ __forceinline__ void nr_body(const NrArgs<T>& a, int bid, unsigned ch
                         for (int c = 0; c < 6; c++) step[c] *= cap;
                         slope *= cap;
                     }
-                    if (!(slope < (T)0)) {
+                    bool whole = false;
+                    if (a.quick_accept && slope < (T)0) {
+                        // a step below the NR tolerance ends the NR whatever the line
+                        // search would pick (a shorter step only lowers erral): take it
+                        // whole; the trial's merit would decide a change below the
+                        // tolerance. FP32 loop sweeps only.
+                        T cnr = 0;
+#pragma unroll
+                        for (int c = 0; c < 6; c++) {
+                            const T d = (old[c] + step[c]) - old[c];
+                            cnr += d * d;
+                        }
+                        if (!(fdiv(sqrt(cnr), signorm) > a.tol)) {
+#pragma unroll
+                            for (int c = 0; c < 6; c++) sig[c] = old[c] + step[c];
+                            whole = true;
+                            finish = true;
+                        }
+                    }
+                    if (whole) {
+                    } else if (!(slope < (T)0)) {
                         if (slope != (T)0) { lsfail = true; break; }
                         finish = true;  // R == 0: at the root already
                     } else {
@@ -1141,6 +1178,7 @@ static void nr_set(Ctx& c, NrSet<T>& S, const Material<T>& mat, T* sig, const T*
     a.orient = c.orient; a.phase = c.phase; a.sgr = sgr; a.edot = edot; a.gamdot = gamdot;
     a.macro = c.macro; a.part = c.part_nr; a.tol = tol; a.itmax = c.nr_itmax;
     a.nr_mode = c.nr_mode; a.stale_mode = stale_mode; a.gate = gate;
+    a.quick_accept = 0;
     S.grid = c.nb_nr;
 }
 
@@ -1155,6 +1193,7 @@ void build_solver_sets(Ctx& c) {
                        c.gamdot64, (double)c.nr_tol64, 0, GATE_ENDING);
         nr_set<float>(c, k.nr32, c.m32, c.sig32, c.ddg32, c.b6_32, c.schm32, c.fc32, c.sgr32, nullptr,
                       nullptr, (float)c.nr_tol32, 1, GATE_RUNNING);
+        k.nr32.a.quick_accept = 1;
     }
     MacroArgs& m = k.mac;
     m.cfg = c.cfg; m.macro = c.macro; m.part = c.part_nr; m.nrows = c.nb_nr * (NR_BLOCK / 32);
