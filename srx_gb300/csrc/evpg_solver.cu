@@ -277,6 +277,16 @@ __device__ __forceinline__ void warp_store(float (&q)[NPART_NR], double* row) {
     }
 }
 
+// Asynchronous copy of one scalar from global to this thread's shared-memory
+// column (no register round trip, all copies of a thread in flight at once).
+template <typename T>
+__device__ __forceinline__ void stage_async(T* dst, const T* src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(d), "l"(src), "n"(sizeof(T)) : "memory");
+}
+__device__ __forceinline__ void stage_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void stage_wait() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
 template <typename T> struct NrMinBlocks { static constexpr int v = 2; };
 template <> struct NrMinBlocks<float> { static constexpr int v = 4; };
 
@@ -315,12 +325,14 @@ __device__ __forceinline__ void nr_body(const NrArgs<T>& a, int bid, unsigned ch
     } else if (v < N) {
         const int nsys = P.n_sys;
         const T* sg = a.sgr + (size_t)a.orient[v] * SGR_STRIDE;
+        // the staging copies overlap the loads of the voxel's state below
         for (int i = 0; i < nsys; i++) {
 #pragma unroll
-            for (int q = 0; q < 5; q++) stg[(i * 5 + q) * NR_BLOCK] = __ldg(a.schm + (size_t)(i * 5 + q) * N + v);
+            for (int q = 0; q < 5; q++) stage_async<T>(stg + (i * 5 + q) * NR_BLOCK, a.schm + (size_t)(i * 5 + q) * N + v);
 #pragma unroll
-            for (int q = 0; q < 3; q++) stg[(60 + 12 * q + i) * NR_BLOCK] = __ldg(a.fc + (size_t)(12 * q + i) * N + v);
+            for (int q = 0; q < 3; q++) stage_async<T>(stg + (60 + 12 * q + i) * NR_BLOCK, a.fc + (size_t)(12 * q + i) * N + v);
         }
+        stage_commit();
         T lam[6], sig[6], av[6], old[6], step[6], te[6];
 #pragma unroll
         for (int c = 0; c < 6; c++) {
@@ -328,6 +340,7 @@ __device__ __forceinline__ void nr_body(const NrArgs<T>& a, int bid, unsigned ch
             sig[c] = lam[c];
             av[c] = a.epsb[(size_t)c * N + v] - a.dg[(size_t)c * N + v];
         }
+        stage_wait();
         T signorm = 0;
 #pragma unroll
         for (int c = 0; c < 6; c++) signorm += lam[c] * lam[c];
