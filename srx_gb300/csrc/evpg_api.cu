@@ -60,6 +60,7 @@ static void make_plan(int n, FftPlan& p) {
         p.ns[s] = ns;
         ns *= p.radix[s];
     }
+    plan_divisors(p);
 }
 
 // exp(-2 pi i t / n) with exact axis values and quadrant symmetry

@@ -81,6 +81,9 @@ template <typename T> struct XArgs {
     const C2<T>* tw;
     int P;
     GreenK<T> gk;
+    // index divisors: n0, and np, n0*np for full tiles ([0], np = P) and the
+    // last tile ([1], np = nh - (tiles - 1) P)
+    FastDiv dn, dnp[2], dnnp[2];
 };
 
 template <typename T> struct NrArgs {
@@ -114,6 +117,7 @@ struct MacroArgs {
     int nrows;
     double* part2;        // [MACRO_BLOCKS][NPART_NR]
     unsigned int* ticket; // last-block detection, reset by the last block
+    int f32rows;          // 1: rows hold float pairs (hi, lo) of the FP32 sweep, else doubles
 };
 
 struct BeginArgs {

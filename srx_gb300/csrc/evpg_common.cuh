@@ -139,10 +139,38 @@ struct Grid {
 };
 
 // Stockham FFT plan for one axis length.
+// Division by a divisor d >= 1 fixed per launch, for dividends below 2^24,
+// as a multiply and shift: q = (x * m) >> s with s = 24 + ceil(log2 d) and
+// m = ceil(2^s / d) < 2^25 + 1. Exact: x m / 2^s exceeds x / d by less than
+// 2^24 d / (d 2^s) <= 1/d, so the floor is unchanged. Replaces the
+// integer-divide sequence in the index arithmetic of the FFT loops.
+struct FastDiv {
+    unsigned long long m;
+    int s;
+    __host__ __device__ void set(int d) {
+        int l = 0;
+        while ((1 << l) < d) l++;
+        s = 24 + l;
+        m = ((1ull << s) + (unsigned long long)d - 1) / (unsigned long long)d;
+    }
+    __device__ __forceinline__ int div(int x) const {
+        return (int)(((unsigned long long)(unsigned)x * m) >> s);
+    }
+};
+
 struct FftPlan {
     int n, nf;
     int radix[12];
     int ns[12];
+    FastDiv dm[12], dns[12];  // n / radix[s] and ns[s]
 };
+
+// Divisors of every stage, after radix[] and ns[] are set.
+inline void plan_divisors(FftPlan& p) {
+    for (int s = 0; s < p.nf; s++) {
+        p.dm[s].set(p.n / p.radix[s]);
+        p.dns[s].set(p.ns[s]);
+    }
+}
 
 }  // namespace evpg

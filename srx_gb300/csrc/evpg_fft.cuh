@@ -94,11 +94,12 @@ __device__ C2<T>* fft_batch(C2<T>* a, C2<T>* b, int npen, int ps, const FftPlan&
     for (int s = 0; s < pl.nf; s++) {
         const int r = pl.radix[s], Ns = pl.ns[s], m = n / r, tws = n / (Ns * r);
         const int total = npen * m;
+        const FastDiv dm = pl.dm[s], dns = pl.dns[s];
         for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
-            const int pen = idx / m, j = idx - pen * m;
-            const int jm = j % Ns;
+            const int pen = dm.div(idx), j = idx - pen * m;
+            const int jq = dns.div(j), jm = j - jq * Ns;
             const C2<T>* src = in + pen * ps + j;
-            C2<T>* dst = out + pen * ps + (j / Ns) * Ns * r + jm;
+            C2<T>* dst = out + pen * ps + jq * Ns * r + jm;
             C2<T> v[8];
             if (r == 8) {
 #pragma unroll

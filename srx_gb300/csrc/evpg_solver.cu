@@ -250,7 +250,8 @@ __device__ __forceinline__ void sgr_v(const T* sg, const T* x, T* y) {
 }
 
 // Warp-level partial sums without a block barrier: every warp writes its own
-// row of NPART_NR values (FP32: compensated within the warp).
+// row of NPART_NR values (FP64 sweeps: doubles; FP32 sweeps: compensated
+// within the warp, stored as the float pair sum + compensation).
 __device__ __forceinline__ void warp_store(double (&q)[NPART_NR], double* row) {
     const int lane = threadIdx.x & 31;
 #pragma unroll
@@ -273,7 +274,7 @@ __device__ __forceinline__ void warp_store(float (&q)[NPART_NR], double* row) {
             ks.add(s);
             ks.c += c;
         }
-        if (lane == 0) row[k] = (double)ks.s + (double)ks.c;
+        if (lane == 0) reinterpret_cast<float2*>(row)[k] = make_float2(ks.s, ks.c);
     }
 }
 
@@ -596,9 +597,11 @@ __global__ void __launch_bounds__(NR_BLOCK, NrMinBlocks<T>::v) kb_nr(const NrArg
 
 
 // get_smacro and the loop test (evolution.c:590-664, 1227-1252, 1150) on the
-// FP64 totals; thread 0 of the last block.
+// FP64 totals; thread 0 of the last block. Everything is computed in
+// registers and written to the macro state once at the end (the state lives
+// in global memory, where every read after a write would wait on L2).
 __device__ void macro_update(const LoopCfg& c, Macro* m, const double* tot) {
-    double s6[6], s16[6], sa[3][3], s1a[3][3];
+    double s6[6], s16[6], sa[3][3], s1a[3][3], dE[3][3];
     for (int q = 0; q < 6; q++) {
         s6[q] = tot[2 + q];
         s16[q] = tot[8 + q];
@@ -607,8 +610,9 @@ __device__ void macro_update(const LoopCfg& c, Macro* m, const double* tot) {
     b6_to_sym<double>(s16, s1a);
     for (int i = 0; i < 3; i++)
         for (int j = 0; j < 3; j++) {
-            m->sig_avg[i][j] = sa[i][j] * c.wgt;
-            m->sig_avg1[i][j] = s1a[i][j] * (c.wgt / c.wgt_ph1);
+            sa[i][j] = sa[i][j] * c.wgt;
+            s1a[i][j] = s1a[i][j] * (c.wgt / c.wgt_ph1);
+            dE[i][j] = 0.0;
         }
     const int IJV[2][6] = {{0, 1, 2, 1, 0, 0}, {0, 1, 2, 2, 2, 1}};
     for (int i = 0; i < 6; i++) {
@@ -617,28 +621,28 @@ __device__ void macro_update(const LoopCfg& c, Macro* m, const double* tot) {
         if (c.vflag[i] == 0)
             for (int k = 0; k < 6; k++) {
                 const int kk = IJV[0][k], ll = IJV[1][k];
-                d += c.s0[ii][jj][kk][ll] * c.sflag[k] * (c.scauchy[kk][ll] - m->sig_avg[kk][ll]);
+                d += c.s0[ii][jj][kk][ll] * c.sflag[k] * (c.scauchy[kk][ll] - sa[kk][ll]);
             }
-        m->dE[ii][jj] = d;
+        dE[ii][jj] = d;
     }
-    for (int i = 0; i < 3; i++)
-        for (int j = 0; j < 3; j++) m->dE_acum[i][j] += m->dE[i][j];
+    double dE9[9];
     {
         double e6[6];
-        sym_to_b6<double>(m->dE, e6);
-        for (int q = 0; q < 6; q++) m->dE9[q] = e6[q];
-        m->dE9[6] = 0.5 * (m->dE[0][1] - m->dE[1][0]);
-        m->dE9[7] = 0.5 * (m->dE[0][2] - m->dE[2][0]);
-        m->dE9[8] = 0.5 * (m->dE[1][2] - m->dE[2][1]);
+        sym_to_b6<double>(dE, e6);
+        for (int q = 0; q < 6; q++) dE9[q] = e6[q];
+        dE9[6] = 0.5 * (dE[0][1] - dE[1][0]);
+        dE9[7] = 0.5 * (dE[0][2] - dE[2][0]);
+        dE9[8] = 0.5 * (dE[1][2] - dE[2][1]);
     }
     // s_vm: the reference's trace term reads SigDevAvg[3][3], one element past
     // the array; in its global layout that is SigAvg1[0][0].
+    double s_vm, s_vm1;
     {
         double v6[6], dev[3][3];
-        sym_to_b6<double>(m->sig_avg, v6);
+        sym_to_b6<double>(sa, v6);
         v6[5] = 0.0;
         b6_to_sym<double>(v6, dev);
-        const double oob = m->sig_avg1[0][0];
+        const double oob = s1a[0][0];
         double s = 0.0;
         for (int i = 0; i < 3; i++)
             for (int j = 0; j < 3; j++) {
@@ -648,60 +652,118 @@ __device__ void macro_update(const LoopCfg& c, Macro* m, const double* tot) {
                     s += d * d;
                 }
             }
-        m->s_vm = sqrt(1.5 * s);
-        sym_to_b6<double>(m->sig_avg1, v6);
+        s_vm = sqrt(1.5 * s);
+        sym_to_b6<double>(s1a, v6);
         v6[5] = 0.0;
         b6_to_sym<double>(v6, dev);
         s = 0.0;
         for (int i = 0; i < 3; i++)
             for (int j = 0; j < 3; j++) s += dev[i][j] * dev[i][j];
-        m->s_vm1 = sqrt(1.5 * s);
+        s_vm1 = sqrt(1.5 * s);
     }
+    const double e_vm = m->e_vm;
+    double ee = tot[0] * c.wgt, es = tot[1] * c.wgt;
+    if (fabs(e_vm) < 1E-5) ee = 0.0;
+    else ee /= e_vm;
+    es /= s_vm;
+    const int iter = m->iter + 1;
+    const double mx = (fabs(es) > fabs(ee)) ? fabs(es) : fabs(ee);
+    const int converged = !(mx > c.err_tol);
+    const int status = m->status;
+    const long long nr = m->nr_iters;
+    double acum[3][3];
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) acum[i][j] = m->dE_acum[i][j] + dE[i][j];
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) {
+            m->sig_avg[i][j] = sa[i][j];
+            m->sig_avg1[i][j] = s1a[i][j];
+            m->dE[i][j] = dE[i][j];
+            m->dE_acum[i][j] = acum[i][j];
+        }
+    for (int q = 0; q < 9; q++) m->dE9[q] = dE9[q];
+    m->s_vm = s_vm;
+    m->s_vm1 = s_vm1;
     m->err_e_sum = tot[0];
     m->err_s_sum = tot[1];
-    double ee = tot[0] * c.wgt, es = tot[1] * c.wgt;
-    if (fabs(m->e_vm) < 1E-5) ee = 0.0;
-    else ee /= m->e_vm;
-    es /= m->s_vm;
     m->err_e = ee;
     m->err_s = es;
-    m->nr_iters += (long long)tot[14];
-    m->iter += 1;
-    const double mx = (fabs(es) > fabs(ee)) ? fabs(es) : fabs(ee);
-    m->converged = !(mx > c.err_tol);
-    m->done = m->converged || m->iter >= c.iter_max || m->status != 0;
+    m->nr_iters = nr + (long long)tot[14];
+    m->iter = iter;
+    m->converged = converged;
+    m->done = converged || iter >= c.iter_max || status != 0;
 }
 
 // Deterministic two-level sum of the NR warp partials: each block sums a
 // contiguous range of rows in a fixed order; the last block to finish sums
 // the block rows in order and runs the macro update.
 // bid: block index within the RVE's MACRO_BLOCKS blocks.
-__device__ __forceinline__ void macro_body(const MacroArgs& a, int bid) {
+// Accumulators of the macro sums: FP64 for the FP64 sweep's rows; for the
+// FP32 sweep's rows, float pairs (hi, lo) added exactly as a double-float
+// (two-sum of the high parts, then the low parts), which keeps ~44 bits on
+// the FP32 pipe instead of the narrow FP64 one.
+struct AccD {
+    double v;
+    __device__ __forceinline__ static AccD zero() { return {0.0}; }
+    __device__ __forceinline__ static AccD load(const double* p) { return {*p}; }
+    __device__ __forceinline__ static AccD load_cg(const double* p) { return {__ldcg(p)}; }
+    __device__ __forceinline__ void add(const AccD& b) { v += b.v; }
+    __device__ __forceinline__ AccD shfl(int o) const { return {__shfl_xor_sync(0xffffffffu, v, o)}; }
+    __device__ __forceinline__ void store(double* p) const { *p = v; }
+    __device__ __forceinline__ double value() const { return v; }
+};
+struct AccF {
+    float h, l;
+    __device__ __forceinline__ static AccF zero() { return {0.0f, 0.0f}; }
+    __device__ __forceinline__ static AccF load(const double* p) {
+        const float2 f = *reinterpret_cast<const float2*>(p);
+        return {f.x, f.y};
+    }
+    __device__ __forceinline__ static AccF load_cg(const double* p) {
+        const float2 f = __ldcg(reinterpret_cast<const float2*>(p));
+        return {f.x, f.y};
+    }
+    __device__ __forceinline__ void add(const AccF& b) {
+        const float s = h + b.h, bv = s - h;
+        float e = (h - (s - bv)) + (b.h - bv);
+        e += l + b.l;
+        h = s + e;
+        l = e - (h - s);
+    }
+    __device__ __forceinline__ AccF shfl(int o) const {
+        return {__shfl_xor_sync(0xffffffffu, h, o), __shfl_xor_sync(0xffffffffu, l, o)};
+    }
+    __device__ __forceinline__ void store(double* p) const { *reinterpret_cast<float2*>(p) = make_float2(h, l); }
+    __device__ __forceinline__ double value() const { return (double)h + (double)l; }
+};
+
+template <typename A>
+__device__ __forceinline__ void macro_body_t(const MacroArgs& a, int bid) {
     Macro* m = a.macro;
-    __shared__ double red[NPART_NR][8];
+    __shared__ A red[NPART_NR][8];
     __shared__ bool last;
     const int nb = MACRO_BLOCKS;
     const int per = (a.nrows + nb - 1) / nb;
     const int r0 = bid * per, r1 = min(a.nrows, r0 + per);
-    double v[NPART_NR];
+    A v[NPART_NR];
 #pragma unroll
-    for (int q = 0; q < NPART_NR; q++) v[q] = 0.0;
+    for (int q = 0; q < NPART_NR; q++) v[q] = A::zero();
     for (int r = r0 + (int)threadIdx.x; r < r1; r += blockDim.x)
 #pragma unroll
-        for (int q = 0; q < NPART_NR; q++) v[q] += a.part[(size_t)r * NPART_NR + q];
+        for (int q = 0; q < NPART_NR; q++) v[q].add(A::load(a.part + (size_t)r * NPART_NR + q));
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
     for (int q = 0; q < NPART_NR; q++) {
-        double x = v[q];
+        A x = v[q];
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+        for (int o = 16; o > 0; o >>= 1) x.add(x.shfl(o));
         if (lane == 0) red[q][wid] = x;
     }
     __syncthreads();
     if (threadIdx.x < NPART_NR) {
-        double s = 0.0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); w++) s += red[threadIdx.x][w];
-        a.part2[(size_t)bid * NPART_NR + threadIdx.x] = s;
+        A s = A::zero();
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) s.add(red[threadIdx.x][w]);
+        s.store(a.part2 + (size_t)bid * NPART_NR + threadIdx.x);
     }
     __threadfence();
     __syncthreads();
@@ -714,25 +776,30 @@ __device__ __forceinline__ void macro_body(const MacroArgs& a, int bid) {
     __shared__ double tot[NPART_NR];
 #pragma unroll
     for (int q = 0; q < NPART_NR; q++)
-        v[q] = (int)threadIdx.x < nb ? __ldcg(a.part2 + (size_t)threadIdx.x * NPART_NR + q) : 0.0;
+        v[q] = (int)threadIdx.x < nb ? A::load_cg(a.part2 + (size_t)threadIdx.x * NPART_NR + q) : A::zero();
 #pragma unroll
     for (int q = 0; q < NPART_NR; q++) {
-        double x = v[q];
+        A x = v[q];
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+        for (int o = 16; o > 0; o >>= 1) x.add(x.shfl(o));
         if (lane == 0) red[q][wid] = x;
     }
     __syncthreads();
     if (threadIdx.x < NPART_NR) {
-        double t = 0.0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += red[threadIdx.x][w];
-        tot[threadIdx.x] = t;
+        A t = A::zero();
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t.add(red[threadIdx.x][w]);
+        tot[threadIdx.x] = t.value();
     }
     __syncthreads();
     if (threadIdx.x == 0) {
         *a.ticket = 0;
         macro_update(a.cfg, m, tot);
     }
+}
+
+__device__ __forceinline__ void macro_body(const MacroArgs& a, int bid) {
+    if (a.f32rows) macro_body_t<AccF>(a, bid);
+    else macro_body_t<AccD>(a, bid);
 }
 
 __global__ void __launch_bounds__(256) k_macro(const __grid_constant__ MacroArgs a) {
@@ -1210,7 +1277,7 @@ void build_solver_sets(Ctx& c) {
     }
     MacroArgs& m = k.mac;
     m.cfg = c.cfg; m.macro = c.macro; m.part = c.part_nr; m.nrows = c.nb_nr * (NR_BLOCK / 32);
-    m.part2 = c.part_nr2; m.ticket = c.ticket;
+    m.part2 = c.part_nr2; m.ticket = c.ticket; m.f32rows = c.precision != 0;
     BeginArgs& b = k.beg;
     b.mat = c.m64; b.g = c.g; b.macro = c.macro; b.gate = GATE_BEGIN;
     b.dg64 = c.dg64; b.dg_old = c.dg_old; b.tranmat = c.tranmat; b.rho_s = c.rho_s;

@@ -101,9 +101,11 @@ __device__ __forceinline__ void x_green_body(const XArgs<T>& a, const GreenK<T>&
     const int y = bid / ntile, kz0 = (bid % ntile) * P, np = min(P, nh - kz0);
     const size_t xs = (size_t)g.n1 * nh;
     const T rn[3] = {gk.rn[0], gk.rn[1], gk.rn[2]};
+    const int tile = np == P ? 0 : 1;
+    const FastDiv dq = a.dnp[tile], dnq = a.dnnp[tile];
     load_tw<T>(tw, a.tw, n);
     for (int i = threadIdx.x; i < 6 * n * np; i += blockDim.x) {
-        const int c = i / (n * np), rem = i - c * n * np, x = rem / np, kk = rem - x * np;
+        const int c = dnq.div(i), rem = i - c * n * np, x = dq.div(rem), kk = rem - x * np;
         cp_async_elem<T>(bA + (c * np + kk) * ps + x, a.spec + (size_t)c * g.Nh + x * xs + (size_t)y * nh + kz0 + kk);
     }
     cp_async_wait_all();
@@ -111,7 +113,7 @@ __device__ __forceinline__ void x_green_body(const XArgs<T>& a, const GreenK<T>&
     C2<T>* R = fft_batch<T, -1>(bA, bB, 6 * np, ps, a.pl, tw);
     C2<T>* W = (R == bA) ? bB : bA;
     for (int i = threadIdx.x; i < n * np; i += blockDim.x) {
-        const int kk = i / n, kx = i - kk * n, kz = kz0 + kk, ky = y;
+        const int kk = a.dn.div(i), kx = i - kk * n, kz = kz0 + kk, ky = y;
         C2<T> sb[6], du[9];
 #pragma unroll
         for (int c = 0; c < 6; c++) sb[c] = R[(c * np + kk) * ps + kx];
@@ -145,7 +147,7 @@ __device__ __forceinline__ void x_green_body(const XArgs<T>& a, const GreenK<T>&
     __syncthreads();
     const C2<T>* R2 = fft_batch<T, 1>(W, (W == bA) ? bB : bA, 9 * np, ps, a.pl, tw);
     for (int i = threadIdx.x; i < 9 * n * np; i += blockDim.x) {
-        const int c = i / (n * np), rem = i - c * n * np, x = rem / np, kk = rem - x * np;
+        const int c = dnq.div(i), rem = i - c * n * np, x = dq.div(rem), kk = rem - x * np;
         a.spec[(size_t)c * g.Nh + x * xs + (size_t)y * nh + kz0 + kk] = R2[(c * np + kk) * ps + x];
     }
 }
@@ -545,6 +547,17 @@ int plane_epl(const Grid& g, size_t elem) {
     return sm <= PLANE_SMEM_MAX ? E : 0;
 }
 
+// Index divisors of the X pass for its grid and pencils per CTA.
+template <typename T> static void set_x_divisors(XArgs<T>& xa) {
+    const Grid& g = xa.g;
+    const int last = g.nh - ((g.nh + xa.P - 1) / xa.P - 1) * xa.P;
+    xa.dn.set(g.n0);
+    xa.dnp[0].set(xa.P);
+    xa.dnnp[0].set(g.n0 * xa.P);
+    xa.dnp[1].set(last);
+    xa.dnnp[1].set(g.n0 * last);
+}
+
 template <typename T>
 static void fill_spec_t(Ctx& c, SpecSet<T>& s, const int P[3], const FftPlan pl[3], T* sig, T* dg,
                         const C2<T>* const* tw, int fused) {
@@ -579,6 +592,7 @@ static void fill_spec_t(Ctx& c, SpecSet<T>& s, const int P[3], const FftPlan pl[
     xa.gk.rn[0] = (T)(1.0 / g.n0);
     xa.gk.rn[1] = (T)(1.0 / g.n1);
     xa.gk.rn[2] = (T)(1.0 / g.n2);
+    set_x_divisors<T>(xa);
     s.grid_x = g.n1 * ((g.nh + xa.P - 1) / xa.P);
     s.sm_x = (size_t)(g.n0 + 18 * xa.P * (g.n0 + 1)) * es;
     s.epl = fused ? plane_epl(g, es) : 0;
@@ -781,6 +795,7 @@ static void plan_of(int n, const std::vector<int>& f, FftPlan& p) {
         p.ns[s] = ns;
         ns *= f[s];
     }
+    plan_divisors(p);
 }
 
 // Factor orders of n: radices 8/4/2 for the power-of-two part (at most one
@@ -1012,6 +1027,7 @@ static void na_plan(int n, FftPlan& p) {
         p.ns[s] = ns;
         ns *= p.radix[s];
     }
+    plan_divisors(p);
 }
 
 // exp(-2 pi i t/n) with exact axis values (same table as the context path)
@@ -1111,6 +1127,7 @@ extern "C" int evpg_green_correction_noalloc(const double* sig6, double* du9, in
     xa.gk.rn[0] = 1.0 / n0;
     xa.gk.rn[1] = 1.0 / n1;
     xa.gk.rn[2] = 1.0 / n2;
+    set_x_divisors<double>(xa);
     const size_t smx = (size_t)(n0 + 18 * xa.P * (n0 + 1)) * es;
     const int ntile_x = (g.nh + xa.P - 1) / xa.P;
     set_kernel_attributes();
