@@ -113,6 +113,9 @@ static void fill_material(const evpg_rve_desc* d, Material<T>& m) {
             k.k_tcut[i] = (T)((kT / 0.62415063631) / s.c2 / s.c3 / b / b * 0.1);
             k.k_rhom[i] = (T)(2.0 * kT / s.c1 / s.c2 / s.c3 / s.shear_g / (b * b * b) * 160.2177);
             k.k_gamo[i] = (T)(1E-3 * 1.0E10 * s.c2 * b * exp(-1.0 * s.q_slip));
+            k.k_ddip[i] = (T)(sqrt(3.0) * s.shear_g * b / 16.0 / 3.14159265359 / (1 - d->nu));
+            k.k_hyd[i] = (T)(s.shear_g * b / 3.14159265359 / (1 - d->nu));
+            k.k_d0b[i] = (T)(d->d0 / b);
             for (int q = 0; q < 5; q++) k.schm_xt[i][q] = (T)s.schm_xt[i][q];
             for (int q = 0; q < 3; q++) {
                 k.bn[i][q] = (T)s.bn[i][q];

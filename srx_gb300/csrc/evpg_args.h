@@ -105,8 +105,9 @@ template <typename T> struct NrArgs {
     int itmax, nr_mode;
     int stale_mode;       // 1: the first flow-rule call of the increment uses the stored rho_m
     int gate;
-    // 1 (FP32-bulk loop sweep only): a line-search Newton step that already meets the
-    // NR tolerance is taken whole, without the trial evaluation of its merit
+    // 1 (FP32-bulk form: loop sweep and FP64 refinement): a line-search Newton step
+    // that already meets the NR tolerance is taken whole, without the trial
+    // evaluation of its merit
     int quick_accept;
 };
 

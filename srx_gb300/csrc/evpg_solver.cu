@@ -426,7 +426,7 @@ __device__ __forceinline__ void nr_body(const NrArgs<T>& a, int bid, unsigned ch
                         // a step below the NR tolerance ends the NR whatever the line
                         // search would pick (a shorter step only lowers erral): take it
                         // whole; the trial's merit would decide a change below the
-                        // tolerance. FP32 loop sweeps only.
+                        // tolerance. FP32-bulk form only.
                         T cnr = 0;
 #pragma unroll
                         for (int c = 0; c < 6; c++) {
@@ -1143,16 +1143,16 @@ __device__ __forceinline__ void end_body(const EndArgs& a, int bid) {
             double s6[6];
 #pragma unroll
             for (int c = 0; c < 6; c++) s6[c] = a.sig64[(size_t)c * N + v];
-            const double G = P.shear_g, nu = a.mat.nu, T = a.mat.temperature, D0 = a.mat.d0;
+            const double T = a.mat.temperature;
             const double eqb = exp(-1.0 * P.q_bulk);
             for (int i = 0; i < P.n_sys; i++) {
                 const double* sc = a.schm64 + (size_t)(i * 5) * N + v;
                 const double rss = sc[0] * s6[0] + sc[(size_t)N] * s6[1] + sc[2 * (size_t)N] * s6[2] +
                                    sc[3 * (size_t)N] * s6[3] + sc[4 * (size_t)N] * s6[4];
                 const double b = P.burgers[i];
-                const double ddip = sqrt(3.0) * G * b / 16.0 / 3.14159265359 / (1 - nu) / (fabs(rss) + 1.0E-4);
-                const double hyd = G * b / 3.14159265359 / (1 - nu) / ddip;
-                const double clim = 1E-17 * rtot * 0.5 * 1E24 * ddip * (D0 / b) * (rs[i] * rs[i]) *
+                const double ddip = P.k_ddip[i] / (fabs(rss) + 1.0E-4);
+                const double hyd = P.k_hyd[i] / ddip;
+                const double clim = 1E-17 * rtot * 0.5 * 1E24 * ddip * P.k_d0b[i] * (rs[i] * rs[i]) *
                                     (exp(fabs(hyd) * b * b * b * 100 / (1.38 * T)) - 1.0) * eqb;
                 const double ag = fabs(gd[i]);
                 const double sq = sqrt(rf[i]);
@@ -1274,6 +1274,10 @@ void build_solver_sets(Ctx& c) {
         nr_set<float>(c, k.nr32, c.m32, c.sig32, c.ddg32, c.b6_32, c.schm32, c.fc32, c.sgr32, nullptr,
                       nullptr, (float)c.nr_tol32, 1, GATE_RUNNING);
         k.nr32.a.quick_accept = 1;
+        // the refinement starts from the converged FP32 stress: its last step
+        // is below the tolerance, and the slip rates it keeps are those of the
+        // evaluation before that step (a change below the NR tolerance)
+        k.nr64.a.quick_accept = 1;
     }
     MacroArgs& m = k.mac;
     m.cfg = c.cfg; m.macro = c.macro; m.part = c.part_nr; m.nrows = c.nb_nr * (NR_BLOCK / 32);
