@@ -192,7 +192,7 @@ struct EndReduceArgs {
 
 // Fused z and y passes: one CTA per (x plane, component pair), warp-register
 // FFTs along z and y, the plane's half spectra staged in shared memory.
-constexpr int PLANE_THREADS = 512;
+constexpr int PLANE_THREADS = 1024;
 constexpr int PLANE_WARPS = PLANE_THREADS / 32;
 
 template <typename T> struct PlaneArgs {
@@ -207,6 +207,7 @@ template <typename T> struct PlaneArgs {
     const double* dE9;   // macro correction added in the inverse pass
     T invN;
     int nhp;             // row length of the shared-memory planes (odd, >= nh)
+    FastDiv dnh;         // divisor nh of the plane copy loops
 };
 
 // Everything one RVE context launches, with grid sizes and dynamic shared

@@ -285,7 +285,7 @@ __device__ __forceinline__ void plane_fwd_body(const PlaneArgs<T>& a, int bid, u
     C2<T>* oa = a.spec + (size_t)(2 * p) * g.Nh + (size_t)x * g.n1 * nh;
     C2<T>* ob = a.spec + (size_t)(2 * p + 1) * g.Nh + (size_t)x * g.n1 * nh;
     for (int i = threadIdx.x; i < g.n1 * nh; i += blockDim.x) {
-        const int y = i / nh, k = i - y * nh;
+        const int y = a.dnh.div(i), k = i - y * nh;
         oa[i] = SA[y * nhp + k];
         ob[i] = SB[y * nhp + k];
     }
@@ -309,7 +309,7 @@ __device__ __forceinline__ void plane_inv_body(const PlaneArgs<T>& a, int bid, u
     const C2<T>* ia = a.spec + (size_t)ca * g.Nh + (size_t)x * g.n1 * nh;
     const C2<T>* ib = a.spec + (size_t)(hasb ? cb : ca) * g.Nh + (size_t)x * g.n1 * nh;
     for (int i = threadIdx.x; i < g.n1 * nh; i += blockDim.x) {
-        const int y = i / nh, k = i - y * nh;
+        const int y = a.dnh.div(i), k = i - y * nh;
         cp_async_elem<T>(SA + y * nhp + k, ia + i);
         if (hasb) cp_async_elem<T>(SB + y * nhp + k, ib + i);
     }
@@ -599,6 +599,7 @@ static void fill_spec_t(Ctx& c, SpecSet<T>& s, const int P[3], const FftPlan pl[
     PlaneArgs<T>& pa = s.pl;
     pa.g = g; pa.macro = c.macro; pa.gate = GATE_RUNNING; pa.sig = sig; pa.dg = dg; pa.spec = spec;
     pa.twz = tw[2]; pa.twy = tw[1]; pa.dE9 = za.dE9; pa.invN = za.invN; pa.nhp = g.nh | 1;
+    pa.dnh.set(g.nh);
     s.grid_pf = 3 * g.n0;
     s.grid_pi = 5 * g.n0;
     s.sm_p = (size_t)(g.n2 + g.n1 + 2 * g.n1 * pa.nhp + PLANE_WARPS * g.n2) * es;
