@@ -251,31 +251,60 @@ __device__ __forceinline__ void sgr_v(const T* sg, const T* x, T* y) {
 
 // Warp-level partial sums without a block barrier: every warp writes its own
 // row of NPART_NR values (FP64 sweeps: doubles; FP32 sweeps: compensated
-// within the warp, stored as the float pair sum + compensation).
+// within the warp, stored as the float pair sum + compensation). The 15
+// values (padded to 16) are reduced by recursive halving: at each of the
+// first four levels a lane keeps half of its values and receives the
+// partner's copy of that half, so the warp exchanges 8+4+2+1 values, then
+// the last level sums lane pairs; lane 2k ends with value k. 16 shuffle
+// steps instead of 15 butterflies of 5.
+constexpr unsigned kFull = 0xffffffffu;
+
 __device__ __forceinline__ void warp_store(double (&q)[NPART_NR], double* row) {
     const int lane = threadIdx.x & 31;
+    double v[16];
 #pragma unroll
-    for (int k = 0; k < NPART_NR; k++) {
-        double x = q[k];
+    for (int k = 0; k < 16; k++) v[k] = k < NPART_NR ? q[k] : 0.0;
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-        if (lane == 0) row[k] = x;
+    for (int st = 0; st < 4; st++) {
+        const int h = 8 >> st, o = 16 >> st;
+        const bool up = (lane & o) != 0;
+#pragma unroll
+        for (int j = 0; j < h; j++) {
+            const double send = up ? v[j] : v[j + h];
+            const double keep = up ? v[j + h] : v[j];
+            v[j] = keep + __shfl_xor_sync(kFull, send, o);
+        }
     }
+    v[0] += __shfl_xor_sync(kFull, v[0], 1);
+    if (!(lane & 1) && (lane >> 1) < NPART_NR) row[lane >> 1] = v[0];
 }
 __device__ __forceinline__ void warp_store(float (&q)[NPART_NR], double* row) {
     const int lane = threadIdx.x & 31;
+    float s[16], c[16];
 #pragma unroll
-    for (int k = 0; k < NPART_NR; k++) {
-        KSum ks{q[k], 0.0f};
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const float s = __shfl_xor_sync(0xffffffffu, ks.s, o);
-            const float c = __shfl_xor_sync(0xffffffffu, ks.c, o);
-            ks.add(s);
-            ks.c += c;
-        }
-        if (lane == 0) reinterpret_cast<float2*>(row)[k] = make_float2(ks.s, ks.c);
+    for (int k = 0; k < 16; k++) {
+        s[k] = k < NPART_NR ? q[k] : 0.0f;
+        c[k] = 0.0f;
     }
+#pragma unroll
+    for (int st = 0; st < 5; st++) {
+        const int h = st < 4 ? 8 >> st : 1, o = 16 >> st;
+        const bool up = st < 4 && (lane & o) != 0;
+#pragma unroll
+        for (int j = 0; j < h; j++) {
+            const float ss = up ? s[j] : s[j + (st < 4 ? h : 0)];
+            const float cs = up ? c[j] : c[j + (st < 4 ? h : 0)];
+            KSum ks{up ? s[j + h] : s[j], up ? c[j + h] : c[j]};
+            const float rs = __shfl_xor_sync(kFull, ss, o);
+            const float rc = __shfl_xor_sync(kFull, cs, o);
+            ks.add(rs);
+            ks.c += rc;
+            s[j] = ks.s;
+            c[j] = ks.c;
+        }
+    }
+    if (!(lane & 1) && (lane >> 1) < NPART_NR)
+        reinterpret_cast<float2*>(row)[lane >> 1] = make_float2(s[0], c[0]);
 }
 
 // Asynchronous copy of one scalar from global to this thread's shared-memory
