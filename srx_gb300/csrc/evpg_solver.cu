@@ -427,16 +427,6 @@ __device__ __forceinline__ void nr_body(const NrArgs<T>& a, int bid, unsigned ch
                     // step = -J^-1 R capped at length 10, i.e. -|R|^2 times the cap
                     // factor; used directly because through an ill-conditioned J
                     // the rounded product can change sign.
-                    T CR[6];
-                    mat6v<T>(C66, te, CR);
-                    f_old = 0;
-#pragma unroll
-                    for (int c = 0; c < 6; c++) {
-                        const T r = dl[c] + CR[c];
-                        f_old += r * r;
-                    }
-                    slope = -f_old;
-                    f_old *= (T)0.5;
                     T nrm = 0;
 #pragma unroll
                     for (int c = 0; c < 6; c++) {
@@ -444,29 +434,42 @@ __device__ __forceinline__ void nr_body(const NrArgs<T>& a, int bid, unsigned ch
                         nrm += step[c] * step[c];
                     }
                     nrm = sqrt(nrm);
-                    if (nrm > (T)10) {
-                        const T cap = fdiv((T)10, nrm);
-#pragma unroll
-                        for (int c = 0; c < 6; c++) step[c] *= cap;
-                        slope *= cap;
-                    }
                     bool whole = false;
-                    if (a.quick_accept && slope < (T)0) {
+                    if (a.quick_accept && nrm <= (T)10) {
                         // a step below the NR tolerance ends the NR whatever the line
                         // search would pick (a shorter step only lowers erral): take it
                         // whole; the trial's merit would decide a change below the
-                        // tolerance. FP32-bulk form only.
+                        // tolerance. FP32-bulk form only. A NaN step fails the test and
+                        // takes the line search's error path.
                         T cnr = 0;
 #pragma unroll
                         for (int c = 0; c < 6; c++) {
                             const T d = (old[c] + step[c]) - old[c];
                             cnr += d * d;
                         }
-                        if (!(fdiv(sqrt(cnr), signorm) > a.tol)) {
+                        if (fdiv(sqrt(cnr), signorm) <= a.tol) {
 #pragma unroll
                             for (int c = 0; c < 6; c++) sig[c] = old[c] + step[c];
                             whole = true;
                             finish = true;
+                        }
+                    }
+                    if (!whole) {
+                        T CR[6];
+                        mat6v<T>(C66, te, CR);
+                        f_old = 0;
+#pragma unroll
+                        for (int c = 0; c < 6; c++) {
+                            const T r = dl[c] + CR[c];
+                            f_old += r * r;
+                        }
+                        slope = -f_old;
+                        f_old *= (T)0.5;
+                        if (nrm > (T)10) {
+                            const T cap = fdiv((T)10, nrm);
+#pragma unroll
+                            for (int c = 0; c < 6; c++) step[c] *= cap;
+                            slope *= cap;
                         }
                     }
                     if (whole) {
