@@ -225,6 +225,13 @@ __device__ __forceinline__ void inv_z_body(const ZArgs<T>& a, int bid, unsigned 
 // DisGrad (same update as the separate inverse-z pass). No intermediate
 // spectrum goes through global memory between the z and y transforms.
 
+// Shared-memory row skew of the plane kernels: row r is stored at r + r/16.
+// The warp FFTs scatter their outputs to rows k2 + E*brev5(lane), which
+// without the skew fall on two 8-byte bank groups per half-warp (8-way
+// conflicts); with it every half-warp access hits 16 distinct groups.
+__device__ __forceinline__ int pskew(int r) { return r + (r >> 4); }
+__host__ __device__ constexpr int plane_rows(int n) { return n + n / 16; }
+
 template <typename T, int E>
 __device__ __forceinline__ void plane_fwd_body(const PlaneArgs<T>& a, int bid, unsigned char* smem) {
     const Grid& g = a.g;
@@ -234,8 +241,8 @@ __device__ __forceinline__ void plane_fwd_body(const PlaneArgs<T>& a, int bid, u
     C2<T>* twz = reinterpret_cast<C2<T>*>(smem);
     C2<T>* twy = twz + n;
     C2<T>* SA = twy + g.n1;
-    C2<T>* SB = SA + (size_t)g.n1 * nhp;
-    C2<T>* R = SB + (size_t)g.n1 * nhp + (size_t)warp * n;
+    C2<T>* SB = SA + (size_t)plane_rows(g.n1) * nhp;
+    C2<T>* R = SB + (size_t)plane_rows(g.n1) * nhp + (size_t)warp * plane_rows(n);
     for (int i = threadIdx.x; i < n; i += blockDim.x) twz[i] = a.twz[i];
     for (int i = threadIdx.x; i < g.n1; i += blockDim.x) twy[i] = a.twy[i];
     __syncthreads();
@@ -258,14 +265,14 @@ __device__ __forceinline__ void plane_fwd_body(const PlaneArgs<T>& a, int bid, u
         warp_fft<T, E, -1>(v, twz, lane);
         const int b = brev5(lane);
 #pragma unroll
-        for (int k2 = 0; k2 < E; k2++) R[k2 + E * b] = v[k2];
+        for (int k2 = 0; k2 < E; k2++) R[pskew(k2 + E * b)] = v[k2];
         __syncwarp();
         for (int k = lane; k < nh; k += 32) {
-            const C2<T> z = R[k];
-            const C2<T> w = R[k == 0 ? 0 : n - k];
+            const C2<T> z = R[pskew(k)];
+            const C2<T> w = R[pskew(k == 0 ? 0 : n - k)];
             // A = (Z(k) + conj Z(n-k))/2, B = (Z(k) - conj Z(n-k))/(2i)
-            SA[y * nhp + k] = mk<T>((T)0.5 * (z.x + w.x), (T)0.5 * (z.y - w.y));
-            SB[y * nhp + k] = mk<T>((T)0.5 * (z.y + w.y), (T)-0.5 * (z.x - w.x));
+            SA[pskew(y) * nhp + k] = mk<T>((T)0.5 * (z.x + w.x), (T)0.5 * (z.y - w.y));
+            SB[pskew(y) * nhp + k] = mk<T>((T)0.5 * (z.y + w.y), (T)-0.5 * (z.x - w.x));
         }
         __syncwarp();
     }
@@ -275,19 +282,19 @@ __device__ __forceinline__ void plane_fwd_body(const PlaneArgs<T>& a, int bid, u
         const int kz = (c < nh) ? c : c - nh;
         C2<T> v[E];
 #pragma unroll
-        for (int q = 0; q < E; q++) v[q] = S[(lane + 32 * q) * nhp + kz];
+        for (int q = 0; q < E; q++) v[q] = S[pskew(lane + 32 * q) * nhp + kz];
         warp_fft<T, E, -1>(v, twy, lane);
         const int b = brev5(lane);
 #pragma unroll
-        for (int k2 = 0; k2 < E; k2++) S[(k2 + E * b) * nhp + kz] = v[k2];
+        for (int k2 = 0; k2 < E; k2++) S[pskew(k2 + E * b) * nhp + kz] = v[k2];
     }
     __syncthreads();
     C2<T>* oa = a.spec + (size_t)(2 * p) * g.Nh + (size_t)x * g.n1 * nh;
     C2<T>* ob = a.spec + (size_t)(2 * p + 1) * g.Nh + (size_t)x * g.n1 * nh;
     for (int i = threadIdx.x; i < g.n1 * nh; i += blockDim.x) {
         const int y = a.dnh.div(i), k = i - y * nh;
-        oa[i] = SA[y * nhp + k];
-        ob[i] = SB[y * nhp + k];
+        oa[i] = SA[pskew(y) * nhp + k];
+        ob[i] = SB[pskew(y) * nhp + k];
     }
 }
 
@@ -302,16 +309,16 @@ __device__ __forceinline__ void plane_inv_body(const PlaneArgs<T>& a, int bid, u
     C2<T>* twz = reinterpret_cast<C2<T>*>(smem);
     C2<T>* twy = twz + n;
     C2<T>* SA = twy + g.n1;
-    C2<T>* SB = SA + (size_t)g.n1 * nhp;
-    C2<T>* R = SB + (size_t)g.n1 * nhp + (size_t)warp * n;
+    C2<T>* SB = SA + (size_t)plane_rows(g.n1) * nhp;
+    C2<T>* R = SB + (size_t)plane_rows(g.n1) * nhp + (size_t)warp * plane_rows(n);
     for (int i = threadIdx.x; i < n; i += blockDim.x) twz[i] = a.twz[i];
     for (int i = threadIdx.x; i < g.n1; i += blockDim.x) twy[i] = a.twy[i];
     const C2<T>* ia = a.spec + (size_t)ca * g.Nh + (size_t)x * g.n1 * nh;
     const C2<T>* ib = a.spec + (size_t)(hasb ? cb : ca) * g.Nh + (size_t)x * g.n1 * nh;
     for (int i = threadIdx.x; i < g.n1 * nh; i += blockDim.x) {
         const int y = a.dnh.div(i), k = i - y * nh;
-        cp_async_elem<T>(SA + y * nhp + k, ia + i);
-        if (hasb) cp_async_elem<T>(SB + y * nhp + k, ib + i);
+        cp_async_elem<T>(SA + pskew(y) * nhp + k, ia + i);
+        if (hasb) cp_async_elem<T>(SB + pskew(y) * nhp + k, ib + i);
     }
     cp_async_wait_all();
     __syncthreads();
@@ -320,11 +327,11 @@ __device__ __forceinline__ void plane_inv_body(const PlaneArgs<T>& a, int bid, u
         const int kz = (c < nh) ? c : c - nh;
         C2<T> v[E];
 #pragma unroll
-        for (int q = 0; q < E; q++) v[q] = S[(lane + 32 * q) * nhp + kz];
+        for (int q = 0; q < E; q++) v[q] = S[pskew(lane + 32 * q) * nhp + kz];
         warp_fft<T, E, 1>(v, twy, lane);
         const int b = brev5(lane);
 #pragma unroll
-        for (int k2 = 0; k2 < E; k2++) S[(k2 + E * b) * nhp + kz] = v[k2];
+        for (int k2 = 0; k2 < E; k2++) S[pskew(k2 + E * b) * nhp + kz] = v[k2];
     }
     __syncthreads();
     const T ea = (T)a.dE9[ca], eb = hasb ? (T)a.dE9[cb] : (T)0;
@@ -343,20 +350,20 @@ __device__ __forceinline__ void plane_inv_body(const PlaneArgs<T>& a, int bid, u
         for (int q = 0; q < E; q++) {
             const int m = lane + 32 * q;
             const int mm = m < nh ? m : n - m;
-            const C2<T> u = SA[y * nhp + mm];
-            const C2<T> w = hasb ? SB[y * nhp + mm] : mk<T>((T)0, (T)0);
+            const C2<T> u = SA[pskew(y) * nhp + mm];
+            const C2<T> w = hasb ? SB[pskew(y) * nhp + mm] : mk<T>((T)0, (T)0);
             if (m < nh) v[q] = mk<T>(u.x - w.y, u.y + w.x);   // u + i w
             else v[q] = mk<T>(u.x + w.y, -u.y + w.x);         // conj u + i conj w
         }
         warp_fft<T, E, 1>(v, twz, lane);
         const int b = brev5(lane);
 #pragma unroll
-        for (int k2 = 0; k2 < E; k2++) R[k2 + E * b] = v[k2];
+        for (int k2 = 0; k2 < E; k2++) R[pskew(k2 + E * b)] = v[k2];
         __syncwarp();
 #pragma unroll
         for (int q = 0; q < E; q++) {
             const int m = lane + 32 * q;
-            const C2<T> z = R[m];
+            const C2<T> z = R[pskew(m)];
             da[m] = pa[q] + (ea + z.x * a.invN);
             if (hasb) db[m] = pb[q] + (eb + z.y * a.invN);
         }
@@ -543,7 +550,7 @@ int plane_epl(const Grid& g, size_t elem) {
     const int E = g.n2 / 32;
     if (E * 32 != g.n2 || (E != 1 && E != 2 && E != 4)) return 0;
     const int nhp = g.nh | 1;
-    const size_t sm = (size_t)(g.n2 + g.n1 + 2 * g.n1 * nhp + PLANE_WARPS * g.n2) * elem;
+    const size_t sm = (size_t)(g.n2 + g.n1 + 2 * plane_rows(g.n1) * nhp + PLANE_WARPS * plane_rows(g.n2)) * elem;
     return sm <= PLANE_SMEM_MAX ? E : 0;
 }
 
@@ -602,7 +609,7 @@ static void fill_spec_t(Ctx& c, SpecSet<T>& s, const int P[3], const FftPlan pl[
     pa.dnh.set(g.nh);
     s.grid_pf = 3 * g.n0;
     s.grid_pi = 5 * g.n0;
-    s.sm_p = (size_t)(g.n2 + g.n1 + 2 * g.n1 * pa.nhp + PLANE_WARPS * g.n2) * es;
+    s.sm_p = (size_t)(g.n2 + g.n1 + 2 * plane_rows(g.n1) * pa.nhp + PLANE_WARPS * plane_rows(g.n2)) * es;
 }
 
 template <typename T>
