@@ -81,11 +81,17 @@ __device__ __forceinline__ C2<T> twid(const C2<T>* tw, int t) {
     return SIGN < 0 ? w : mk<T>(w.x, -w.y);
 }
 
+// Position of element p of a pencil in shared memory: with SKEW, p + p/16,
+// which spreads the strided butterfly writes of the early Stockham stages
+// over the banks (the pencil stride must then be at least n + n/16).
+template <bool SKEW> __device__ __forceinline__ int fsk(int p) { return SKEW ? p + (p >> 4) : p; }
+__host__ __device__ constexpr int skewed_len(int n) { return n + n / 16; }
+
 // Run every stage of `pl` on npen pencils held in `a` (pencil p starts at
-// element p*ps, ps >= n; scratch `b` has the same layout). Returns the buffer
-// holding the result. Must be called by all threads of the CTA; ends with a
-// __syncthreads.
-template <typename T, int SIGN>
+// element p*ps, ps >= n, or >= n + n/16 with SKEW; scratch `b` has the same
+// layout). Returns the buffer holding the result. Must be called by all
+// threads of the CTA; ends with a __syncthreads.
+template <typename T, int SIGN, bool SKEW = false>
 __device__ C2<T>* fft_batch(C2<T>* a, C2<T>* b, int npen, int ps, const FftPlan& pl,
                             const C2<T>* tw) {
     const int n = pl.n;
@@ -98,61 +104,62 @@ __device__ C2<T>* fft_batch(C2<T>* a, C2<T>* b, int npen, int ps, const FftPlan&
         for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
             const int pen = dm.div(idx), j = idx - pen * m;
             const int jq = dns.div(j), jm = j - jq * Ns;
-            const C2<T>* src = in + pen * ps + j;
-            C2<T>* dst = out + pen * ps + jq * Ns * r + jm;
+            const C2<T>* src = in + pen * ps;
+            C2<T>* dst = out + pen * ps;
+            const int d0 = jq * Ns * r + jm;
             C2<T> v[8];
             if (r == 8) {
 #pragma unroll
                 for (int q = 0; q < 8; q++) {
-                    v[q] = src[q * m];
+                    v[q] = src[fsk<SKEW>(j + q * m)];
                     if (q) v[q] = cmul<T>(v[q], twid<T, SIGN>(tw, q * jm * tws));
                 }
                 dft8<T, SIGN>(v);
 #pragma unroll
-                for (int q = 0; q < 8; q++) dst[q * Ns] = v[q];
+                for (int q = 0; q < 8; q++) dst[fsk<SKEW>(d0 + q * Ns)] = v[q];
             } else if (r == 4) {
 #pragma unroll
                 for (int q = 0; q < 4; q++) {
-                    v[q] = src[q * m];
+                    v[q] = src[fsk<SKEW>(j + q * m)];
                     if (q) v[q] = cmul<T>(v[q], twid<T, SIGN>(tw, q * jm * tws));
                 }
                 dft4<T, SIGN>(v[0], v[1], v[2], v[3]);
 #pragma unroll
-                for (int q = 0; q < 4; q++) dst[q * Ns] = v[q];
+                for (int q = 0; q < 4; q++) dst[fsk<SKEW>(d0 + q * Ns)] = v[q];
             } else if (r == 2) {
-                v[0] = src[0];
-                v[1] = cmul<T>(src[m], twid<T, SIGN>(tw, jm * tws));
-                dst[0] = cadd<T>(v[0], v[1]);
-                dst[Ns] = csub<T>(v[0], v[1]);
+                v[0] = src[fsk<SKEW>(j)];
+                v[1] = cmul<T>(src[fsk<SKEW>(j + m)], twid<T, SIGN>(tw, jm * tws));
+                dst[fsk<SKEW>(d0)] = cadd<T>(v[0], v[1]);
+                dst[fsk<SKEW>(d0 + Ns)] = csub<T>(v[0], v[1]);
             } else if (r == 3) {
 #pragma unroll
                 for (int q = 0; q < 3; q++) {
-                    v[q] = src[q * m];
+                    v[q] = src[fsk<SKEW>(j + q * m)];
                     if (q) v[q] = cmul<T>(v[q], twid<T, SIGN>(tw, q * jm * tws));
                 }
                 dft3<T, SIGN>(v);
 #pragma unroll
-                for (int q = 0; q < 3; q++) dst[q * Ns] = v[q];
+                for (int q = 0; q < 3; q++) dst[fsk<SKEW>(d0 + q * Ns)] = v[q];
             } else if (r == 5) {
 #pragma unroll
                 for (int q = 0; q < 5; q++) {
-                    v[q] = src[q * m];
+                    v[q] = src[fsk<SKEW>(j + q * m)];
                     if (q) v[q] = cmul<T>(v[q], twid<T, SIGN>(tw, q * jm * tws));
                 }
                 dft5<T, SIGN>(v);
 #pragma unroll
-                for (int q = 0; q < 5; q++) dst[q * Ns] = v[q];
+                for (int q = 0; q < 5; q++) dst[fsk<SKEW>(d0 + q * Ns)] = v[q];
             } else {
                 // generic prime radix: O(r^2) with the table (W_r^k = W_n^{k n/r})
                 const int step = n / r;
                 for (int q = 0; q < r; q++) {
                     C2<T> acc = mk<T>((T)0, (T)0);
                     for (int p = 0; p < r; p++) {
-                        C2<T> x = src[p * m];
+                        C2<T> x = src[fsk<SKEW>(j + p * m)];
                         if (p) x = cmul<T>(x, twid<T, SIGN>(tw, p * jm * tws));
                         acc = cadd<T>(acc, cmul<T>(x, twid<T, SIGN>(tw, ((p * q) % r) * step)));
                     }
-                    dst[q * Ns] = acc;
+                    dst[fsk<SKEW>(d0 + q * Ns)] = acc;
                 }
             }
         }

@@ -89,11 +89,19 @@ __device__ __forceinline__ void y_body(const YArgs<T>& a, int bid, unsigned char
 }
 
 // Forward x, Green contraction, inverse x on pencils (y, kz..kz+P).
+// Shared-memory layout of the X pass: FP32 pencils are skewed (fsk), which
+// removes the bank conflicts of the early Stockham stages; FP64 pencils, whose
+// pass is bound by the FP64 pipe, keep the plain layout and its smaller
+// footprint. Pencil stride (odd) for element size es of a complex value.
+__host__ __device__ constexpr bool x_skew(size_t es) { return es == 8; }
+__host__ __device__ constexpr int x_pencil_stride(int n, size_t es) { return x_skew(es) ? skewed_len(n) | 1 : n + 1; }
+
 template <typename T, bool SHARED_C0>
 __device__ __forceinline__ void x_green_body(const XArgs<T>& a, const GreenK<T>& gk, int bid,
                                              unsigned char* smem) {
     const Grid& g = a.g;
-    const int n = g.n0, ps = n + 1, P = a.P, nh = g.nh;
+    constexpr bool SK = x_skew(sizeof(C2<T>));
+    const int n = g.n0, ps = x_pencil_stride(n, sizeof(C2<T>)), P = a.P, nh = g.nh;
     C2<T>* tw = reinterpret_cast<C2<T>*>(smem);
     C2<T>* bA = tw + n;
     C2<T>* bB = bA + 9 * P * ps;
@@ -106,17 +114,17 @@ __device__ __forceinline__ void x_green_body(const XArgs<T>& a, const GreenK<T>&
     load_tw<T>(tw, a.tw, n);
     for (int i = threadIdx.x; i < 6 * n * np; i += blockDim.x) {
         const int c = dnq.div(i), rem = i - c * n * np, x = dq.div(rem), kk = rem - x * np;
-        cp_async_elem<T>(bA + (c * np + kk) * ps + x, a.spec + (size_t)c * g.Nh + x * xs + (size_t)y * nh + kz0 + kk);
+        cp_async_elem<T>(bA + (c * np + kk) * ps + fsk<SK>(x), a.spec + (size_t)c * g.Nh + x * xs + (size_t)y * nh + kz0 + kk);
     }
     cp_async_wait_all();
     __syncthreads();
-    C2<T>* R = fft_batch<T, -1>(bA, bB, 6 * np, ps, a.pl, tw);
+    C2<T>* R = fft_batch<T, -1, SK>(bA, bB, 6 * np, ps, a.pl, tw);
     C2<T>* W = (R == bA) ? bB : bA;
     for (int i = threadIdx.x; i < n * np; i += blockDim.x) {
         const int kk = a.dn.div(i), kx = i - kk * n, kz = kz0 + kk, ky = y;
         C2<T> sb[6], du[9];
 #pragma unroll
-        for (int c = 0; c < 6; c++) sb[c] = R[(c * np + kk) * ps + kx];
+        for (int c = 0; c < 6; c++) sb[c] = R[(c * np + kk) * ps + fsk<SK>(kx)];
         if ((kx | ky | kz) == 0) {
             green_k0<T>(gk.s0, gk.elast_bc, sb, du);
         } else {
@@ -142,13 +150,13 @@ __device__ __forceinline__ void x_green_body(const XArgs<T>& a, const GreenK<T>&
             }
         }
 #pragma unroll
-        for (int c = 0; c < 9; c++) W[(c * np + kk) * ps + kx] = du[c];
+        for (int c = 0; c < 9; c++) W[(c * np + kk) * ps + fsk<SK>(kx)] = du[c];
     }
     __syncthreads();
-    const C2<T>* R2 = fft_batch<T, 1>(W, (W == bA) ? bB : bA, 9 * np, ps, a.pl, tw);
+    const C2<T>* R2 = fft_batch<T, 1, SK>(W, (W == bA) ? bB : bA, 9 * np, ps, a.pl, tw);
     for (int i = threadIdx.x; i < 9 * n * np; i += blockDim.x) {
         const int c = dnq.div(i), rem = i - c * n * np, x = dq.div(rem), kk = rem - x * np;
-        a.spec[(size_t)c * g.Nh + x * xs + (size_t)y * nh + kz0 + kk] = R2[(c * np + kk) * ps + x];
+        a.spec[(size_t)c * g.Nh + x * xs + (size_t)y * nh + kz0 + kk] = R2[(c * np + kk) * ps + fsk<SK>(x)];
     }
 }
 
@@ -521,7 +529,7 @@ void spec_pmax(const Grid& g, size_t es, int pmax[3]) {
     if (pmax[0] < 1) pmax[0] = 1;
     pmax[1] = pick_p(2 * (g.n1 + 1), es, SPEC_BUDGET);
     if (pmax[1] > g.nh) pmax[1] = g.nh;
-    pmax[2] = pick_p(18 * (g.n0 + 1), es, SPEC_BUDGET_X);
+    pmax[2] = pick_p(18 * x_pencil_stride(g.n0, es), es, SPEC_BUDGET_X);
     if (pmax[2] > g.nh) pmax[2] = g.nh;
 }
 
@@ -601,7 +609,7 @@ static void fill_spec_t(Ctx& c, SpecSet<T>& s, const int P[3], const FftPlan pl[
     xa.gk.rn[2] = (T)(1.0 / g.n2);
     set_x_divisors<T>(xa);
     s.grid_x = g.n1 * ((g.nh + xa.P - 1) / xa.P);
-    s.sm_x = (size_t)(g.n0 + 18 * xa.P * (g.n0 + 1)) * es;
+    s.sm_x = (size_t)(g.n0 + 18 * xa.P * x_pencil_stride(g.n0, es)) * es;
     s.epl = fused ? plane_epl(g, es) : 0;
     PlaneArgs<T>& pa = s.pl;
     pa.g = g; pa.macro = c.macro; pa.gate = GATE_RUNNING; pa.sig = sig; pa.dg = dg; pa.spec = spec;
@@ -1125,7 +1133,7 @@ extern "C" int evpg_green_correction_noalloc(const double* sig6, double* du9, in
     const int ntile_y = (g.nh + ya.P - 1) / ya.P;
     XArgs<double> xa;
     xa.g = g; xa.pl = pl[0]; xa.macro = nullptr; xa.gate = GATE_ALWAYS; xa.spec = spec; xa.tw = twp[0];
-    xa.P = pick_p(18 * (n0 + 1), es, 150 * 1024);
+    xa.P = pick_p(18 * x_pencil_stride(n0, es), es, 150 * 1024);
     if (xa.P > g.nh) xa.P = g.nh;
     for (int i = 0; i < 81; i++) {
         (&xa.gk.c0[0][0][0][0])[i] = c0[i];
@@ -1136,7 +1144,7 @@ extern "C" int evpg_green_correction_noalloc(const double* sig6, double* du9, in
     xa.gk.rn[1] = 1.0 / n1;
     xa.gk.rn[2] = 1.0 / n2;
     set_x_divisors<double>(xa);
-    const size_t smx = (size_t)(n0 + 18 * xa.P * (n0 + 1)) * es;
+    const size_t smx = (size_t)(n0 + 18 * xa.P * x_pencil_stride(n0, es)) * es;
     const int ntile_x = (g.nh + xa.P - 1) / xa.P;
     set_kernel_attributes();
     k_fwd_z<double><<<(ncol + za.P - 1) / za.P, SPEC_THREADS, sm, st>>>(za);
