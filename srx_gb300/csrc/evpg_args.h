@@ -60,6 +60,7 @@ template <typename T> struct ZArgs {
     const double* dE9;   // macro correction added in the inverse pass
     int P;
     T invN;
+    FastDiv dn, dnh;     // divisors n2 and nh of the copy loops
 };
 
 template <typename T> struct YArgs {
@@ -70,6 +71,7 @@ template <typename T> struct YArgs {
     C2<T>* spec;
     const C2<T>* tw;
     int ncomp, P;
+    FastDiv dnp[2];      // np of full tiles ([0], np = P) and of the last tile ([1])
 };
 
 template <typename T> struct XArgs {

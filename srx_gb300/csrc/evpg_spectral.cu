@@ -29,29 +29,42 @@ __device__ __forceinline__ void cp_async_wait_all() {
     asm volatile("cp.async.wait_group 0;\n" ::: "memory");
 }
 
+// Shared-memory layout of the Stockham passes: FP32 pencils are skewed (fsk),
+// which removes the bank conflicts of the early stages; FP64 pencils, whose
+// passes are bound by the FP64 pipe, keep the plain layout and its smaller
+// footprint. Pencil strides for element size es of a complex value: x and y
+// passes (odd), z passes.
+__host__ __device__ constexpr bool x_skew(size_t es) { return es == 8; }
+__host__ __device__ constexpr int x_pencil_stride(int n, size_t es) { return x_skew(es) ? skewed_len(n) | 1 : n + 1; }
+__host__ __device__ constexpr int z_pencil_stride(int n, size_t es) { return x_skew(es) ? skewed_len(n) | 1 : n; }
+
 // Forward z: three complex FFTs of (sig[2p] + i sig[2p+1]) per column, split
 // into the two half spectra. bid: CTA index within this RVE's grid.
 template <typename T>
 __device__ __forceinline__ void fwd_z_body(const ZArgs<T>& a, int bid, unsigned char* smem) {
     const Grid& g = a.g;
-    const int n = g.n2, nh = g.nh, P = a.P;
+    constexpr bool SK = x_skew(sizeof(C2<T>));
+    const int n = g.n2, nh = g.nh, P = a.P, ps = z_pencil_stride(n, sizeof(C2<T>));
     C2<T>* tw = reinterpret_cast<C2<T>*>(smem);
     C2<T>* bA = tw + n;
-    C2<T>* bB = bA + P * n;
+    C2<T>* bB = bA + P * ps;
     const int ncol = g.n0 * g.n1, c0 = bid * P, np = min(P, ncol - c0);
     load_tw<T>(tw, a.tw, n);
     for (int pair = 0; pair < 3; pair++) {
         const T* sa = a.sig + (size_t)(2 * pair) * g.N + (size_t)c0 * n;
         const T* sb = a.sig + (size_t)(2 * pair + 1) * g.N + (size_t)c0 * n;
-        for (int i = threadIdx.x; i < np * n; i += blockDim.x) bA[i] = mk<T>(sa[i], sb[i]);
+        for (int i = threadIdx.x; i < np * n; i += blockDim.x) {
+            const int col = a.dn.div(i), k = i - col * n;
+            bA[col * ps + fsk<SK>(k)] = mk<T>(sa[i], sb[i]);
+        }
         __syncthreads();
-        const C2<T>* r = fft_batch<T, -1>(bA, bB, np, n, a.pl, tw);
+        const C2<T>* r = fft_batch<T, -1, SK>(bA, bB, np, ps, a.pl, tw);
         C2<T>* oa = a.spec + (size_t)(2 * pair) * g.Nh + (size_t)c0 * nh;
         C2<T>* ob = a.spec + (size_t)(2 * pair + 1) * g.Nh + (size_t)c0 * nh;
         for (int i = threadIdx.x; i < np * nh; i += blockDim.x) {
-            const int col = i / nh, k = i - col * nh;
-            const C2<T> z = r[col * n + k];
-            const C2<T> w = r[col * n + (k == 0 ? 0 : n - k)];
+            const int col = a.dnh.div(i), k = i - col * nh;
+            const C2<T> z = r[col * ps + fsk<SK>(k)];
+            const C2<T> w = r[col * ps + fsk<SK>(k == 0 ? 0 : n - k)];
             // A = (Z(k) + conj Z(n-k))/2, B = (Z(k) - conj Z(n-k))/(2i)
             oa[i] = mk<T>((T)0.5 * (z.x + w.x), (T)0.5 * (z.y - w.y));
             ob[i] = mk<T>((T)0.5 * (z.y + w.y), (T)-0.5 * (z.x - w.x));
@@ -64,38 +77,33 @@ __device__ __forceinline__ void fwd_z_body(const ZArgs<T>& a, int bid, unsigned 
 template <typename T, int SIGN>
 __device__ __forceinline__ void y_body(const YArgs<T>& a, int bid, unsigned char* smem) {
     const Grid& g = a.g;
-    const int n = g.n1, ps = n + 1, P = a.P, nh = g.nh;
+    constexpr bool SK = x_skew(sizeof(C2<T>));
+    const int n = g.n1, ps = x_pencil_stride(n, sizeof(C2<T>)), P = a.P, nh = g.nh;
     C2<T>* tw = reinterpret_cast<C2<T>*>(smem);
     C2<T>* bA = tw + n;
     C2<T>* bB = bA + P * ps;
     const int ntile = (nh + P - 1) / P;
     const int x = bid / ntile, kz0 = (bid % ntile) * P, np = min(P, nh - kz0);
+    const FastDiv dq = a.dnp[np == P ? 0 : 1];
     load_tw<T>(tw, a.tw, n);
     for (int c = 0; c < a.ncomp; c++) {
         C2<T>* base = a.spec + (size_t)c * g.Nh + (size_t)x * n * nh + kz0;
         for (int i = threadIdx.x; i < n * np; i += blockDim.x) {
-            const int y = i / np, kk = i - y * np;
-            cp_async_elem<T>(bA + kk * ps + y, base + (size_t)y * nh + kk);
+            const int y = dq.div(i), kk = i - y * np;
+            cp_async_elem<T>(bA + kk * ps + fsk<SK>(y), base + (size_t)y * nh + kk);
         }
         cp_async_wait_all();
         __syncthreads();
-        const C2<T>* r = fft_batch<T, SIGN>(bA, bB, np, ps, a.pl, tw);
+        const C2<T>* r = fft_batch<T, SIGN, SK>(bA, bB, np, ps, a.pl, tw);
         for (int i = threadIdx.x; i < n * np; i += blockDim.x) {
-            const int y = i / np, kk = i - y * np;
-            base[(size_t)y * nh + kk] = r[kk * ps + y];
+            const int y = dq.div(i), kk = i - y * np;
+            base[(size_t)y * nh + kk] = r[kk * ps + fsk<SK>(y)];
         }
         __syncthreads();
     }
 }
 
 // Forward x, Green contraction, inverse x on pencils (y, kz..kz+P).
-// Shared-memory layout of the X pass: FP32 pencils are skewed (fsk), which
-// removes the bank conflicts of the early Stockham stages; FP64 pencils, whose
-// pass is bound by the FP64 pipe, keep the plain layout and its smaller
-// footprint. Pencil stride (odd) for element size es of a complex value.
-__host__ __device__ constexpr bool x_skew(size_t es) { return es == 8; }
-__host__ __device__ constexpr int x_pencil_stride(int n, size_t es) { return x_skew(es) ? skewed_len(n) | 1 : n + 1; }
-
 template <typename T, bool SHARED_C0>
 __device__ __forceinline__ void x_green_body(const XArgs<T>& a, const GreenK<T>& gk, int bid,
                                              unsigned char* smem) {
@@ -169,10 +177,11 @@ constexpr int INVZ_EPT = 16;
 template <typename T>
 __device__ __forceinline__ void inv_z_body(const ZArgs<T>& a, int bid, unsigned char* smem) {
     const Grid& g = a.g;
-    const int n = g.n2, nh = g.nh, P = a.P;
+    constexpr bool SK = x_skew(sizeof(C2<T>));
+    const int n = g.n2, nh = g.nh, P = a.P, ps = z_pencil_stride(n, sizeof(C2<T>));
     C2<T>* tw = reinterpret_cast<C2<T>*>(smem);
     C2<T>* bA = tw + n;
-    C2<T>* bB = bA + P * n;
+    C2<T>* bB = bA + P * ps;
     const int ncol = g.n0 * g.n1, c0 = bid * P, np = min(P, ncol - c0);
     const int tot = np * n;
     load_tw<T>(tw, a.tw, n);
@@ -191,7 +200,7 @@ __device__ __forceinline__ void inv_z_body(const ZArgs<T>& a, int bid, unsigned 
         const C2<T>* sa = a.spec + (size_t)ca * g.Nh + (size_t)c0 * nh;
         const C2<T>* sb = a.spec + (size_t)(hasb ? cb : ca) * g.Nh + (size_t)c0 * nh;
         for (int i = threadIdx.x; i < tot; i += blockDim.x) {
-            const int col = i / n, k = i - col * n;
+            const int col = a.dn.div(i), k = i - col * n;
             C2<T> z;
             if (k < nh) {
                 const C2<T> u = sa[col * nh + k];
@@ -202,16 +211,17 @@ __device__ __forceinline__ void inv_z_body(const ZArgs<T>& a, int bid, unsigned 
                 const C2<T> v = hasb ? sb[col * nh + (n - k)] : mk<T>((T)0, (T)0);
                 z = mk<T>(u.x + v.y, -u.y + v.x);  // conj u + i conj v
             }
-            bA[i] = z;
+            bA[col * ps + fsk<SK>(k)] = z;
         }
         __syncthreads();
-        const C2<T>* r = fft_batch<T, 1>(bA, bB, np, n, a.pl, tw);
+        const C2<T>* r = fft_batch<T, 1, SK>(bA, bB, np, ps, a.pl, tw);
         const T ea = (T)a.dE9[ca], eb = hasb ? (T)a.dE9[cb] : (T)0;
 #pragma unroll
         for (int e = 0; e < INVZ_EPT; e++) {
             const int i = threadIdx.x + e * blockDim.x;
             if (i < tot) {
-                const C2<T> z = r[i];
+                const int col = a.dn.div(i), k = i - col * n;
+                const C2<T> z = r[col * ps + fsk<SK>(k)];
                 da[i] = pa[e] + (ea + z.x * a.invN);
                 if (hasb) db[i] = pb[e] + (eb + z.y * a.invN);
             }
@@ -524,10 +534,10 @@ constexpr size_t SPEC_BUDGET_X = 75 * 1024;
 // Largest pencil counts the shared-memory budgets and the register prefetch
 // of the inverse-z pass allow, per pass (z, y, x).
 void spec_pmax(const Grid& g, size_t es, int pmax[3]) {
-    pmax[0] = pick_p(2 * g.n2, es, SPEC_BUDGET);
+    pmax[0] = pick_p(2 * z_pencil_stride(g.n2, es), es, SPEC_BUDGET);
     if (pmax[0] * g.n2 > SPEC_THREADS * INVZ_EPT) pmax[0] = (SPEC_THREADS * INVZ_EPT) / g.n2;
     if (pmax[0] < 1) pmax[0] = 1;
-    pmax[1] = pick_p(2 * (g.n1 + 1), es, SPEC_BUDGET);
+    pmax[1] = pick_p(2 * x_pencil_stride(g.n1, es), es, SPEC_BUDGET);
     if (pmax[1] > g.nh) pmax[1] = g.nh;
     pmax[2] = pick_p(18 * x_pencil_stride(g.n0, es), es, SPEC_BUDGET_X);
     if (pmax[2] > g.nh) pmax[2] = g.nh;
@@ -562,6 +572,17 @@ int plane_epl(const Grid& g, size_t elem) {
     return sm <= PLANE_SMEM_MAX ? E : 0;
 }
 
+// Index divisors of the z and y passes.
+template <typename T> static void set_z_divisors(ZArgs<T>& za) {
+    za.dn.set(za.g.n2);
+    za.dnh.set(za.g.nh);
+}
+template <typename T> static void set_y_divisors(YArgs<T>& ya) {
+    const int last = ya.g.nh - ((ya.g.nh + ya.P - 1) / ya.P - 1) * ya.P;
+    ya.dnp[0].set(ya.P);
+    ya.dnp[1].set(last);
+}
+
 // Index divisors of the X pass for its grid and pencils per CTA.
 template <typename T> static void set_x_divisors(XArgs<T>& xa) {
     const Grid& g = xa.g;
@@ -586,15 +607,17 @@ static void fill_spec_t(Ctx& c, SpecSet<T>& s, const int P[3], const FftPlan pl[
     za.P = P[0];
     const int ncol = g.n0 * g.n1;
     s.grid_z = (ncol + za.P - 1) / za.P;
-    s.sm_z = (size_t)(g.n2 + 2 * za.P * g.n2) * es;
+    s.sm_z = (size_t)(g.n2 + 2 * za.P * z_pencil_stride(g.n2, es)) * es;
+    set_z_divisors<T>(za);
     YArgs<T>& ya = s.yf;
     ya.g = g; ya.pl = pl[1]; ya.macro = c.macro; ya.gate = GATE_RUNNING; ya.spec = spec; ya.tw = tw[1];
     ya.ncomp = 6;
     ya.P = P[1];
+    set_y_divisors<T>(ya);
     s.yi = ya;
     s.yi.ncomp = 9;
     s.grid_y = g.n0 * ((g.nh + ya.P - 1) / ya.P);
-    s.sm_y = (size_t)(g.n1 + 2 * ya.P * (g.n1 + 1)) * es;
+    s.sm_y = (size_t)(g.n1 + 2 * ya.P * x_pencil_stride(g.n1, es)) * es;
     XArgs<T>& xa = s.x;
     xa.g = g; xa.pl = pl[0]; xa.macro = c.macro; xa.gate = GATE_RUNNING; xa.spec = spec; xa.tw = tw[0];
     xa.P = P[2];
@@ -1121,15 +1144,17 @@ extern "C" int evpg_green_correction_noalloc(const double* sig6, double* du9, in
     ZArgs<double> za;
     za.g = g; za.pl = pl[2]; za.macro = nullptr; za.gate = GATE_ALWAYS; za.sig = sig6; za.dg = du9; za.spec = spec;
     za.tw = twp[2]; za.dE9 = zero9; za.invN = 1.0 / (double)g.N;
-    za.P = pick_p(2 * n2, es, budget);
+    za.P = pick_p(2 * z_pencil_stride(n2, es), es, budget);
     if (za.P * n2 > SPEC_THREADS * INVZ_EPT) za.P = (SPEC_THREADS * INVZ_EPT) / n2;
+    set_z_divisors<double>(za);
     const int ncol = n0 * n1;
-    const size_t sm = (size_t)(n2 + 2 * za.P * n2) * es;
+    const size_t sm = (size_t)(n2 + 2 * za.P * z_pencil_stride(n2, es)) * es;
     YArgs<double> ya;
     ya.g = g; ya.pl = pl[1]; ya.macro = nullptr; ya.gate = GATE_ALWAYS; ya.spec = spec; ya.tw = twp[1]; ya.ncomp = 6;
-    ya.P = pick_p(2 * (n1 + 1), es, budget);
+    ya.P = pick_p(2 * x_pencil_stride(n1, es), es, budget);
     if (ya.P > g.nh) ya.P = g.nh;
-    const size_t smy = (size_t)(n1 + 2 * ya.P * (n1 + 1)) * es;
+    set_y_divisors<double>(ya);
+    const size_t smy = (size_t)(n1 + 2 * ya.P * x_pencil_stride(n1, es)) * es;
     const int ntile_y = (g.nh + ya.P - 1) / ya.P;
     XArgs<double> xa;
     xa.g = g; xa.pl = pl[0]; xa.macro = nullptr; xa.gate = GATE_ALWAYS; xa.spec = spec; xa.tw = twp[0];
