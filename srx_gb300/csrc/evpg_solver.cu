@@ -769,6 +769,30 @@ struct AccF {
     __device__ __forceinline__ double value() const { return (double)h + (double)l; }
 };
 
+// Warp sums of NPART_NR accumulators by recursive halving (as warp_store):
+// on return lane 2k holds the warp total of value k in v[0].
+template <typename A>
+__device__ __forceinline__ A warp_halving(A (&v)[NPART_NR]) {
+    const int lane = threadIdx.x & 31;
+    A w[16];
+#pragma unroll
+    for (int k = 0; k < 16; k++) w[k] = k < NPART_NR ? v[k] : A::zero();
+#pragma unroll
+    for (int st = 0; st < 4; st++) {
+        const int h = 8 >> st, o = 16 >> st;
+        const bool up = (lane & o) != 0;
+#pragma unroll
+        for (int j = 0; j < h; j++) {
+            const A send = up ? w[j] : w[j + h];
+            A keep = up ? w[j + h] : w[j];
+            keep.add(send.shfl(o));
+            w[j] = keep;
+        }
+    }
+    w[0].add(w[0].shfl(1));
+    return w[0];
+}
+
 template <typename A>
 __device__ __forceinline__ void macro_body_t(const MacroArgs& a, int bid) {
     Macro* m = a.macro;
@@ -784,12 +808,9 @@ __device__ __forceinline__ void macro_body_t(const MacroArgs& a, int bid) {
 #pragma unroll
         for (int q = 0; q < NPART_NR; q++) v[q].add(A::load(a.part + (size_t)r * NPART_NR + q));
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-#pragma unroll
-    for (int q = 0; q < NPART_NR; q++) {
-        A x = v[q];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) x.add(x.shfl(o));
-        if (lane == 0) red[q][wid] = x;
+    {
+        const A x = warp_halving<A>(v);
+        if (!(lane & 1) && (lane >> 1) < NPART_NR) red[lane >> 1][wid] = x;
     }
     __syncthreads();
     if (threadIdx.x < NPART_NR) {
@@ -809,12 +830,9 @@ __device__ __forceinline__ void macro_body_t(const MacroArgs& a, int bid) {
 #pragma unroll
     for (int q = 0; q < NPART_NR; q++)
         v[q] = (int)threadIdx.x < nb ? A::load_cg(a.part2 + (size_t)threadIdx.x * NPART_NR + q) : A::zero();
-#pragma unroll
-    for (int q = 0; q < NPART_NR; q++) {
-        A x = v[q];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) x.add(x.shfl(o));
-        if (lane == 0) red[q][wid] = x;
+    {
+        const A x = warp_halving<A>(v);
+        if (!(lane & 1) && (lane >> 1) < NPART_NR) red[lane >> 1][wid] = x;
     }
     __syncthreads();
     if (threadIdx.x < NPART_NR) {

@@ -237,11 +237,13 @@ __device__ __forceinline__ void inv_z_body(const ZArgs<T>& a, int bid, unsigned 
 // two half spectra through a per-warp row buffer into the shared planes A and
 // B; then every warp takes kz columns of A and B and transforms them along y
 // in registers, in place; finally the planes are stored contiguously
-// (spec[c][x] is one n1*nh block). Inverse, CTA (x, pair p of the nine
-// components): load the planes, inverse along y in place, then per z row the
-// Hermitian pair is rebuilt, inverse-transformed in registers and added to
-// DisGrad (same update as the separate inverse-z pass). No intermediate
-// spectrum goes through global memory between the z and y transforms.
+// (spec[c][x] is one n1*nh block). Inverse, CTA (plane x, components 2p and
+// 2p+1, p < 4) or (component 8, planes 2j and 2j+1), so no CTA carries a
+// single component except an odd last plane: load the two half planes,
+// inverse along y in place, then per z row the Hermitian pair is rebuilt,
+// inverse-transformed in registers and added to DisGrad (same update as the
+// separate inverse-z pass). No intermediate spectrum goes through global
+// memory between the z and y transforms.
 
 // Shared-memory row skew of the plane kernels: row r is stored at r + r/16.
 // The warp FFTs scatter their outputs to rows k2 + E*brev5(lane), which
@@ -320,9 +322,23 @@ template <typename T, int E>
 __device__ __forceinline__ void plane_inv_body(const PlaneArgs<T>& a, int bid, unsigned char* smem) {
     const Grid& g = a.g;
     const int n = g.n2, nh = g.nh, nhp = a.nhp;
-    const int x = bid / 5, p = bid - 5 * x;
-    const int ca = 2 * p, cb = 2 * p + 1;
-    const bool hasb = cb < 9;
+    // CTAs b < 4 n0: plane b/4, components (2p, 2p+1) with p = b % 4; then
+    // component 8 of planes (2j, 2j+1), j = b - 4 n0 (one plane when 2j+1 == n0)
+    int xa, xb, ca, cb;
+    bool hasb;
+    if (bid < 4 * g.n0) {
+        xa = xb = bid >> 2;
+        ca = 2 * (bid & 3);
+        cb = ca + 1;
+        hasb = true;
+    } else {
+        const int j = bid - 4 * g.n0;
+        xa = 2 * j;
+        xb = 2 * j + 1;
+        ca = cb = 8;
+        hasb = xb < g.n0;
+        if (!hasb) xb = xa;
+    }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     C2<T>* twz = reinterpret_cast<C2<T>*>(smem);
     C2<T>* twy = twz + n;
@@ -331,8 +347,8 @@ __device__ __forceinline__ void plane_inv_body(const PlaneArgs<T>& a, int bid, u
     C2<T>* R = SB + (size_t)plane_rows(g.n1) * nhp + (size_t)warp * plane_rows(n);
     for (int i = threadIdx.x; i < n; i += blockDim.x) twz[i] = a.twz[i];
     for (int i = threadIdx.x; i < g.n1; i += blockDim.x) twy[i] = a.twy[i];
-    const C2<T>* ia = a.spec + (size_t)ca * g.Nh + (size_t)x * g.n1 * nh;
-    const C2<T>* ib = a.spec + (size_t)(hasb ? cb : ca) * g.Nh + (size_t)x * g.n1 * nh;
+    const C2<T>* ia = a.spec + (size_t)ca * g.Nh + (size_t)xa * g.n1 * nh;
+    const C2<T>* ib = a.spec + (size_t)cb * g.Nh + (size_t)xb * g.n1 * nh;
     for (int i = threadIdx.x; i < g.n1 * nh; i += blockDim.x) {
         const int y = a.dnh.div(i), k = i - y * nh;
         cp_async_elem<T>(SA + pskew(y) * nhp + k, ia + i);
@@ -354,8 +370,8 @@ __device__ __forceinline__ void plane_inv_body(const PlaneArgs<T>& a, int bid, u
     __syncthreads();
     const T ea = (T)a.dE9[ca], eb = hasb ? (T)a.dE9[cb] : (T)0;
     for (int y = warp; y < g.n1; y += PLANE_WARPS) {
-        T* da = a.dg + (size_t)ca * g.N + ((size_t)x * g.n1 + y) * n;
-        T* db = a.dg + (size_t)(hasb ? cb : ca) * g.N + ((size_t)x * g.n1 + y) * n;
+        T* da = a.dg + (size_t)ca * g.N + ((size_t)xa * g.n1 + y) * n;
+        T* db = a.dg + (size_t)cb * g.N + ((size_t)xb * g.n1 + y) * n;
         // DisGrad of this row, loaded before the transform hides its latency
         T pa[E], pb[E];
 #pragma unroll
@@ -639,7 +655,7 @@ static void fill_spec_t(Ctx& c, SpecSet<T>& s, const int P[3], const FftPlan pl[
     pa.twz = tw[2]; pa.twy = tw[1]; pa.dE9 = za.dE9; pa.invN = za.invN; pa.nhp = g.nh | 1;
     pa.dnh.set(g.nh);
     s.grid_pf = 3 * g.n0;
-    s.grid_pi = 5 * g.n0;
+    s.grid_pi = 4 * g.n0 + (g.n0 + 1) / 2;
     s.sm_p = (size_t)(g.n2 + g.n1 + 2 * plane_rows(g.n1) * pa.nhp + PLANE_WARPS * plane_rows(g.n2)) * es;
 }
 
