@@ -396,6 +396,7 @@ typedef struct evpg_server_cfg {
     int32_t round_ticks;   /* equilibrium iterations per round */
     int32_t loaders;       /* host threads opening requests */
     int32_t keep_fields;   /* keep each finished solve's stress, SSD density and scalars */
+    int32_t job_options;   /* evpg_job_open_opts options of every request (EVPG_JOB_GND) */
 } evpg_server_cfg;
 
 typedef struct evpg_request_info {

@@ -99,6 +99,8 @@ static void *loader_main(void *arg)
         pthread_mutex_unlock(&s->mu);
         st = evpg_job_grid(r->input, n);
         if (!st) st = evpg_estimate_bytes(n, s->cfg.precision, 0, &bytes);
+        /* GND densities: 24 doubles and one byte per voxel */
+        if (!st && (s->cfg.job_options & EVPG_JOB_GND)) bytes += 193LL * n[0] * n[1] * n[2];
         /* orientation rows and allocator granularity */
         bytes += bytes / 16 + (16 << 20);
         pthread_mutex_lock(&s->mu);
@@ -110,7 +112,8 @@ static void *loader_main(void *arg)
             r->bytes = bytes;
             r->state = RQ_LOADING;
             pthread_mutex_unlock(&s->mu);
-            st = evpg_job_open(r->input, r->rho0[0] ? r->rho0 : NULL, s->cfg.precision, s->cfg.nr_mode, &r->job);
+            st = evpg_job_open_opts(r->input, r->rho0[0] ? r->rho0 : NULL, s->cfg.precision, s->cfg.nr_mode,
+                                    s->cfg.job_options, &r->job);
             pthread_mutex_lock(&s->mu);
         }
         s->loading--;

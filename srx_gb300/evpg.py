@@ -249,7 +249,7 @@ class ServeStats(C.Structure):
 class ServerCfg(C.Structure):
     _fields_ = [("precision", C.c_int32), ("nr_mode", C.c_int32), ("hbm_budget", C.c_int64),
                 ("max_slots", C.c_int32), ("round_ticks", C.c_int32), ("loaders", C.c_int32),
-                ("keep_fields", C.c_int32)]
+                ("keep_fields", C.c_int32), ("job_options", C.c_int32)]
 
 
 class Server:
@@ -257,7 +257,7 @@ class Server:
 
     def __init__(self, precision: int = FP32_BULK, nr_mode: int = NR_LINESEARCH,
                  hbm_budget: int = 64 << 30, max_slots: int = 64, round_ticks: int = 16,
-                 loaders: int = 4, keep_fields: bool = False):
+                 loaders: int = 4, keep_fields: bool = False, gnd: bool = False):
         L = lib()
         vp = C.c_void_p
         L.evpg_server_create.argtypes = [C.POINTER(ServerCfg), C.POINTER(vp)]
@@ -270,7 +270,7 @@ class Server:
                                          C.c_size_t, C.POINTER(C.c_double)]
         L.evpg_server_destroy.argtypes = [vp]
         cfg = ServerCfg(precision, nr_mode, hbm_budget, max_slots, round_ticks, loaders,
-                        1 if keep_fields else 0)
+                        1 if keep_fields else 0, JOB_GND if gnd else 0)
         h = C.c_void_p()
         check(L.evpg_server_create(C.byref(cfg), C.byref(h)))
         self._h = h

@@ -132,3 +132,30 @@ def test_failing_request_fails_alone(tmp_path):
             assert srv.request(rid).state == 4
             gs, gr, gsc = srv.result(rid, c["N"])
             assert np.array_equal(gs, sig) and np.array_equal(gr, rho) and np.array_equal(gsc, sc)
+
+
+def test_served_gnd_requests_equal_alone(tmp_path):
+    """A server opened with GND densities (job option of every request):
+    four-increment solves in the mix give the same bits as each alone."""
+    from srx_gb300 import rve
+    evpg = _evpg()
+    reqs = []
+    for i, (n, load) in enumerate((((12, 12, 12), "tension"), ((16, 12, 8), "compression"))):
+        job = rve.Job(n=n, load=load, rate=1e-3, strain_per_step=2e-4, n_steps=4)
+        c = rve.make_case(str(tmp_path / ("g%d" % i)), n, 5, 300 + i, job, rho0=(0.5, 5.0))
+        c["N"] = int(np.prod(n))
+        reqs.append(c)
+    ref = []
+    for c in reqs:
+        with evpg.Job(c["input"], c["rho0"], precision=1, nr_mode=1, gnd=True) as j:
+            for k in range(4):
+                j.increment(k)
+            ref.append((j.download(evpg.F_SIG6), j.download(evpg.F_RHO_S), j.scalars()))
+    with evpg.Server(precision=1, nr_mode=1, max_slots=2, round_ticks=17, keep_fields=True,
+                     gnd=True) as srv:
+        ids = [srv.submit(c["input"], 4, rho0=c["rho0"]) for c in reqs]
+        srv.wait(600)
+        for rid, c, (sig, rho, sc) in zip(ids, reqs, ref):
+            assert srv.request(rid).state == 4
+            gs, gr, gsc = srv.result(rid, c["N"])
+            assert np.array_equal(gs, sig) and np.array_equal(gr, rho) and np.array_equal(gsc, sc)
