@@ -963,18 +963,20 @@ __device__ __forceinline__ void begin_body(const BeginArgs& a, int bid) {
 #pragma unroll
         for (int j = 0; j < 3; j++) R[i][j] = a.tranmat[(size_t)(3 * i + j) * N + v];
     for (int s = 0; s < P.n_sys; s++) {
-        double x5[6] = {P.schm_xt[s][0], P.schm_xt[s][1], P.schm_xt[s][2], P.schm_xt[s][3],
-                        P.schm_xt[s][4], 0.0};
-        double t[3][3], u[3][3], w[3][3];
-        b6_to_sym<double>(x5, t);
+        // R sym(n (x) b) R^T = sym(Rn (x) Rb): the rotated Schmid tensor from the
+        // rotated slip normal and direction (kinematics.c:430-463 rotates the
+        // tensor of Schm_xt, which is sym(n (x) b), init.c:205-212)
+        double bs[3], ns[3], w[3][3];
 #pragma unroll
-        for (int i = 0; i < 3; i++)
+        for (int i = 0; i < 3; i++) {
+            bs[i] = R[i][0] * P.bb[s][0] + R[i][1] * P.bb[s][1] + R[i][2] * P.bb[s][2];
+            ns[i] = R[i][0] * P.bn[s][0] + R[i][1] * P.bn[s][1] + R[i][2] * P.bn[s][2];
+        }
 #pragma unroll
-            for (int j = 0; j < 3; j++) u[i][j] = R[i][0] * t[0][j] + R[i][1] * t[1][j] + R[i][2] * t[2][j];
-#pragma unroll
-        for (int i = 0; i < 3; i++)
-#pragma unroll
-            for (int j = 0; j < 3; j++) w[i][j] = u[i][0] * R[j][0] + u[i][1] * R[j][1] + u[i][2] * R[j][2];
+        for (int i = 0; i < 3; i++) w[i][i] = ns[i] * bs[i];
+        w[1][2] = w[2][1] = 0.5 * (ns[1] * bs[2] + ns[2] * bs[1]);
+        w[0][2] = w[2][0] = 0.5 * (ns[0] * bs[2] + ns[2] * bs[0]);
+        w[0][1] = w[1][0] = 0.5 * (ns[0] * bs[1] + ns[1] * bs[0]);
         double o6[6];
         sym_to_b6<double>(w, o6);
 #pragma unroll
