@@ -116,6 +116,9 @@ static void fill_material(const evpg_rve_desc* d, Material<T>& m) {
             k.k_ddip[i] = (T)(sqrt(3.0) * s.shear_g * b / 16.0 / 3.14159265359 / (1 - d->nu));
             k.k_hyd[i] = (T)(s.shear_g * b / 3.14159265359 / (1 - d->nu));
             k.k_d0b[i] = (T)(d->d0 / b);
+            k.k_hydr[i] = (T)((s.shear_g * b / 3.14159265359 / (1 - d->nu)) /
+                              (sqrt(3.0) * s.shear_g * b / 16.0 / 3.14159265359 / (1 - d->nu)));
+            k.k_hexp[i] = (T)(b * b * b * 100 / (1.38 * d->temperature));
             for (int q = 0; q < 5; q++) k.schm_xt[i][q] = (T)s.schm_xt[i][q];
             for (int q = 0; q < 3; q++) {
                 k.bn[i][q] = (T)s.bn[i][q];

@@ -68,11 +68,16 @@ template <typename T> struct PhaseK {
     T k_tcut[NS];    // (kT/0.624)/c2/c3/b/b*0.1 -> tau_cut = k*sqrt(rho_f)
     T k_rhom[NS];    // 2kT/c1/c2/c3/G/b^3*160.2177 -> rho_m = k*sqrt(rho_P*rho_f)
     T k_gamo[NS];    // 1e-3*1e10*c2*b*exp(-q_slip) -> gam_o = k*rho_m/sqrt(rho_f)
-    // DislocationEvolution prefixes (constitutive.c:1401-1403, evaluated left to
-    // right as there): d_dipole = k_ddip/(|rss|+1e-4), hydro = k_hyd/d_dipole
+    // DislocationEvolution prefixes (constitutive.c:1401-1403): d_dipole =
+    // k_ddip/(|rss|+1e-4) (left to right as there)
     T k_ddip[NS];    // sqrt(3)*G*b/16/pi/(1-nu)
     T k_hyd[NS];     // G*b/pi/(1-nu)
     T k_d0b[NS];     // D_0/b
+    // one division per system instead of three: hydro = k_hydr (|rss| + 1e-4)
+    // with k_hydr = k_hyd / k_ddip, and the exponent |hydro| k_hexp with
+    // k_hexp = b^3 100 / (1.38 T)
+    T k_hydr[NS];
+    T k_hexp[NS];
     T tau0;
     T schm_xt[NS][5];
     T bn[NS][3], bb[NS][3];

@@ -1195,17 +1195,17 @@ __device__ __forceinline__ void end_body(const EndArgs& a, int bid) {
             double s6[6];
 #pragma unroll
             for (int c = 0; c < 6; c++) s6[c] = a.sig64[(size_t)c * N + v];
-            const double T = a.mat.temperature;
             const double eqb = exp(-1.0 * P.q_bulk);
             for (int i = 0; i < P.n_sys; i++) {
                 const double* sc = a.schm64 + (size_t)(i * 5) * N + v;
                 const double rss = sc[0] * s6[0] + sc[(size_t)N] * s6[1] + sc[2 * (size_t)N] * s6[2] +
                                    sc[3 * (size_t)N] * s6[3] + sc[4 * (size_t)N] * s6[4];
                 const double b = P.burgers[i];
-                const double ddip = P.k_ddip[i] / (fabs(rss) + 1.0E-4);
-                const double hyd = P.k_hyd[i] / ddip;
+                const double den = fabs(rss) + 1.0E-4;
+                const double ddip = P.k_ddip[i] / den;
+                const double hyd = P.k_hydr[i] * den;  // k_hyd / ddip
                 const double clim = 1E-17 * rtot * 0.5 * 1E24 * ddip * P.k_d0b[i] * (rs[i] * rs[i]) *
-                                    (exp(fabs(hyd) * b * b * b * 100 / (1.38 * T)) - 1.0) * eqb;
+                                    (exp(fabs(hyd) * P.k_hexp[i]) - 1.0) * eqb;
                 const double ag = fabs(gd[i]);
                 const double sq = sqrt(rf[i]);
                 q[4] += clim * dt;
