@@ -841,6 +841,36 @@ int evpg_set_fused(void* ctx, int32_t mode) {
     return EVPG_OK;
 }
 
+int evpg_set_radix(void* ctx, int32_t axis, const int32_t* radix, int32_t nstages) {
+    Ctx* c = (Ctx*)ctx;
+    if (!c || axis < 0 || axis > 2 || !radix || nstages < 1 || nstages > 12)
+        return fail(EVPG_ERR_ARG, "bad argument");
+    long long prod = 1;
+    for (int s = 0; s < nstages; s++) {
+        const int r = radix[s];
+        // radix 16 runs in the FP32 transforms only
+        if (r < 2 || (r == 16 && c->precision == EVPG_FP64)) return fail(EVPG_ERR_ARG, "radix %d", r);
+        prod *= r;
+    }
+    const int n = axis == 0 ? c->g.n0 : axis == 1 ? c->g.n1 : c->g.n2;
+    if (prod != n) return fail(EVPG_ERR_ARG, "radices do not multiply to %d", n);
+    CK(cudaStreamSynchronize(c->stream));
+    FftPlan& p = c->pl[axis];
+    memset(&p, 0, sizeof p);
+    p.n = n;
+    p.nf = nstages;
+    int ns = 1;
+    for (int s = 0; s < nstages; s++) {
+        p.radix[s] = radix[s];
+        p.ns[s] = ns;
+        ns *= radix[s];
+    }
+    plan_divisors(p);
+    build_sets(*c);
+    c->version++;
+    return EVPG_OK;
+}
+
 int evpg_get_schedule(void* ctx, int32_t pencils[3], int32_t radix[3][12], int32_t nstages[3]) {
     Ctx* c = (Ctx*)ctx;
     if (!c) return fail(EVPG_ERR_ARG, "null context");

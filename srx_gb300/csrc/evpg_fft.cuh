@@ -45,6 +45,40 @@ __device__ __forceinline__ void dft8(C2<T>* v) {
     v[3] = cadd<T>(e3, w3); v[7] = csub<T>(e3, w3);
 }
 
+// 16-point DFT as 4 x 4: inner DFT4 over q2 of v[q1 + 4 q2], twiddles
+// W16^(q1 k2), outer DFT4 over q1; output V[4 k1 + k2] in natural order.
+template <typename T, int SIGN>
+__device__ __forceinline__ void dft16(C2<T>* v) {
+    const T c1 = (T)0.92387953251128675613, s1 = (T)0.38268343236508977173;
+    const T h = (T)0.70710678118654752440, sg = (T)SIGN;
+#pragma unroll
+    for (int q1 = 0; q1 < 4; q1++) dft4<T, SIGN>(v[q1], v[q1 + 4], v[q1 + 8], v[q1 + 12]);
+    // v[q1 + 4 k2] now holds X[q1][k2]; multiply by W16^(q1 k2)
+    const C2<T> w1 = mk<T>(c1, sg * s1), w2 = mk<T>(h, sg * h), w3 = mk<T>(s1, sg * c1);
+    const C2<T> w6 = mk<T>(-h, sg * h), w9 = mk<T>(-c1, -sg * s1);
+    v[5] = cmul<T>(v[5], w1);
+    v[9] = cmul<T>(v[9], w2);
+    v[13] = cmul<T>(v[13], w3);
+    v[6] = cmul<T>(v[6], w2);
+    v[10] = mul_isign<T, SIGN>(v[10]);
+    v[14] = cmul<T>(v[14], w6);
+    v[7] = cmul<T>(v[7], w3);
+    v[11] = cmul<T>(v[11], w6);
+    v[15] = cmul<T>(v[15], w9);
+    C2<T> o[16];
+#pragma unroll
+    for (int k2 = 0; k2 < 4; k2++) {
+        C2<T> a0 = v[4 * k2], a1 = v[4 * k2 + 1], a2 = v[4 * k2 + 2], a3 = v[4 * k2 + 3];
+        dft4<T, SIGN>(a0, a1, a2, a3);
+        o[k2] = a0;
+        o[4 + k2] = a1;
+        o[8 + k2] = a2;
+        o[12 + k2] = a3;
+    }
+#pragma unroll
+    for (int k = 0; k < 16; k++) v[k] = o[k];
+}
+
 template <typename T, int SIGN>
 __device__ __forceinline__ void dft3(C2<T>* v) {
     const T s = (T)SIGN * (T)0.86602540378443864676;
@@ -107,8 +141,20 @@ __device__ C2<T>* fft_batch(C2<T>* a, C2<T>* b, int npen, int ps, const FftPlan&
             const C2<T>* src = in + pen * ps;
             C2<T>* dst = out + pen * ps;
             const int d0 = jq * Ns * r + jm;
-            C2<T> v[8];
-            if (r == 8) {
+            // radix 16 in FP32 only (the tuner offers it there): an FP64 buffer of
+            // 16 complex values would cost the FP64 kernels occupancy
+            constexpr bool R16 = sizeof(T) == 4;
+            C2<T> v[R16 ? 16 : 8];
+            if (R16 && r == 16) {
+#pragma unroll
+                for (int q = 0; q < 16; q++) {
+                    v[q] = src[fsk<SKEW>(j + q * m)];
+                    if (q) v[q] = cmul<T>(v[q], twid<T, SIGN>(tw, q * jm * tws));
+                }
+                dft16<T, SIGN>(v);
+#pragma unroll
+                for (int q = 0; q < 16; q++) dst[fsk<SKEW>(d0 + q * Ns)] = v[q];
+            } else if (r == 8) {
 #pragma unroll
                 for (int q = 0; q < 8; q++) {
                     v[q] = src[fsk<SKEW>(j + q * m)];

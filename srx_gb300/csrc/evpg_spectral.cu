@@ -853,10 +853,10 @@ static void plan_of(int n, const std::vector<int>& f, FftPlan& p) {
     plan_divisors(p);
 }
 
-// Factor orders of n: radices 8/4/2 for the power-of-two part (at most one
-// radix-2 stage), all distinct permutations, the odd factors after them or
-// before them.
-static std::vector<std::vector<int>> factor_orders(int n) {
+// Factor orders of n: radices 16 (with r16)/8/4/2 for the power-of-two part
+// (at most one radix-2 stage), all distinct permutations, the odd factors
+// after them or before them.
+static std::vector<std::vector<int>> factor_orders(int n, bool r16) {
     int m = n, k = 0;
     while (m % 2 == 0) { m /= 2; k++; }
     std::vector<int> odd;
@@ -865,25 +865,28 @@ static std::vector<std::vector<int>> factor_orders(int n) {
     for (int q = 7; m > 1; q += 2)
         while (m % q == 0) { odd.push_back(q); m /= q; }
     std::vector<std::vector<int>> out;
-    for (int n8 = k / 3; n8 >= 0; n8--)
-        for (int n2 = 0; n2 <= 1; n2++) {
-            const int rest = k - 3 * n8 - n2;
-            if (rest < 0 || rest % 2) continue;
-            std::vector<int> f;
-            for (int i = 0; i < n8; i++) f.push_back(8);
-            for (int i = 0; i < rest / 2; i++) f.push_back(4);
-            for (int i = 0; i < n2; i++) f.push_back(2);
-            std::sort(f.begin(), f.end());
-            do {
-                for (int front = 0; front < (odd.empty() ? 1 : 2); front++) {
-                    std::vector<int> g;
-                    if (front) g.insert(g.end(), odd.begin(), odd.end());
-                    g.insert(g.end(), f.begin(), f.end());
-                    if (!front) g.insert(g.end(), odd.begin(), odd.end());
-                    if (g.size() <= 12 && std::find(out.begin(), out.end(), g) == out.end()) out.push_back(g);
-                }
-            } while (std::next_permutation(f.begin(), f.end()) && out.size() < 48);
-        }
+    // power-of-two part 2^k as radices 16/8/4 with at most one radix-2 stage
+    for (int n16 = r16 ? k / 4 : 0; n16 >= 0; n16--)
+        for (int n8 = (k - 4 * n16) / 3; n8 >= 0; n8--)
+            for (int n2 = 0; n2 <= 1; n2++) {
+                const int rest = k - 4 * n16 - 3 * n8 - n2;
+                if (rest < 0 || rest % 2) continue;
+                std::vector<int> f;
+                for (int i = 0; i < n16; i++) f.push_back(16);
+                for (int i = 0; i < n8; i++) f.push_back(8);
+                for (int i = 0; i < rest / 2; i++) f.push_back(4);
+                for (int i = 0; i < n2; i++) f.push_back(2);
+                std::sort(f.begin(), f.end());
+                do {
+                    for (int front = 0; front < (odd.empty() ? 1 : 2); front++) {
+                        std::vector<int> g;
+                        if (front) g.insert(g.end(), odd.begin(), odd.end());
+                        g.insert(g.end(), f.begin(), f.end());
+                        if (!front) g.insert(g.end(), odd.begin(), odd.end());
+                        if (g.size() <= 12 && std::find(out.begin(), out.end(), g) == out.end()) out.push_back(g);
+                    }
+                } while (std::next_permutation(f.begin(), f.end()) && out.size() < 64);
+            }
     if (out.empty()) out.push_back(odd);
     return out;
 }
@@ -965,7 +968,7 @@ static int tune_t(Ctx& c, T* sig, const C2<T>* const* tw, int force, double* gai
         const int ax = axis_of_pass[pass];
         float best = time_pass<T>(c, pass, P, pl, sig, scratch, tw, e0, e1);
         if (pass == 2 || !fused_default) t0 += best;
-        for (const std::vector<int>& f : factor_orders(len_of_pass[pass])) {
+        for (const std::vector<int>& f : factor_orders(len_of_pass[pass], sizeof(T) == 4)) {
             FftPlan trial[3] = {pl[0], pl[1], pl[2]};
             plan_of(len_of_pass[pass], f, trial[ax]);
             const float t = time_pass<T>(c, pass, P, trial, sig, scratch, tw, e0, e1);

@@ -203,6 +203,13 @@ class Job:
         lib().evpg_set_fused.argtypes = [C.c_void_p, C.c_int32]
         check(lib().evpg_set_fused(self.ctx, mode))
 
+    def set_radix(self, axis: int, radices) -> None:
+        """FFT radix order of one axis (0 x, 1 y, 2 z) for the Stockham passes."""
+        L = lib()
+        L.evpg_set_radix.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.c_int32]
+        arr = (C.c_int32 * len(radices))(*radices)
+        check(L.evpg_set_radix(self.ctx, axis, arr, len(radices)))
+
     def schedule(self) -> dict:
         """Pencils per CTA (z, y, x passes) and radix stages (x, y, z axes)."""
         lib().evpg_get_schedule.argtypes = [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32),

@@ -256,3 +256,29 @@ def test_batch_with_gnd_slot_equals_alone(tmp_path, precision):
     finally:
         for j in jobs:
             j.close()
+
+
+def test_radix16_stages(tmp_path):
+    """Radix-16 Stockham stages (FP32) on all three axes, separate passes,
+    against the default radix orders: FP32-bulk results within the form's
+    tolerance."""
+    from conftest import rel_err
+    from srx_gb300 import rve
+    evpg = _evpg()
+    grid = (32, 64, 64)
+    job = rve.Job(n=grid, load="tension", rate=1e-3, strain_per_step=2e-4, n_steps=2)
+    c = rve.make_case(str(tmp_path / "c"), grid, 6, 33, job, rho0=(0.5, 5.0))
+    res = []
+    for orders in (None, ([16, 2], [16, 4], [4, 16])):
+        with evpg.Job(c["input"], c["rho0"], precision=1, nr_mode=1) as j:
+            j.set_fused(0)
+            if orders:
+                for ax, r in enumerate(orders):
+                    j.set_radix(ax, r)
+                assert [list(x) for x in j.schedule()["radix_xyz"]] == [list(o) for o in orders]
+            its = [j.increment(k) for k in range(2)]
+            res.append((its, j.download(evpg.F_SIG6), j.scalars()))
+    assert abs(sum(res[0][0]) - sum(res[1][0])) <= 2
+    assert rel_err(res[1][2][7:16], res[0][2][7:16]) < 1e-5
+    l2 = np.linalg.norm(res[1][1] - res[0][1]) / np.linalg.norm(res[0][1])
+    assert l2 < 1e-4, l2
