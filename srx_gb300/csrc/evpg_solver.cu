@@ -127,7 +127,8 @@ __device__ __forceinline__ T resolved_shear(const T* cs, const T* s, int i, T (&
 
 template <typename T>
 __device__ __forceinline__ void flow_eval(const NrArgs<T>& a, int nsys, int v, const T* cs,
-                                          const T* s, bool stale, T* ed, T* dd, T* gam, bool& bad) {
+                                          const T (&s)[6], bool stale, T (&ed)[5], T (&dd)[15], T* gam,
+                                          bool& bad) {
     const size_t N = a.g.N;
 #pragma unroll
     for (int q = 0; q < 5; q++) ed[q] = (T)0;
