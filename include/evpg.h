@@ -249,8 +249,9 @@ int evpg_set_nr_tolerance(void *ctx, double tol, int32_t itmax);
  * evpg_get_schedule then reports 0 pencils for the z and y passes. */
 int evpg_set_fused(void *ctx, int32_t mode);
 /* FFT radix order of one axis (0 x, 1 y, 2 z) for the Stockham passes:
- * nstages radices (2..16, product n of the axis; 16 in FP32 contexts only)
- * applied in the given order. The autotuner chooses among such orders. */
+ * nstages radices (2..16, product n of the axis; 16 in FP32 contexts on the
+ * x axis only) applied in the given order. The autotuner chooses among such
+ * orders. */
 int evpg_set_radix(void *ctx, int32_t axis, const int32_t *radix, int32_t nstages);
 /* Device bytes evpg_create allocates for an n[0] x n[1] x n[2] RVE with
  * n_orient distinct orientations (for admission by HBM footprint); GND

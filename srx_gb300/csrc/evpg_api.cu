@@ -848,8 +848,9 @@ int evpg_set_radix(void* ctx, int32_t axis, const int32_t* radix, int32_t nstage
     long long prod = 1;
     for (int s = 0; s < nstages; s++) {
         const int r = radix[s];
-        // radix 16 runs in the FP32 transforms only
-        if (r < 2 || (r == 16 && c->precision == EVPG_FP64)) return fail(EVPG_ERR_ARG, "radix %d", r);
+        // radix 16 runs in the FP32 x transforms only
+        if (r < 2 || (r == 16 && (c->precision == EVPG_FP64 || axis != 0)))
+            return fail(EVPG_ERR_ARG, "radix %d on axis %d", r, axis);
         prod *= r;
     }
     const int n = axis == 0 ? c->g.n0 : axis == 1 ? c->g.n1 : c->g.n2;

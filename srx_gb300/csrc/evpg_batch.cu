@@ -56,7 +56,26 @@ __global__ void __launch_bounds__(ADVANCE_THREADS) k_round_start(Macro* const* _
     __syncthreads();
     if (threadIdx.x == 0) {
         *tick = 0;
+        tick[2] = 0;
         cudaGraphSetConditional(h, (any && *kmax > 0) ? 1u : 0u);
+    }
+}
+
+// After the macro update of an iteration: the increment-tail section of the
+// iteration (an IF node: fold, FP64 refinement, tail, each gated per RVE)
+// runs only when some RVE's loop ended in this iteration; tick[2] counts the
+// iterations in which it ran.
+__global__ void __launch_bounds__(ADVANCE_THREADS) k_if_ending(Macro* const* __restrict__ ms, int n, int* tick,
+                                                               cudaGraphConditionalHandle h) {
+    __shared__ int any;
+    if (threadIdx.x == 0) any = 0;
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+        if (gate_open(ms[i], GATE_ENDING)) any = 1;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        if (any) tick[2] += 1;
+        cudaGraphSetConditional(h, any ? 1u : 0u);
     }
 }
 
@@ -93,14 +112,14 @@ struct Batch {
     void* dtab[BL_COUNT] = {};
     int2* dmap[BL_COUNT] = {};
     BatchLaunch L[BL_COUNT] = {};
-    int* dtk = nullptr;        // [0] tick, [1] kmax
+    int* dtk = nullptr;        // [0] tick, [1] kmax, [2] iterations that ran the tail section
     int* htk = nullptr;        // pinned mirror
     IncrCtl* hctl = nullptr;   // pinned, one per slot
     std::vector<char> staged;
     int cap = 0;               // capacity of hctl
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
-    int prologue_kernels = 0, body_kernels = 0;
+    int prologue_kernels = 0, body_kernels = 0, tail_kernels = 0;
     long long launches = 0;
     long long rounds = 0;
 };
@@ -311,8 +330,11 @@ static int build_graph(Batch& b) {
     cp.conditional.size = 1;
     BCK(cudaGraphAddNode(&wn, b.graph, deps.data(), nullptr, deps.size(), &cp));
     cudaGraph_t body = cp.conditional.phGraph_out[0];
+    cudaGraphConditionalHandle hif;
+    BCK(cudaGraphConditionalHandleCreate(&hif, b.graph, 0, cudaGraphCondAssignDefault));
+    // body: the equilibrium iteration of every running RVE ...
     BCK(cudaStreamBeginCaptureToGraph(b.stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-    int nb = 0;
+    int nb = 0, nt = 0;
     if (one) {
         cudaStream_t cs = c0->stream;
         c0->stream = b.stream;
@@ -321,21 +343,63 @@ static int build_graph(Batch& b) {
         launch_macro(*c0);
         const int fused = c0->precision ? c0->ks->s32.epl : c0->ks->s64.epl;
         nb = (fused ? 3 : 5) + 2;
-        if (c0->precision != 0) {
-            launch_fold(*c0, GATE_ENDING);
-            launch_nr(*c0, 1, GATE_ENDING);
-            nb += 2;
-        }
-        launch_end(*c0, GATE_ENDING);
-        nb += 2;
         c0->stream = cs;
     } else {
         nb = launch_spectral_batch(b.precision, b.L, b.stream) + 2;
         launch_nr_batch(b.precision, b.nr_mode, b.L[BL_NR], b.stream);
         launch_macro_batch(b.L[BL_MACRO], b.stream);
-        launch_end_batch(b.precision, b.nr_mode, b.L, b.stream);
-        nb += (b.precision != 0) ? 4 : 2;
     }
+    k_if_ending<<<1, ADVANCE_THREADS, 0, b.stream>>>(dm, n, b.dtk, hif);
+    nb++;
+    std::vector<cudaGraphNode_t> bdeps;
+    {
+        cudaStreamCaptureStatus cst;
+        const cudaGraphNode_t* d = nullptr;
+        size_t nd = 0;
+        cudaError_t ce = cudaStreamGetCaptureInfo(b.stream, &cst, nullptr, nullptr, &d, nullptr, &nd);
+        if (ce == cudaSuccess && d) bdeps.assign(d, d + nd);
+        cudaGraph_t g_out = nullptr;
+        cudaError_t ce2 = cudaStreamEndCapture(b.stream, &g_out);
+        if (ce != cudaSuccess || ce2 != cudaSuccess || bdeps.empty()) {
+            if (one) c0->launches = saved;
+            return bfail(EVPG_ERR_CUDA, "body capture: %s / %s", cudaGetErrorString(ce), cudaGetErrorString(ce2));
+        }
+    }
+    // ... then, only in iterations where some RVE's loop ended, its tail
+    // (each kernel still gated per RVE) ...
+    cudaGraphNode_t ifn;
+    cudaGraphNodeParams ip = {cudaGraphNodeTypeConditional};
+    ip.conditional.handle = hif;
+    ip.conditional.type = cudaGraphCondTypeIf;
+    ip.conditional.size = 1;
+    BCK(cudaGraphAddNode(&ifn, body, bdeps.data(), nullptr, bdeps.size(), &ip));
+    BCK(cudaStreamBeginCaptureToGraph(b.stream, ip.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                      cudaStreamCaptureModeThreadLocal));
+    if (one) {
+        cudaStream_t cs = c0->stream;
+        c0->stream = b.stream;
+        if (c0->precision != 0) {
+            launch_fold(*c0, GATE_ENDING);
+            launch_nr(*c0, 1, GATE_ENDING);
+            nt += 2;
+        }
+        launch_end(*c0, GATE_ENDING);
+        nt += 2;
+        c0->stream = cs;
+    } else {
+        launch_end_batch(b.precision, b.nr_mode, b.L, b.stream);
+        nt += (b.precision != 0) ? 4 : 2;
+    }
+    {
+        cudaGraph_t g_out = nullptr;
+        cudaError_t ce = cudaStreamEndCapture(b.stream, &g_out);
+        if (ce != cudaSuccess) {
+            if (one) c0->launches = saved;
+            return bfail(EVPG_ERR_CUDA, "tail capture: %s", cudaGetErrorString(ce));
+        }
+    }
+    // ... and the loop control
+    BCK(cudaStreamBeginCaptureToGraph(b.stream, body, &ifn, nullptr, 1, cudaStreamCaptureModeThreadLocal));
     k_advance<<<1, ADVANCE_THREADS, 0, b.stream>>>(dm, n, b.dtk, b.dtk + 1, h);
     nb++;
     cudaGraph_t body_out = nullptr;
@@ -345,6 +409,7 @@ static int build_graph(Batch& b) {
     BCK(cudaGraphInstantiate(&b.exec, b.graph, 0));
     b.prologue_kernels = np;
     b.body_kernels = nb;
+    b.tail_kernels = nt;
     return EVPG_OK;
 }
 
@@ -432,10 +497,10 @@ static int run_round(Batch& b, int kmax, int* ticks) {
     BCK(cudaGraphLaunch(b.exec, b.stream));
     for (Ctx* c : b.slots)
         BCK(cudaMemcpyAsync(c->macro_host, c->macro, sizeof(Macro), cudaMemcpyDeviceToHost, b.stream));
-    BCK(cudaMemcpyAsync(b.htk, b.dtk, sizeof(int), cudaMemcpyDeviceToHost, b.stream));
+    BCK(cudaMemcpyAsync(b.htk, b.dtk, 3 * sizeof(int), cudaMemcpyDeviceToHost, b.stream));
     BCK(cudaStreamSynchronize(b.stream));
     const int t = b.htk[0];
-    const long long nl = b.prologue_kernels + (long long)t * b.body_kernels;
+    const long long nl = b.prologue_kernels + (long long)t * b.body_kernels + (long long)b.htk[2] * b.tail_kernels;
     b.launches += nl;
     if (b.slots.size() == 1) b.slots[0]->launches += nl;
     b.rounds++;
@@ -466,14 +531,14 @@ static int create_batch(int precision, int nr_mode, cudaStream_t stream, Batch**
         e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
         b->own_stream = e == cudaSuccess;
     }
-    if (e == cudaSuccess) e = cudaMalloc((void**)&b->dtk, 2 * sizeof(int));
-    if (e == cudaSuccess) e = cudaMemset(b->dtk, 0, 2 * sizeof(int));
-    if (e == cudaSuccess) e = cudaMallocHost((void**)&b->htk, 2 * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b->dtk, 3 * sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(b->dtk, 0, 3 * sizeof(int));
+    if (e == cudaSuccess) e = cudaMallocHost((void**)&b->htk, 3 * sizeof(int));
     if (e != cudaSuccess) {
         destroy_batch(b);
         return bfail(EVPG_ERR_CUDA, "batch creation: %s", cudaGetErrorString(e));
     }
-    b->htk[0] = b->htk[1] = 0;
+    b->htk[0] = b->htk[1] = b->htk[2] = 0;
     *out = b;
     return EVPG_OK;
 }

@@ -124,8 +124,10 @@ __host__ __device__ constexpr int skewed_len(int n) { return n + n / 16; }
 // Run every stage of `pl` on npen pencils held in `a` (pencil p starts at
 // element p*ps, ps >= n, or >= n + n/16 with SKEW; scratch `b` has the same
 // layout). Returns the buffer holding the result. Must be called by all
-// threads of the CTA; ends with a __syncthreads.
-template <typename T, int SIGN, bool SKEW = false>
+// threads of the CTA; ends with a __syncthreads. R16: the plan may contain
+// radix-16 stages (FP32 only; the 16-value buffer costs registers, so only the
+// X pass, whose two-stage transforms of n = 128 gain most, is built with it).
+template <typename T, int SIGN, bool SKEW = false, bool R16 = false>
 __device__ C2<T>* fft_batch(C2<T>* a, C2<T>* b, int npen, int ps, const FftPlan& pl,
                             const C2<T>* tw) {
     const int n = pl.n;
@@ -141,11 +143,9 @@ __device__ C2<T>* fft_batch(C2<T>* a, C2<T>* b, int npen, int ps, const FftPlan&
             const C2<T>* src = in + pen * ps;
             C2<T>* dst = out + pen * ps;
             const int d0 = jq * Ns * r + jm;
-            // radix 16 in FP32 only (the tuner offers it there): an FP64 buffer of
-            // 16 complex values would cost the FP64 kernels occupancy
-            constexpr bool R16 = sizeof(T) == 4;
-            C2<T> v[R16 ? 16 : 8];
-            if (R16 && r == 16) {
+            constexpr bool W16 = R16 && sizeof(T) == 4;
+            C2<T> v[W16 ? 16 : 8];
+            if (W16 && r == 16) {
 #pragma unroll
                 for (int q = 0; q < 16; q++) {
                     v[q] = src[fsk<SKEW>(j + q * m)];

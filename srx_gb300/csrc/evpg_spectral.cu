@@ -126,7 +126,7 @@ __device__ __forceinline__ void x_green_body(const XArgs<T>& a, const GreenK<T>&
     }
     cp_async_wait_all();
     __syncthreads();
-    C2<T>* R = fft_batch<T, -1, SK>(bA, bB, 6 * np, ps, a.pl, tw);
+    C2<T>* R = fft_batch<T, -1, SK, true>(bA, bB, 6 * np, ps, a.pl, tw);
     C2<T>* W = (R == bA) ? bB : bA;
     for (int i = threadIdx.x; i < n * np; i += blockDim.x) {
         const int kk = a.dn.div(i), kx = i - kk * n, kz = kz0 + kk, ky = y;
@@ -161,7 +161,7 @@ __device__ __forceinline__ void x_green_body(const XArgs<T>& a, const GreenK<T>&
         for (int c = 0; c < 9; c++) W[(c * np + kk) * ps + fsk<SK>(kx)] = du[c];
     }
     __syncthreads();
-    const C2<T>* R2 = fft_batch<T, 1, SK>(W, (W == bA) ? bB : bA, 9 * np, ps, a.pl, tw);
+    const C2<T>* R2 = fft_batch<T, 1, SK, true>(W, (W == bA) ? bB : bA, 9 * np, ps, a.pl, tw);
     for (int i = threadIdx.x; i < 9 * n * np; i += blockDim.x) {
         const int c = dnq.div(i), rem = i - c * n * np, x = dq.div(rem), kk = rem - x * np;
         a.spec[(size_t)c * g.Nh + x * xs + (size_t)y * nh + kz0 + kk] = R2[(c * np + kk) * ps + fsk<SK>(x)];
@@ -968,7 +968,8 @@ static int tune_t(Ctx& c, T* sig, const C2<T>* const* tw, int force, double* gai
         const int ax = axis_of_pass[pass];
         float best = time_pass<T>(c, pass, P, pl, sig, scratch, tw, e0, e1);
         if (pass == 2 || !fused_default) t0 += best;
-        for (const std::vector<int>& f : factor_orders(len_of_pass[pass], sizeof(T) == 4)) {
+        // radix 16: FP32 X pass (the z and y passes are built without it)
+        for (const std::vector<int>& f : factor_orders(len_of_pass[pass], sizeof(T) == 4 && pass == 2)) {
             FftPlan trial[3] = {pl[0], pl[1], pl[2]};
             plan_of(len_of_pass[pass], f, trial[ax]);
             const float t = time_pass<T>(c, pass, P, trial, sig, scratch, tw, e0, e1);
