@@ -187,6 +187,9 @@ __host__ __device__ constexpr int sidx(int i, int j) { return i * 6 - i * (i - 1
 
 // Solve M x = b for symmetric positive definite M (packed upper, 21 entries)
 // by LDL^T without pivoting. Returns false when a pivot is not positive.
+// Every loop has a constant trip count with the triangle as a guard, so the
+// loops unroll whole and m stays in registers (triangular bounds left the
+// packed matrix in local memory).
 template <typename T>
 __device__ __forceinline__ bool ldl_solve(T (&m)[21], const T (&b)[6], T (&x)[6]) {
     // in place: m[sidx(k,i)] holds L(i,k) for i > k and d_k on the diagonal
@@ -196,16 +199,20 @@ __device__ __forceinline__ bool ldl_solve(T (&m)[21], const T (&b)[6], T (&x)[6]
     for (int j = 0; j < 6; j++) {
         T dj = m[sidx(j, j)];
 #pragma unroll
-        for (int k = 0; k < j; k++) dj -= m[sidx(k, j)] * m[sidx(k, j)] * m[sidx(k, k)];
+        for (int k = 0; k < 6; k++)
+            if (k < j) dj -= m[sidx(k, j)] * m[sidx(k, j)] * m[sidx(k, k)];
         m[sidx(j, j)] = dj;
         ok = ok && (dj > (T)0);
         id[j] = fdiv((T)1, dj);
 #pragma unroll
-        for (int i = j + 1; i < 6; i++) {
-            T t = m[sidx(j, i)];
+        for (int i = 0; i < 6; i++) {
+            if (i > j) {
+                T t = m[sidx(j, i)];
 #pragma unroll
-            for (int k = 0; k < j; k++) t -= m[sidx(k, i)] * m[sidx(k, j)] * m[sidx(k, k)];
-            m[sidx(j, i)] = t * id[j];
+                for (int k = 0; k < 6; k++)
+                    if (k < j) t -= m[sidx(k, i)] * m[sidx(k, j)] * m[sidx(k, k)];
+                m[sidx(j, i)] = t * id[j];
+            }
         }
     }
     T y[6];
@@ -213,14 +220,16 @@ __device__ __forceinline__ bool ldl_solve(T (&m)[21], const T (&b)[6], T (&x)[6]
     for (int i = 0; i < 6; i++) {
         T t = b[i];
 #pragma unroll
-        for (int k = 0; k < i; k++) t -= m[sidx(k, i)] * y[k];
+        for (int k = 0; k < 6; k++)
+            if (k < i) t -= m[sidx(k, i)] * y[k];
         y[i] = t;
     }
 #pragma unroll
     for (int i = 5; i >= 0; i--) {
         T t = y[i] * id[i];
 #pragma unroll
-        for (int k = i + 1; k < 6; k++) t -= m[sidx(i, k)] * x[k];
+        for (int k = 0; k < 6; k++)
+            if (k > i) t -= m[sidx(i, k)] * x[k];
         x[i] = t;
     }
     return ok;
