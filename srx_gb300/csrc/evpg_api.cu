@@ -481,8 +481,17 @@ int evpg_create(const evpg_rve_desc* d, void** out) {
         }
         e = put(c->sgr64, t.data(), t.size() * sizeof(double));
         if (e == cudaSuccess && f32) {
-            std::vector<float> hf(t.size());
-            for (size_t i = 0; i < hf.size(); i++) hf[i] = (float)t[i];
+            // FP32 rows: packed upper triangle of (S_gr + S_gr^T)/2 only (21);
+            // the NR adds S066 from its constant bank. S_gr is symmetric up to
+            // the rounding of its inversion, far below FP32 resolution.
+            std::vector<float> hf(t.size(), 0.0f);
+            for (int o = 0; o < d->n_orient; o++) {
+                const double* sg = d->s_gr + 36 * (size_t)o;
+                float* row = hf.data() + SGR_STRIDE * (size_t)o;
+                int k = 0;
+                for (int i = 0; i < 6; i++)
+                    for (int j = i; j < 6; j++) row[k++] = (float)(0.5 * (sg[i * 6 + j] + sg[j * 6 + i]));
+            }
             e = put(c->sgr32, hf.data(), hf.size() * sizeof(float));
         }
     }

@@ -247,9 +247,24 @@ __device__ __forceinline__ void mat6v(const T (&m)[6][6], const T* x, T* y) {
 }
 
 // S x with S read from the per-orientation table (L1-resident: voxels of a
-// grain share it)
+// grain share it). FP64 rows hold S_gr (36) and the packed NR matrix base
+// S066 + sym(S_gr) (21); FP32 rows hold the packed sym(S_gr) alone (21), which
+// serves both (36 + 21 loads per Newton step become 21).
 template <typename T>
 __device__ __forceinline__ void sgr_v(const T* sg, const T* x, T* y) {
+    if (sizeof(T) == 4) {
+        T u[21];
+#pragma unroll
+        for (int k = 0; k < 21; k++) u[k] = __ldg(sg + k);
+#pragma unroll
+        for (int i = 0; i < 6; i++) {
+            T s = (T)0;
+#pragma unroll
+            for (int j = 0; j < 6; j++) s += u[i <= j ? sidx(i, j) : sidx(j, i)] * x[j];
+            y[i] = s;
+        }
+        return;
+    }
 #pragma unroll
     for (int i = 0; i < 6; i++) {
         T s = (T)0;
@@ -257,6 +272,21 @@ __device__ __forceinline__ void sgr_v(const T* sg, const T* x, T* y) {
         for (int j = 0; j < 6; j++) s += __ldg(sg + i * 6 + j) * x[j];
         y[i] = s;
     }
+}
+
+// Packed base of the NR matrix, S066 + sym(S_gr), of the voxel's orientation.
+template <typename T>
+__device__ __forceinline__ void nr_matrix_base(const T* sg, const T (&S66)[6][6], T (&m)[21]) {
+    if (sizeof(T) == 4) {
+#pragma unroll
+        for (int i = 0; i < 6; i++)
+#pragma unroll
+            for (int j = 0; j < 6; j++)
+                if (j >= i) m[sidx(i, j)] = S66[i][j] + __ldg(sg + sidx(i, j));
+        return;
+    }
+#pragma unroll
+    for (int k = 0; k < 21; k++) m[k] = __ldg(sg + 36 + k);
 }
 
 // Warp-level partial sums without a block barrier: every warp writes its own
@@ -412,8 +442,7 @@ __device__ __forceinline__ void nr_body(const NrArgs<T>& a, int bid, unsigned ch
                 // M = S066 + sym(S) + dt d_edot (the first two per orientation);
                 // rhs = S066 R = S066 (sig - lam) + te
                 T m[21];
-#pragma unroll
-                for (int k = 0; k < 21; k++) m[k] = __ldg(sg + 36 + k);
+                nr_matrix_base<T>(sg, S66, m);
                 {
                     int k = 0;
 #pragma unroll
