@@ -248,6 +248,11 @@ int evpg_set_nr_tolerance(void *ctx, double tol, int32_t itmax);
  * default (on for FP32 bulk where eligible), 0 off, 1 on where eligible.
  * evpg_get_schedule then reports 0 pencils for the z and y passes. */
 int evpg_set_fused(void *ctx, int32_t mode);
+/* X pass as warp-register transforms (one warp per (y, kz) pencil with the six
+ * stress components in registers, FP32 with n0 in {32, 64, 128}): mode -1
+ * default (on where eligible), 0 the shared-memory Stockham pass (whose radix
+ * order evpg_set_radix sets), 1 on where eligible. The autotuner times both. */
+int evpg_set_xpass(void *ctx, int32_t mode);
 /* FFT radix order of one axis (0 x, 1 y, 2 z) for the Stockham passes:
  * nstages radices (2..16, product n of the axis; 16 in FP32 contexts on the
  * x axis only) applied in the given order. The autotuner chooses among such

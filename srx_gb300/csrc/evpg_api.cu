@@ -532,6 +532,7 @@ int evpg_create(const evpg_rve_desc* d, void** out) {
     }
     set_kernel_attributes();
     c->sched_fused = -1;
+    c->sched_xpass = -1;
     for (int i = 0; i < 2 && e == cudaSuccess; i++) e = cudaEventCreateWithFlags(&c->dl_ev[i], cudaEventDisableTiming);
     if (e != cudaSuccess) {
         free_ctx(c);
@@ -845,6 +846,16 @@ int evpg_set_fused(void* ctx, int32_t mode) {
     if (!c || mode < -1 || mode > 1) return fail(EVPG_ERR_ARG, "bad argument");
     CK(cudaStreamSynchronize(c->stream));
     c->sched_fused = mode;
+    build_sets(*c);
+    c->version++;
+    return EVPG_OK;
+}
+
+int evpg_set_xpass(void* ctx, int32_t mode) {
+    Ctx* c = (Ctx*)ctx;
+    if (!c || mode < -1 || mode > 1) return fail(EVPG_ERR_ARG, "bad argument");
+    CK(cudaStreamSynchronize(c->stream));
+    c->sched_xpass = mode;
     build_sets(*c);
     c->version++;
     return EVPG_OK;

@@ -84,8 +84,8 @@ template <typename T> struct XArgs {
     int P;
     GreenK<T> gk;
     // index divisors: n0, and np, n0*np for full tiles ([0], np = P) and the
-    // last tile ([1], np = nh - (tiles - 1) P)
-    FastDiv dn, dnp[2], dnnp[2];
+    // last tile ([1], np = nh - (tiles - 1) P); nh (warp-register pass)
+    FastDiv dn, dnp[2], dnnp[2], dnh;
 };
 
 template <typename T> struct NrArgs {
@@ -225,6 +225,9 @@ template <typename T> struct SpecSet {
     int epl;
     int grid_pf, grid_pi;
     size_t sm_p;
+    // warp-register X pass (xw = n0/32 elements per lane; 0: shared-memory pass)
+    int xw, grid_xw;
+    size_t sm_xw;
 };
 
 template <typename T> struct NrSet {

@@ -61,6 +61,7 @@ struct Ctx {
     KernelSets* ks;     // launch arguments of every kernel (built at creation)
     int sched_p[3];     // pencils per CTA of the z, y, x passes (0: default)
     int sched_fused;    // fused z+y passes: -1 default (FP32 bulk when eligible), 0 off, 1 on
+    int sched_xpass;    // warp-register X pass: -1 default (when eligible), 0 off, 1 on
     int nsm;            // SM count of the device
     long long version;  // bumped whenever ks changes (batches refresh their tables)
     double* dl_dev;     // download packing buffers (2 chunks, allocated on first use)

@@ -250,4 +250,38 @@ __device__ __forceinline__ void warp_fft(C2<T> (&v)[EPL], const C2<T>* tw, int l
     }
 }
 
+// Inverse of warp_fft<T, EPL, -1>, unnormalised (n times the inverse): lane
+// l holds X[k2 + EPL * brev5(l)] in v[k2] (the forward transform's output
+// order); on return lane l holds x[l + 32 q] in v[q]. The forward steps
+// undone in reverse: the cross-lane radix-2 stages from h = 1 up, each
+// (A, B) = (a + b, (a - b) w) mapped back to (A + B conj(w), A - B conj(w)),
+// then the conjugate twiddles and the length-EPL DFT with the opposite sign.
+template <typename T, int EPL>
+__device__ __forceinline__ void warp_ifft_brev(C2<T> (&v)[EPL], const C2<T>* tw, int lane) {
+#pragma unroll
+    for (int h = 1; h <= 16; h <<= 1) {
+        const bool hi = (lane & h) != 0;
+        const C2<T> w = twid<T, 1>(tw, (lane & (h - 1)) * (16 / h) * EPL);
+#pragma unroll
+        for (int k2 = 0; k2 < EPL; k2++) {
+            const C2<T> t = hi ? cmul<T>(v[k2], w) : v[k2];
+            C2<T> p;
+            p.x = __shfl_xor_sync(0xffffffffu, t.x, h);
+            p.y = __shfl_xor_sync(0xffffffffu, t.y, h);
+            v[k2] = hi ? csub<T>(p, t) : cadd<T>(t, p);
+        }
+    }
+#pragma unroll
+    for (int k2 = 1; k2 < EPL; k2++) v[k2] = cmul<T>(v[k2], twid<T, 1>(tw, lane * k2));
+    if (EPL == 2) {
+        const C2<T> a = v[0], b = v[1];
+        v[0] = cadd<T>(a, b);
+        v[1] = csub<T>(a, b);
+    } else if (EPL == 4) {
+        dft4<T, 1>(v[0], v[1], v[2], v[3]);
+    } else if (EPL == 8) {
+        dft8<T, 1>(v);
+    }
+}
+
 }  // namespace evpg

@@ -104,6 +104,37 @@ __device__ __forceinline__ void y_body(const YArgs<T>& a, int bid, unsigned char
 }
 
 // Forward x, Green contraction, inverse x on pencils (y, kz..kz+P).
+// Green correction du(k) = Gamma(k) : sig_hat(k) at one wave vector, with the
+// k = 0 term, and on the Nyquist planes the Hermitian part
+// (du(k) + conj du(-k))/2 with sig_hat(-k) = conj sig_hat(k).
+template <typename T, bool SHARED_C0>
+__device__ __forceinline__ void green_point(const GreenK<T>& gk, const Grid& g, const T (&rn)[3], int kx,
+                                            int ky, int kz, const C2<T> (&sb)[6], C2<T> (&du)[9]) {
+    if ((kx | ky | kz) == 0) {
+        green_k0<T>(gk.s0, gk.elast_bc, sb, du);
+        return;
+    }
+    T nv[3];
+    kvec<T>(kx, ky, kz, g, rn, nv);
+    if (SHARED_C0) green_du<T>(C0Shared<T>{&gk.c0[0][0][0][0]}, nv, sb, du);
+    else green_du<T>(C0Param<T>{gk.c0}, nv, sb, du);
+    const bool nyq = ((g.n0 & 1) == 0 && 2 * kx == g.n0) ||
+                     ((g.n1 & 1) == 0 && 2 * ky == g.n1) ||
+                     ((g.n2 & 1) == 0 && 2 * kz == g.n2);
+    if (nyq) {
+        C2<T> sm[6], dm[9];
+#pragma unroll
+        for (int c = 0; c < 6; c++) sm[c] = cconj<T>(sb[c]);
+        const int mx = (g.n0 - kx) % g.n0, my = (g.n1 - ky) % g.n1, mz = (g.n2 - kz) % g.n2;
+        kvec<T>(mx, my, mz, g, rn, nv);
+        if (SHARED_C0) green_du<T>(C0Shared<T>{&gk.c0[0][0][0][0]}, nv, sm, dm);
+        else green_du<T>(C0Param<T>{gk.c0}, nv, sm, dm);
+#pragma unroll
+        for (int c = 0; c < 9; c++)
+            du[c] = mk<T>((T)0.5 * (du[c].x + dm[c].x), (T)0.5 * (du[c].y - dm[c].y));
+    }
+}
+
 template <typename T, bool SHARED_C0>
 __device__ __forceinline__ void x_green_body(const XArgs<T>& a, const GreenK<T>& gk, int bid,
                                              unsigned char* smem) {
@@ -133,30 +164,7 @@ __device__ __forceinline__ void x_green_body(const XArgs<T>& a, const GreenK<T>&
         C2<T> sb[6], du[9];
 #pragma unroll
         for (int c = 0; c < 6; c++) sb[c] = R[(c * np + kk) * ps + fsk<SK>(kx)];
-        if ((kx | ky | kz) == 0) {
-            green_k0<T>(gk.s0, gk.elast_bc, sb, du);
-        } else {
-            T nv[3];
-            kvec<T>(kx, ky, kz, g, rn, nv);
-            if (SHARED_C0) green_du<T>(C0Shared<T>{&gk.c0[0][0][0][0]}, nv, sb, du);
-            else green_du<T>(C0Param<T>{gk.c0}, nv, sb, du);
-            const bool nyq = ((g.n0 & 1) == 0 && 2 * kx == g.n0) ||
-                             ((g.n1 & 1) == 0 && 2 * ky == g.n1) ||
-                             ((g.n2 & 1) == 0 && 2 * kz == g.n2);
-            if (nyq) {
-                // Hermitian part: (du(k) + conj du(-k))/2 with sig_hat(-k) = conj sig_hat(k)
-                C2<T> sm[6], dm[9];
-#pragma unroll
-                for (int c = 0; c < 6; c++) sm[c] = cconj<T>(sb[c]);
-                const int mx = (g.n0 - kx) % g.n0, my = (g.n1 - ky) % g.n1, mz = (g.n2 - kz) % g.n2;
-                kvec<T>(mx, my, mz, g, rn, nv);
-                if (SHARED_C0) green_du<T>(C0Shared<T>{&gk.c0[0][0][0][0]}, nv, sm, dm);
-                else green_du<T>(C0Param<T>{gk.c0}, nv, sm, dm);
-#pragma unroll
-                for (int c = 0; c < 9; c++)
-                    du[c] = mk<T>((T)0.5 * (du[c].x + dm[c].x), (T)0.5 * (du[c].y - dm[c].y));
-            }
-        }
+        green_point<T, SHARED_C0>(gk, g, rn, kx, ky, kz, sb, du);
 #pragma unroll
         for (int c = 0; c < 9; c++) W[(c * np + kk) * ps + fsk<SK>(kx)] = du[c];
     }
@@ -165,6 +173,81 @@ __device__ __forceinline__ void x_green_body(const XArgs<T>& a, const GreenK<T>&
     for (int i = threadIdx.x; i < 9 * n * np; i += blockDim.x) {
         const int c = dnq.div(i), rem = i - c * n * np, x = dq.div(rem), kk = rem - x * np;
         a.spec[(size_t)c * g.Nh + x * xs + (size_t)y * nh + kz0 + kk] = R2[(c * np + kk) * ps + fsk<SK>(x)];
+    }
+}
+
+// X pass as warp-register transforms (FP32, n0 = 32 E with E in {1, 2, 4}).
+// A CTA takes XW_PEN consecutive pencils of the flattened (y, kz) index (one
+// x-row of the spectrum holds them contiguously), one warp per pencil with
+// the six stress components in registers (lane l holds x = l + 32 q): the
+// forward transforms, the Green contraction at the lane's E wave numbers and
+// the nine inverse transforms use shared memory only for the coalesced
+// global loads and stores. The [component][x][pencil] tile has padded rows
+// (8-byte column reads without bank conflicts), and every warp reads and
+// writes its own column, so no barrier separates the forward and inverse work.
+constexpr int XW_PEN = 4;
+constexpr int XW_ROW = XW_PEN + 1;
+constexpr int XW_THREADS = 32 * XW_PEN;
+
+__host__ __device__ constexpr bool xw_eligible(int n0, size_t es) {
+    return es == 8 && (n0 == 32 || n0 == 64 || n0 == 128);
+}
+__host__ __device__ constexpr size_t xw_smem(int n0, size_t es) { return (size_t)(n0 + 9 * n0 * XW_ROW) * es; }
+
+template <typename T, int E, bool SHARED_C0>
+__device__ __forceinline__ void x_warp_body(const XArgs<T>& a, const GreenK<T>& gk, int bid, unsigned char* smem) {
+    const Grid& g = a.g;
+    constexpr int n = 32 * E, LOGN = E == 1 ? 5 : E == 2 ? 6 : 7;
+    const int nh = g.nh;
+    C2<T>* tw = reinterpret_cast<C2<T>*>(smem);
+    C2<T>* tile = tw + n;
+    const int p0 = bid * XW_PEN, np = min(XW_PEN, g.n1 * nh - p0);
+    const size_t xs = (size_t)g.n1 * nh;
+    const T rn[3] = {gk.rn[0], gk.rn[1], gk.rn[2]};
+    load_tw<T>(tw, a.tw, n);
+    for (int i = threadIdx.x; i < 6 * n * XW_PEN; i += blockDim.x) {
+        const int kk = i % XW_PEN, row = i / XW_PEN, c = row >> LOGN, x = row & (n - 1);
+        if (kk < np) cp_async_elem<T>(tile + row * XW_ROW + kk, a.spec + (size_t)c * g.Nh + x * xs + p0 + kk);
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (w < np) {
+        const int p = p0 + w, ky = a.dnh.div(p), kz = p - ky * nh;
+        C2<T>* col = tile + w;
+        C2<T> v[6][E];
+#pragma unroll
+        for (int c = 0; c < 6; c++)
+#pragma unroll
+            for (int q = 0; q < E; q++) v[c][q] = col[(c * n + lane + 32 * q) * XW_ROW];
+#pragma unroll
+        for (int c = 0; c < 6; c++) warp_fft<T, E, -1>(v[c], tw, lane);
+        // lane l holds kx = k2 + E brev5(l) in v[.][k2]; du goes to the lane's
+        // own slots, which its inverse transforms read back in that order
+        const int kb = E * brev5(lane);
+#pragma unroll
+        for (int k2 = 0; k2 < E; k2++) {
+            C2<T> sb[6], du[9];
+#pragma unroll
+            for (int c = 0; c < 6; c++) sb[c] = v[c][k2];
+            green_point<T, SHARED_C0>(gk, g, rn, k2 + kb, ky, kz, sb, du);
+#pragma unroll
+            for (int c = 0; c < 9; c++) col[(c * n + lane + 32 * k2) * XW_ROW] = du[c];
+        }
+#pragma unroll 1
+        for (int c = 0; c < 9; c++) {
+            C2<T> u[E];
+#pragma unroll
+            for (int q = 0; q < E; q++) u[q] = col[(c * n + lane + 32 * q) * XW_ROW];
+            warp_ifft_brev<T, E>(u, tw, lane);
+#pragma unroll
+            for (int q = 0; q < E; q++) col[(c * n + lane + 32 * q) * XW_ROW] = u[q];
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < 9 * n * XW_PEN; i += blockDim.x) {
+        const int kk = i % XW_PEN, row = i / XW_PEN, c = row >> LOGN, x = row & (n - 1);
+        if (kk < np) a.spec[(size_t)c * g.Nh + x * xs + p0 + kk] = tile[row * XW_ROW + kk];
     }
 }
 
@@ -462,6 +545,13 @@ __global__ void __launch_bounds__(SPEC_THREADS) k_x_green(const __grid_constant_
     x_green_body<T, false>(a, a.gk, blockIdx.x, smem);
 }
 
+template <typename T, int E>
+__global__ void __launch_bounds__(XW_THREADS) k_x_warp(const __grid_constant__ XArgs<T> a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    if (!gate_open(a.macro, a.gate)) return;
+    x_warp_body<T, E, false>(a, a.gk, blockIdx.x, smem);
+}
+
 template <typename T>
 __global__ void __launch_bounds__(SPEC_THREADS) k_inv_z(const __grid_constant__ ZArgs<T> a) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -608,11 +698,12 @@ template <typename T> static void set_x_divisors(XArgs<T>& xa) {
     xa.dnnp[0].set(g.n0 * xa.P);
     xa.dnp[1].set(last);
     xa.dnnp[1].set(g.n0 * last);
+    xa.dnh.set(g.nh);
 }
 
 template <typename T>
 static void fill_spec_t(Ctx& c, SpecSet<T>& s, const int P[3], const FftPlan pl[3], T* sig, T* dg,
-                        const C2<T>* const* tw, int fused) {
+                        const C2<T>* const* tw, int fused, int xpass) {
     const Grid& g = c.g;
     C2<T>* spec = reinterpret_cast<C2<T>*>(c.spec);
     const size_t es = sizeof(C2<T>);
@@ -649,6 +740,10 @@ static void fill_spec_t(Ctx& c, SpecSet<T>& s, const int P[3], const FftPlan pl[
     set_x_divisors<T>(xa);
     s.grid_x = g.n1 * ((g.nh + xa.P - 1) / xa.P);
     s.sm_x = (size_t)(g.n0 + 18 * xa.P * x_pencil_stride(g.n0, es)) * es;
+    // warp-register X pass: FP32 with n0 in {32, 64, 128}, unless switched off
+    s.xw = (xpass != 0 && xw_eligible(g.n0, es)) ? g.n0 / 32 : 0;
+    s.grid_xw = (g.n1 * g.nh + XW_PEN - 1) / XW_PEN;
+    s.sm_xw = xw_smem(g.n0, es);
     s.epl = fused ? plane_epl(g, es) : 0;
     PlaneArgs<T>& pa = s.pl;
     pa.g = g; pa.macro = c.macro; pa.gate = GATE_RUNNING; pa.sig = sig; pa.dg = dg; pa.spec = spec;
@@ -671,7 +766,7 @@ static void build_spec_t(Ctx& c, T* sig, T* dg, const C2<T>* const* tw) {
     }
     // fused z+y passes: FP32-bulk by default, FP64 only when chosen (tuner)
     const int fused = c.sched_fused < 0 ? (sizeof(T) == 4) : c.sched_fused;
-    fill_spec_t<T>(c, spec_of<T>(*c.ks), P, c.pl, sig, dg, tw, fused);
+    fill_spec_t<T>(c, spec_of<T>(*c.ks), P, c.pl, sig, dg, tw, fused, c.sched_xpass);
 }
 
 void build_spectral_sets(Ctx& c) {
@@ -696,6 +791,9 @@ template <typename T> static void spec_attributes() {
     cudaFuncSetAttribute(kb_y<T, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
     cudaFuncSetAttribute(kb_y<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
     cudaFuncSetAttribute(kb_x_green<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx - 2048);
+    cudaFuncSetAttribute(k_x_warp<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(k_x_warp<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(k_x_warp<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
     cudaFuncSetAttribute(k_plane_fwd<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
     cudaFuncSetAttribute(k_plane_fwd<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
     cudaFuncSetAttribute(k_plane_fwd<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
@@ -737,6 +835,15 @@ static void plane_launch_batch(int fwd, int E, const BatchLaunch& L, cudaStream_
     }
 }
 
+// The X pass of the single-RVE chain: warp-register kernel when chosen.
+template <typename T>
+static void x_launch(const SpecSet<T>& s, const XArgs<T>& xa, cudaStream_t st) {
+    if (s.xw == 1) k_x_warp<T, 1><<<s.grid_xw, XW_THREADS, s.sm_xw, st>>>(xa);
+    else if (s.xw == 2) k_x_warp<T, 2><<<s.grid_xw, XW_THREADS, s.sm_xw, st>>>(xa);
+    else if (s.xw == 4) k_x_warp<T, 4><<<s.grid_xw, XW_THREADS, s.sm_xw, st>>>(xa);
+    else k_x_green<T><<<s.grid_x, SPEC_THREADS, s.sm_x, st>>>(xa);
+}
+
 void spectral_attributes() {
     spec_attributes<double>();
     spec_attributes<float>();
@@ -756,7 +863,7 @@ static cudaError_t spectral_t(Ctx& c, int gate) {
         plane_launch<T>(1, s.epl, s.grid_pf, s.sm_p, c.stream, pa);
         prof_mark(c, PG_FWD_Z, false);
         prof_mark(c, PG_X_GREEN, true);
-        k_x_green<T><<<s.grid_x, SPEC_THREADS, s.sm_x, c.stream>>>(xa);
+        x_launch<T>(s, xa, c.stream);
         prof_mark(c, PG_X_GREEN, false);
         prof_mark(c, PG_INV_Z, true);
         plane_launch<T>(0, s.epl, s.grid_pi, s.sm_p, c.stream, pa);
@@ -770,7 +877,7 @@ static cudaError_t spectral_t(Ctx& c, int gate) {
     k_y<T, -1><<<s.grid_y, SPEC_THREADS, s.sm_y, c.stream>>>(yf);
     prof_mark(c, PG_FWD_Y, false);
     prof_mark(c, PG_X_GREEN, true);
-    k_x_green<T><<<s.grid_x, SPEC_THREADS, s.sm_x, c.stream>>>(xa);
+    x_launch<T>(s, xa, c.stream);
     prof_mark(c, PG_X_GREEN, false);
     prof_mark(c, PG_INV_Y, true);
     k_y<T, 1><<<s.grid_y, SPEC_THREADS, s.sm_y, c.stream>>>(yi);
@@ -835,7 +942,7 @@ struct TuneEntry {
     int n0, n1, n2, prec;
     int P[3];
     FftPlan pl[3];
-    int fused;
+    int fused, xpass;
 };
 static std::mutex g_tune_mu;
 static std::vector<TuneEntry> g_tune_cache;
@@ -897,12 +1004,12 @@ constexpr size_t TUNE_SMEM_MAX = 200 * 1024;
 // Green contraction, 3: fused z+y plane kernels (forward + inverse)
 template <typename T>
 static float time_pass(Ctx& c, int pass, const int P[3], const FftPlan pl[3], T* sig, T* scratch,
-                       const C2<T>* const* tw, cudaEvent_t e0, cudaEvent_t e1) {
+                       const C2<T>* const* tw, cudaEvent_t e0, cudaEvent_t e1, int xpass = 0) {
     SpecSet<T> s;
-    fill_spec_t<T>(c, s, P, pl, sig, scratch, tw, pass == 3);
+    fill_spec_t<T>(c, s, P, pl, sig, scratch, tw, pass == 3, xpass);
     s.z.gate = s.yf.gate = s.yi.gate = s.x.gate = s.pl.gate = GATE_ALWAYS;
     if (pass == 3 && !s.epl) return 1e30f;
-    const size_t sm = pass == 0 ? s.sm_z : pass == 1 ? s.sm_y : pass == 2 ? s.sm_x : s.sm_p;
+    const size_t sm = pass == 0 ? s.sm_z : pass == 1 ? s.sm_y : pass == 2 ? (s.xw ? s.sm_xw : s.sm_x) : s.sm_p;
     if (sm > TUNE_SMEM_MAX) return 1e30f;
     if (pass == 0 && P[0] * c.g.n2 > SPEC_THREADS * INVZ_EPT) return 1e30f;
     auto launch = [&]() {
@@ -916,7 +1023,7 @@ static float time_pass(Ctx& c, int pass, const int P[3], const FftPlan pl[3], T*
             k_y<T, -1><<<s.grid_y, SPEC_THREADS, s.sm_y, c.stream>>>(s.yf);
             k_y<T, 1><<<s.grid_y, SPEC_THREADS, s.sm_y, c.stream>>>(s.yi);
         } else {
-            k_x_green<T><<<s.grid_x, SPEC_THREADS, s.sm_x, c.stream>>>(s.x);
+            x_launch<T>(s, s.x, c.stream);
         }
     };
     launch();
@@ -943,6 +1050,7 @@ static int tune_t(Ctx& c, T* sig, const C2<T>* const* tw, int force, double* gai
                     c.pl[a] = e.pl[a];
                 }
                 c.sched_fused = e.fused;
+                c.sched_xpass = e.xpass;
                 build_sets(c);
                 c.version++;
                 if (gain) *gain = 0.0;
@@ -964,10 +1072,12 @@ static int tune_t(Ctx& c, T* sig, const C2<T>* const* tw, int force, double* gai
     // the fused z+y kernels use the default radix-free warp transforms
     const float tf = time_pass<T>(c, 3, P, pl, sig, scratch, tw, e0, e1);
     const bool fused_default = cur.epl != 0;
+    int xpass = 0;
     for (int pass = 0; pass < 3; pass++) {
         const int ax = axis_of_pass[pass];
         float best = time_pass<T>(c, pass, P, pl, sig, scratch, tw, e0, e1);
-        if (pass == 2 || !fused_default) t0 += best;
+        if (pass == 2 && cur.xw) t0 += time_pass<T>(c, 2, P, pl, sig, scratch, tw, e0, e1, 1);
+        else if (pass == 2 || !fused_default) t0 += best;
         // radix 16: FP32 X pass (the z and y passes are built without it)
         for (const std::vector<int>& f : factor_orders(len_of_pass[pass], sizeof(T) == 4 && pass == 2)) {
             FftPlan trial[3] = {pl[0], pl[1], pl[2]};
@@ -989,6 +1099,14 @@ static int tune_t(Ctx& c, T* sig, const C2<T>* const* tw, int force, double* gai
                 P[pass] = q;
             }
         }
+        if (pass == 2 && xw_eligible(g.n0, sizeof(C2<T>))) {
+            // the warp-register X pass (no radix order or pencil count to choose)
+            const float t = time_pass<T>(c, 2, P, pl, sig, scratch, tw, e0, e1, 1);
+            if (t < best) {
+                best = t;
+                xpass = 1;
+            }
+        }
         tb[pass] = best;
     }
     if (fused_default) t0 += tf;
@@ -1004,6 +1122,7 @@ static int tune_t(Ctx& c, T* sig, const C2<T>* const* tw, int force, double* gai
         c.pl[a] = pl[a];
     }
     c.sched_fused = fused;
+    c.sched_xpass = xpass;
     build_sets(c);
     c.version++;
     if (gain) *gain = t1 > 0 ? t0 / t1 : 0.0;
@@ -1011,6 +1130,7 @@ static int tune_t(Ctx& c, T* sig, const C2<T>* const* tw, int force, double* gai
     TuneEntry e;
     e.n0 = g.n0; e.n1 = g.n1; e.n2 = g.n2; e.prec = prec;
     e.fused = fused;
+    e.xpass = xpass;
     for (int a = 0; a < 3; a++) {
         e.P[a] = P[a];
         e.pl[a] = pl[a];

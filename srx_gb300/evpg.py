@@ -203,6 +203,11 @@ class Job:
         lib().evpg_set_fused.argtypes = [C.c_void_p, C.c_int32]
         check(lib().evpg_set_fused(self.ctx, mode))
 
+    def set_xpass(self, mode: int) -> None:
+        """Warp-register X pass: -1 default, 0 shared-memory pass, 1 on where eligible."""
+        lib().evpg_set_xpass.argtypes = [C.c_void_p, C.c_int32]
+        check(lib().evpg_set_xpass(self.ctx, mode))
+
     def set_radix(self, axis: int, radices) -> None:
         """FFT radix order of one axis (0 x, 1 y, 2 z) for the Stockham passes."""
         L = lib()

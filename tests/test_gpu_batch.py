@@ -275,6 +275,7 @@ def test_radix16_stages(tmp_path):
     for orders in (None, ([16, 2], [8, 8], [2, 4, 8])):
         with evpg.Job(c["input"], c["rho0"], precision=1, nr_mode=1) as j:
             j.set_fused(0)
+            j.set_xpass(0)
             if orders:
                 for ax, r in enumerate(orders):
                     j.set_radix(ax, r)
@@ -284,6 +285,31 @@ def test_radix16_stages(tmp_path):
     with evpg.Job(c["input"], c["rho0"], precision=1, nr_mode=1) as j:
         with pytest.raises(evpg.EvpgError):
             j.set_radix(1, [4, 16])
+    assert abs(sum(res[0][0]) - sum(res[1][0])) <= 2
+    assert rel_err(res[1][2][7:16], res[0][2][7:16]) < 1e-5
+    l2 = np.linalg.norm(res[1][1] - res[0][1]) / np.linalg.norm(res[0][1])
+    assert l2 < 1e-4, l2
+
+
+@pytest.mark.parametrize("n0", [32, 64, 128])
+def test_warp_x_pass_equals_shared_memory_pass(tmp_path, n0):
+    """The warp-register X pass (one warp per pencil, all six components in
+    registers, inverse transforms from the bit-reversed order) against the
+    shared-memory Stockham X pass on the same FP32-bulk increments: results
+    within the form's tolerance, for 1, 2 and 4 elements per lane, with a
+    mixed-radix y axis (18) and an odd z axis (15) beside the x axis."""
+    from conftest import rel_err
+    from srx_gb300 import rve
+    evpg = _evpg()
+    grid = (n0, 18, 15)
+    job = rve.Job(n=grid, load="tension", rate=1e-3, strain_per_step=2e-4, n_steps=2)
+    c = rve.make_case(str(tmp_path / "c"), grid, 6, 34, job, rho0=(0.5, 5.0))
+    res = []
+    for mode in (0, 1):
+        with evpg.Job(c["input"], c["rho0"], precision=1, nr_mode=1) as j:
+            j.set_xpass(mode)
+            its = [j.increment(k) for k in range(2)]
+            res.append((its, j.download(evpg.F_SIG6), j.scalars()))
     assert abs(sum(res[0][0]) - sum(res[1][0])) <= 2
     assert rel_err(res[1][2][7:16], res[0][2][7:16]) < 1e-5
     l2 = np.linalg.norm(res[1][1] - res[0][1]) / np.linalg.norm(res[0][1])
