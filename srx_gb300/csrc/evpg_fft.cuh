@@ -215,15 +215,46 @@ __device__ C2<T>* fft_batch(C2<T>* a, C2<T>* b, int npen, int ps, const FftPlan&
     return in;
 }
 
+// Per-lane constants of the warp transforms, loaded once per kernel from the
+// W_n^t table (they depend on the lane only): the twiddle of each cross-lane
+// stage h = 16, 8, 4, 2 (1 on the low lane of a pair, whose result is not
+// rotated), the sign +1 / -1 of the low / high lane of each stage
+// h = 16 .. 1, and W_n^(l k2) for k2 = 1 .. EPL-1. The butterfly then reads
+// p + s u (partner p, own value u: a + b on the low lane, a - b on the high
+// lane) followed by one complex product, with no select between two results.
+template <typename T, int EPL> struct WarpTw {
+    C2<T> w[4];
+    T s[5];
+    C2<T> k[EPL > 1 ? EPL - 1 : 1];
+    __device__ __forceinline__ void init(const C2<T>* tw, int lane) {
+#pragma unroll
+        for (int st = 0; st < 5; st++) {
+            const int h = 16 >> st;
+            const bool hi = (lane & h) != 0;
+            s[st] = hi ? (T)-1 : (T)1;
+            if (st < 4) w[st] = hi ? tw[(lane & (h - 1)) * (16 / h) * EPL] : mk<T>((T)1, (T)0);
+        }
+#pragma unroll
+        for (int k2 = 1; k2 < EPL; k2++) k[k2 - 1] = tw[lane * k2];
+    }
+};
+
+// a * w (SIGN < 0) or a * conj(w) (SIGN > 0)
+template <typename T, int SIGN>
+__device__ __forceinline__ C2<T> cmul_s(C2<T> a, C2<T> w) {
+    return SIGN < 0 ? cmul<T>(a, w) : mk<T>(a.x * w.x + a.y * w.y, a.y * w.x - a.x * w.y);
+}
+
 // Warp-register FFT of length n = 32*EPL (EPL = 1, 2, 4 or 8): lane l holds
 // x[l + 32 q] in v[q]. Four-step split n = EPL x 32: a length-EPL DFT in
 // registers, twiddles W_n^(l k2), then for every k2 a 32-point radix-2
 // decimation-in-frequency transform across the lanes with shuffles. On
-// return lane l holds X[k2 + EPL * brev5(l)] in v[k2]. tw: W_n^t table.
+// return lane l holds X[k2 + EPL * brev5(l)] in v[k2]. t: the lane's
+// constants of the W_n^t table.
 __device__ __forceinline__ int brev5(int l) { return (int)(__brev((unsigned)l) >> 27); }
 
 template <typename T, int EPL, int SIGN>
-__device__ __forceinline__ void warp_fft(C2<T> (&v)[EPL], const C2<T>* tw, int lane) {
+__device__ __forceinline__ void warp_fft(C2<T> (&v)[EPL], const WarpTw<T, EPL>& t) {
     if (EPL == 2) {
         const C2<T> a = v[0], b = v[1];
         v[0] = cadd<T>(a, b);
@@ -234,18 +265,19 @@ __device__ __forceinline__ void warp_fft(C2<T> (&v)[EPL], const C2<T>* tw, int l
         dft8<T, SIGN>(v);
     }
 #pragma unroll
-    for (int k2 = 1; k2 < EPL; k2++) v[k2] = cmul<T>(v[k2], twid<T, SIGN>(tw, lane * k2));
+    for (int k2 = 1; k2 < EPL; k2++) v[k2] = cmul_s<T, SIGN>(v[k2], t.k[k2 - 1]);
 #pragma unroll
-    for (int h = 16; h >= 1; h >>= 1) {
-        const bool hi = (lane & h) != 0;
-        const C2<T> w = twid<T, SIGN>(tw, (lane & (h - 1)) * (16 / h) * EPL);
+    for (int st = 0; st < 5; st++) {
+        const int h = 16 >> st;
 #pragma unroll
         for (int k2 = 0; k2 < EPL; k2++) {
             const C2<T> u = v[k2];
-            C2<T> p;
-            p.x = __shfl_xor_sync(0xffffffffu, u.x, h);
-            p.y = __shfl_xor_sync(0xffffffffu, u.y, h);
-            v[k2] = hi ? cmul<T>(csub<T>(p, u), w) : cadd<T>(u, p);
+            C2<T> r;
+            r.x = __shfl_xor_sync(0xffffffffu, u.x, h);
+            r.y = __shfl_xor_sync(0xffffffffu, u.y, h);
+            r.x = fma(t.s[st], u.x, r.x);
+            r.y = fma(t.s[st], u.y, r.y);
+            v[k2] = st < 4 ? cmul_s<T, SIGN>(r, t.w[st < 4 ? st : 0]) : r;
         }
     }
 }
@@ -257,22 +289,21 @@ __device__ __forceinline__ void warp_fft(C2<T> (&v)[EPL], const C2<T>* tw, int l
 // (A, B) = (a + b, (a - b) w) mapped back to (A + B conj(w), A - B conj(w)),
 // then the conjugate twiddles and the length-EPL DFT with the opposite sign.
 template <typename T, int EPL>
-__device__ __forceinline__ void warp_ifft_brev(C2<T> (&v)[EPL], const C2<T>* tw, int lane) {
+__device__ __forceinline__ void warp_ifft_brev(C2<T> (&v)[EPL], const WarpTw<T, EPL>& t) {
 #pragma unroll
-    for (int h = 1; h <= 16; h <<= 1) {
-        const bool hi = (lane & h) != 0;
-        const C2<T> w = twid<T, 1>(tw, (lane & (h - 1)) * (16 / h) * EPL);
+    for (int st = 4; st >= 0; st--) {
+        const int h = 16 >> st;
 #pragma unroll
         for (int k2 = 0; k2 < EPL; k2++) {
-            const C2<T> t = hi ? cmul<T>(v[k2], w) : v[k2];
+            const C2<T> u = st < 4 ? cmul_s<T, 1>(v[k2], t.w[st < 4 ? st : 0]) : v[k2];
             C2<T> p;
-            p.x = __shfl_xor_sync(0xffffffffu, t.x, h);
-            p.y = __shfl_xor_sync(0xffffffffu, t.y, h);
-            v[k2] = hi ? csub<T>(p, t) : cadd<T>(t, p);
+            p.x = __shfl_xor_sync(0xffffffffu, u.x, h);
+            p.y = __shfl_xor_sync(0xffffffffu, u.y, h);
+            v[k2] = mk<T>(fma(t.s[st], u.x, p.x), fma(t.s[st], u.y, p.y));
         }
     }
 #pragma unroll
-    for (int k2 = 1; k2 < EPL; k2++) v[k2] = cmul<T>(v[k2], twid<T, 1>(tw, lane * k2));
+    for (int k2 = 1; k2 < EPL; k2++) v[k2] = cmul_s<T, 1>(v[k2], t.k[k2 - 1]);
     if (EPL == 2) {
         const C2<T> a = v[0], b = v[1];
         v[0] = cadd<T>(a, b);

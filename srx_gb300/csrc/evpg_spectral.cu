@@ -215,13 +215,15 @@ __device__ __forceinline__ void x_warp_body(const XArgs<T>& a, const GreenK<T>& 
     if (w < np) {
         const int p = p0 + w, ky = a.dnh.div(p), kz = p - ky * nh;
         C2<T>* col = tile + w;
+        WarpTw<T, E> wt;
+        wt.init(tw, lane);
         C2<T> v[6][E];
 #pragma unroll
         for (int c = 0; c < 6; c++)
 #pragma unroll
             for (int q = 0; q < E; q++) v[c][q] = col[(c * n + lane + 32 * q) * XW_ROW];
 #pragma unroll
-        for (int c = 0; c < 6; c++) warp_fft<T, E, -1>(v[c], tw, lane);
+        for (int c = 0; c < 6; c++) warp_fft<T, E, -1>(v[c], wt);
         // lane l holds kx = k2 + E brev5(l) in v[.][k2]; du goes to the lane's
         // own slots, which its inverse transforms read back in that order
         const int kb = E * brev5(lane);
@@ -239,7 +241,7 @@ __device__ __forceinline__ void x_warp_body(const XArgs<T>& a, const GreenK<T>& 
             C2<T> u[E];
 #pragma unroll
             for (int q = 0; q < E; q++) u[q] = col[(c * n + lane + 32 * q) * XW_ROW];
-            warp_ifft_brev<T, E>(u, tw, lane);
+            warp_ifft_brev<T, E>(u, wt);
 #pragma unroll
             for (int q = 0; q < E; q++) col[(c * n + lane + 32 * q) * XW_ROW] = u[q];
         }
@@ -349,6 +351,9 @@ __device__ __forceinline__ void plane_fwd_body(const PlaneArgs<T>& a, int bid, u
     for (int i = threadIdx.x; i < n; i += blockDim.x) twz[i] = a.twz[i];
     for (int i = threadIdx.x; i < g.n1; i += blockDim.x) twy[i] = a.twy[i];
     __syncthreads();
+    // one set of lane constants serves both axes (n1 == n2)
+    WarpTw<T, E> wt;
+    wt.init(twz, lane);
     const T* sa = a.sig + (size_t)(2 * p) * g.N + (size_t)x * g.n1 * n;
     const T* sb = a.sig + (size_t)(2 * p + 1) * g.N + (size_t)x * g.n1 * n;
     // rows are software-pipelined: the next row's loads are in flight while
@@ -365,7 +370,7 @@ __device__ __forceinline__ void plane_fwd_body(const PlaneArgs<T>& a, int bid, u
         if (yn < g.n1)
 #pragma unroll
             for (int q = 0; q < E; q++) nxt[q] = mk<T>(sa[(size_t)yn * n + lane + 32 * q], sb[(size_t)yn * n + lane + 32 * q]);
-        warp_fft<T, E, -1>(v, twz, lane);
+        warp_fft<T, E, -1>(v, wt);
         const int b = brev5(lane);
 #pragma unroll
         for (int k2 = 0; k2 < E; k2++) R[pskew(k2 + E * b)] = v[k2];
@@ -386,7 +391,7 @@ __device__ __forceinline__ void plane_fwd_body(const PlaneArgs<T>& a, int bid, u
         C2<T> v[E];
 #pragma unroll
         for (int q = 0; q < E; q++) v[q] = S[pskew(lane + 32 * q) * nhp + kz];
-        warp_fft<T, E, -1>(v, twy, lane);
+        warp_fft<T, E, -1>(v, wt);
         const int b = brev5(lane);
 #pragma unroll
         for (int k2 = 0; k2 < E; k2++) S[pskew(k2 + E * b) * nhp + kz] = v[k2];
@@ -439,13 +444,16 @@ __device__ __forceinline__ void plane_inv_body(const PlaneArgs<T>& a, int bid, u
     }
     cp_async_wait_all();
     __syncthreads();
+    // one set of lane constants serves both axes (n1 == n2)
+    WarpTw<T, E> wt;
+    wt.init(twz, lane);
     for (int c = warp; c < (hasb ? 2 : 1) * nh; c += PLANE_WARPS) {
         C2<T>* S = (c < nh) ? SA : SB;
         const int kz = (c < nh) ? c : c - nh;
         C2<T> v[E];
 #pragma unroll
         for (int q = 0; q < E; q++) v[q] = S[pskew(lane + 32 * q) * nhp + kz];
-        warp_fft<T, E, 1>(v, twy, lane);
+        warp_fft<T, E, 1>(v, wt);
         const int b = brev5(lane);
 #pragma unroll
         for (int k2 = 0; k2 < E; k2++) S[pskew(k2 + E * b) * nhp + kz] = v[k2];
@@ -472,7 +480,7 @@ __device__ __forceinline__ void plane_inv_body(const PlaneArgs<T>& a, int bid, u
             if (m < nh) v[q] = mk<T>(u.x - w.y, u.y + w.x);   // u + i w
             else v[q] = mk<T>(u.x + w.y, -u.y + w.x);         // conj u + i conj w
         }
-        warp_fft<T, E, 1>(v, twz, lane);
+        warp_fft<T, E, 1>(v, wt);
         const int b = brev5(lane);
 #pragma unroll
         for (int k2 = 0; k2 < E; k2++) R[pskew(k2 + E * b)] = v[k2];
