@@ -65,6 +65,9 @@ def parse():
     p.add_argument("--serve-requests", type=int, default=24)
     p.add_argument("--serve-rates", default="2,16")
     p.add_argument("--forms", default="batch,serve", help="extra forms to measure ('' for none)")
+    p.add_argument("--no-tune", action="store_true",
+                   help="keep the default spectral schedule (no autotuner trials; for launch-list profiling, "
+                        "where the trial timings are not the kernels' own)")
     return p.parse_args()
 
 
@@ -257,7 +260,8 @@ def batch_leg(a, evpg, root):
     for prec, tag in ((evpg.FP32_BULK, "fp32"), (evpg.FP64, "fp64")):
         jobs = [evpg.Job(c["input"], c["rho0"], precision=prec, nr_mode=evpg.NR_LINESEARCH) for c in cases]
         for j in jobs:
-            j.tune()  # searched once per grid, cached for the others
+            if not a.no_tune:
+                j.tune()  # searched once per grid, cached for the others
         t0 = time.perf_counter()
         its, rounds = evpg.run_batched(jobs, nsteps, max_ticks=32)
         tb = time.perf_counter() - t0
@@ -269,7 +273,8 @@ def batch_leg(a, evpg, root):
         if tag == "fp32":
             jobs = [evpg.Job(c["input"], c["rho0"], precision=prec, nr_mode=evpg.NR_LINESEARCH) for c in cases]
             for j in jobs:
-                j.tune()
+                if not a.no_tune:
+                    j.tune()
             t0 = time.perf_counter()
             its_alone = [[j.increment(k) for k in range(a.batch_steps)] for j in jobs]
             ta = time.perf_counter() - t0
@@ -340,7 +345,7 @@ def gpu_arm(a, ws, rank, local):
 
         # ---------------- FP32 bulk: headline
         j32 = open_job(evpg.FP32_BULK)
-        tune32 = {"gain": j32.tune(), "schedule": j32.schedule()}
+        tune32 = {"gain": None if a.no_tune else j32.tune(), "schedule": j32.schedule()}
         for s in range(a.warmup):
             j32.increment(s)
         barrier(ws)
@@ -397,7 +402,7 @@ def gpu_arm(a, ws, rank, local):
 
         # ---------------- FP64 plain form on the same increments
         j64 = open_job(evpg.FP64)
-        tune64 = {"gain": j64.tune(), "schedule": j64.schedule()}
+        tune64 = {"gain": None if a.no_tune else j64.tune(), "schedule": j64.schedule()}
         for s in range(a.warmup):
             j64.increment(s)
         torch.cuda.synchronize()
