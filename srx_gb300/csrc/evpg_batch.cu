@@ -184,9 +184,9 @@ static cudaError_t build_tables_t(Batch& b) {
     {
         std::vector<ZArgs<T>> z;
         std::vector<YArgs<T>> yf, yi;
-        std::vector<XArgs<T>> x;
-        std::vector<int> gz, gy, gx;
-        size_t smz = 0, smy = 0, smx = 0;
+        std::vector<XArgs<T>> x, xw[3];
+        std::vector<int> gz, gy, gx, gxw[3];
+        size_t smz = 0, smy = 0, smx = 0, smxw[3] = {0, 0, 0};
         // every slot runs the spectral variant it runs alone: the fused z+y
         // plane kernels (one table per lane layout) or the separate passes
         std::vector<PlaneArgs<T>> pa[3];
@@ -194,9 +194,18 @@ static cudaError_t build_tables_t(Batch& b) {
         size_t smp[3] = {0, 0, 0};
         for (Ctx* c : b.slots) {
             const SpecSet<T>& s = sset<T>(*c);
-            x.push_back(s.x); x.back().gate = GATE_RUNNING;
-            gx.push_back(s.grid_x);
-            if (s.sm_x > smx) smx = s.sm_x;
+            if (s.xw) {
+                const int q = s.xw == 1 ? 0 : s.xw == 2 ? 1 : 2;
+                xw[q].push_back(s.x);
+                xw[q].back().gate = GATE_RUNNING;
+                gxw[q].push_back(s.grid_xw);
+                if (s.sm_xw > smxw[q]) smxw[q] = s.sm_xw;
+            } else {
+                x.push_back(s.x);
+                x.back().gate = GATE_RUNNING;
+                gx.push_back(s.grid_x);
+                if (s.sm_x > smx) smx = s.sm_x;
+            }
             if (s.epl) {
                 const int q = s.epl == 1 ? 0 : s.epl == 2 ? 1 : 2;
                 pa[q].push_back(s.pl);
@@ -221,6 +230,7 @@ static cudaError_t build_tables_t(Batch& b) {
         if (e == cudaSuccess) e = put_table(b, BL_YF, yf, gy, smy);
         if (e == cudaSuccess) e = put_table(b, BL_YI, yi, gy, smy);
         if (e == cudaSuccess) e = put_table(b, BL_X, x, gx, smx);
+        for (int q = 0; q < 3 && e == cudaSuccess; q++) e = put_table(b, BL_XW1 + q, xw[q], gxw[q], smxw[q]);
     }
     {
         std::vector<NrArgs<T>> nr;

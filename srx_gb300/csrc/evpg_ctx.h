@@ -122,11 +122,13 @@ struct BatchLaunch {
 };
 enum BatchKind { BL_Z, BL_YF, BL_X, BL_YI, BL_NR, BL_MACRO, BL_MBEGIN, BL_BEGIN, BL_FOLD,
                  BL_REFINE, BL_END, BL_ENDR, BL_PF1, BL_PF2, BL_PF4, BL_PI1, BL_PI2, BL_PI4,
-                 BL_COUNT };
+                 BL_XW1, BL_XW2, BL_XW4, BL_COUNT };
 // Spectral chain of a batch: the separate z and y passes over the slots in
 // BL_Z/BL_YF/BL_YI, the fused plane kernels over the slots in BL_PF*/BL_PI*
-// (1, 2, 4 elements per lane), the X pass over all; launches with no slot are
-// skipped. Returns the number of kernels launched.
+// (1, 2, 4 elements per lane), the X pass as the warp-register kernel over the
+// slots in BL_XW* (1, 2, 4 elements per lane) and the shared-memory kernel over
+// those in BL_X; launches with no slot are skipped. Returns the number of
+// kernels launched.
 int launch_spectral_batch(int precision, const BatchLaunch* L, cudaStream_t st);
 int plane_epl(const Grid& g, size_t elem_bytes);
 // NR sweep, macro update for every slot

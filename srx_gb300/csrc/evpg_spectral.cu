@@ -612,6 +612,27 @@ __global__ void __launch_bounds__(SPEC_THREADS) kb_x_green(const XArgs<T>* __res
     x_green_body<T, true>(a, gks, m.y, smem);
 }
 
+template <typename T, int E>
+__global__ void __launch_bounds__(XW_THREADS) kb_x_warp(const XArgs<T>* __restrict__ tab,
+                                                      const int2* __restrict__ map) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ GreenK<T> gks;
+    const int2 m = map[blockIdx.x];
+    const XArgs<T>& a = tab[m.x];
+    if (!gate_open(a.macro, a.gate)) return;
+    const T* src = &a.gk.c0[0][0][0][0];
+    T* dst = &gks.c0[0][0][0][0];
+    for (int i = threadIdx.x; i < 162; i += blockDim.x) dst[i] = src[i];
+    if (threadIdx.x == 0) {
+        gks.elast_bc = a.gk.elast_bc;
+        gks.rn[0] = a.gk.rn[0];
+        gks.rn[1] = a.gk.rn[1];
+        gks.rn[2] = a.gk.rn[2];
+    }
+    __syncthreads();
+    x_warp_body<T, E, true>(a, gks, m.y, smem);
+}
+
 template <typename T>
 __global__ void __launch_bounds__(SPEC_THREADS) kb_inv_z(const ZArgs<T>* __restrict__ tab,
                                                          const int2* __restrict__ map) {
@@ -802,6 +823,9 @@ template <typename T> static void spec_attributes() {
     cudaFuncSetAttribute(k_x_warp<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
     cudaFuncSetAttribute(k_x_warp<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
     cudaFuncSetAttribute(k_x_warp<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(kb_x_warp<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx - 2048);
+    cudaFuncSetAttribute(kb_x_warp<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx - 2048);
+    cudaFuncSetAttribute(kb_x_warp<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx - 2048);
     cudaFuncSetAttribute(k_plane_fwd<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
     cudaFuncSetAttribute(k_plane_fwd<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
     cudaFuncSetAttribute(k_plane_fwd<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
@@ -916,8 +940,19 @@ static int spectral_batch_t(const BatchLaunch* L, cudaStream_t st) {
         kb_y<T, -1><<<yf.nblk, SPEC_THREADS, yf.smem, st>>>((const YArgs<T>*)yf.tab, yf.map);
         n += 2;
     }
-    kb_x_green<T><<<x.nblk, SPEC_THREADS, x.smem, st>>>((const XArgs<T>*)x.tab, x.map);
-    n++;
+    for (int q = 0; q < 3; q++) {
+        const BatchLaunch& w = L[BL_XW1 + q];
+        if (!w.nblk) continue;
+        const XArgs<T>* tab = (const XArgs<T>*)w.tab;
+        if (q == 0) kb_x_warp<T, 1><<<w.nblk, XW_THREADS, w.smem, st>>>(tab, w.map);
+        else if (q == 1) kb_x_warp<T, 2><<<w.nblk, XW_THREADS, w.smem, st>>>(tab, w.map);
+        else kb_x_warp<T, 4><<<w.nblk, XW_THREADS, w.smem, st>>>(tab, w.map);
+        n++;
+    }
+    if (x.nblk) {
+        kb_x_green<T><<<x.nblk, SPEC_THREADS, x.smem, st>>>((const XArgs<T>*)x.tab, x.map);
+        n++;
+    }
     if (z.nblk) {
         kb_y<T, 1><<<yi.nblk, SPEC_THREADS, yi.smem, st>>>((const YArgs<T>*)yi.tab, yi.map);
         kb_inv_z<T><<<z.nblk, SPEC_THREADS, z.smem, st>>>((const ZArgs<T>*)z.tab, z.map);
