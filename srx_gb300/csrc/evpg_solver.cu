@@ -252,7 +252,7 @@ __device__ __forceinline__ void mat6v(const T (&m)[6][6], const T* x, T* y) {
 // serves both (36 + 21 loads per Newton step become 21).
 template <typename T>
 __device__ __forceinline__ void sgr_v(const T* sg, const T* x, T* y) {
-    if (sizeof(T) == 4) {
+    if constexpr (sizeof(T) == 4) {
         T u[21];
 #pragma unroll
         for (int k = 0; k < 21; k++) u[k] = __ldg(sg + k);
@@ -263,30 +263,30 @@ __device__ __forceinline__ void sgr_v(const T* sg, const T* x, T* y) {
             for (int j = 0; j < 6; j++) s += u[i <= j ? sidx(i, j) : sidx(j, i)] * x[j];
             y[i] = s;
         }
-        return;
-    }
+    } else {
 #pragma unroll
-    for (int i = 0; i < 6; i++) {
-        T s = (T)0;
+        for (int i = 0; i < 6; i++) {
+            T s = (T)0;
 #pragma unroll
-        for (int j = 0; j < 6; j++) s += __ldg(sg + i * 6 + j) * x[j];
-        y[i] = s;
+            for (int j = 0; j < 6; j++) s += __ldg(sg + i * 6 + j) * x[j];
+            y[i] = s;
+        }
     }
 }
 
 // Packed base of the NR matrix, S066 + sym(S_gr), of the voxel's orientation.
 template <typename T>
 __device__ __forceinline__ void nr_matrix_base(const T* sg, const T (&S66)[6][6], T (&m)[21]) {
-    if (sizeof(T) == 4) {
+    if constexpr (sizeof(T) == 4) {
 #pragma unroll
         for (int i = 0; i < 6; i++)
 #pragma unroll
             for (int j = 0; j < 6; j++)
                 if (j >= i) m[sidx(i, j)] = S66[i][j] + __ldg(sg + sidx(i, j));
-        return;
-    }
+    } else {
 #pragma unroll
-    for (int k = 0; k < 21; k++) m[k] = __ldg(sg + 36 + k);
+        for (int k = 0; k < 21; k++) m[k] = __ldg(sg + 36 + k);
+    }
 }
 
 // Warp-level partial sums without a block barrier: every warp writes its own
@@ -971,13 +971,86 @@ __device__ __forceinline__ void forest_parallel_gnd(const PhaseK<double>& P, con
     }
 }
 
+// update_schmid and the flow-rule constants of one voxel (constitutive.c:
+// 585-692 prefixes), in arithmetic type R: FP64, or FP32 for the FP32-bulk
+// form, whose FP64 copies are then its FP32 values widened.
+template <typename R>
+__device__ __forceinline__ void begin_rates(const BeginArgs& a, int v, int ph, const PhaseK<R>& P) {
+    const int N = a.g.N;
+    const R drx = (R)a.macro->ctl.drx;
+    R Rm[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) Rm[i][j] = (R)a.tranmat[(size_t)(3 * i + j) * N + v];
+    for (int s = 0; s < P.n_sys; s++) {
+        // R sym(n (x) b) R^T = sym(Rn (x) Rb): the rotated Schmid tensor from the
+        // rotated slip normal and direction (kinematics.c:430-463 rotates the
+        // tensor of Schm_xt, which is sym(n (x) b), init.c:205-212)
+        R bs[3], ns[3], w[3][3];
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+            bs[i] = Rm[i][0] * P.bb[s][0] + Rm[i][1] * P.bb[s][1] + Rm[i][2] * P.bb[s][2];
+            ns[i] = Rm[i][0] * P.bn[s][0] + Rm[i][1] * P.bn[s][1] + Rm[i][2] * P.bn[s][2];
+        }
+#pragma unroll
+        for (int i = 0; i < 3; i++) w[i][i] = ns[i] * bs[i];
+        w[1][2] = w[2][1] = (R)0.5 * (ns[1] * bs[2] + ns[2] * bs[1]);
+        w[0][2] = w[2][0] = (R)0.5 * (ns[0] * bs[2] + ns[2] * bs[0]);
+        w[0][1] = w[1][0] = (R)0.5 * (ns[0] * bs[1] + ns[1] * bs[0]);
+        R o6[6];
+        sym_to_b6<R>(w, o6);
+#pragma unroll
+        for (int q = 0; q < 5; q++) {
+            a.schm64[(size_t)(s * 5 + q) * N + v] = (double)o6[q];
+            if (a.schm32) a.schm32[(size_t)(s * 5 + q) * N + v] = (float)o6[q];
+        }
+    }
+    R rs[NS];
+#pragma unroll
+    for (int i = 0; i < NS; i++) rs[i] = (i < P.n_sys) ? (R)a.rho_s[(size_t)i * N + v] : (R)0;
+    // GND densities enter the FP64 form of the constants only (an FP32-bulk
+    // context with GND computes them in FP64)
+    double g1[NS], g2[NS];
+    const double* gp = a.rho_g ? a.gproj + (size_t)(ph - 1) * GP_STRIDE : nullptr;
+    if constexpr (sizeof(R) == 8)
+        if (gp) load_gnd(a.rho_g, N, v, P.n_sys, g1, g2);
+    for (int i = 0; i < P.n_sys; i++) {
+        R rP = (R)0, rf = (R)0;
+        bool done = false;
+        if constexpr (sizeof(R) == 8)
+            if (gp) {
+                forest_parallel_gnd(P, gp, i, rs, g1, g2, rP, rf);
+                done = true;
+            }
+        if (!done) {
+#pragma unroll
+            for (int j = 0; j < NS; j++) {
+                rP += P.chi[i][j] * rs[j];
+                rf += P.chi1[i][j] * rs[j];
+            }
+        }
+        const R rm_stale = (R)a.rho_m[(size_t)i * N + v];
+        const R rm = P.k_rhom[i] * sqrt(rP * rf);
+        const R tp = P.k_tpass[i] * sqrt(fabs(rP + rm)) + drx;
+        const R tps = P.k_tpass[i] * sqrt(fabs(rP + rm_stale)) + drx;
+        const R itc = (R)1 / (P.tau0 + P.k_tcut[i] * sqrt(rf));
+        const R go = P.k_gamo[i] * rm / sqrt(rf);
+        const R f4[4] = {tp, itc, go, tps};
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            a.fc64[(size_t)(12 * q + i) * N + v] = (double)f4[q];
+            if (a.fc32) a.fc32[(size_t)(12 * q + i) * N + v] = (float)f4[q];
+        }
+    }
+}
+
 __device__ __forceinline__ void begin_body(const BeginArgs& a, int bid) {
     const int v = bid * 128 + threadIdx.x;
     const int N = a.g.N;
     if (v >= N) return;
     const IncrCtl& ctl = a.macro->ctl;
     const int creep = ctl.creep;
-    const double drx = ctl.drx;
 #pragma unroll
     for (int c = 0; c < 9; c++) {
         const double d = a.dg64[(size_t)c * N + v];
@@ -995,65 +1068,9 @@ __device__ __forceinline__ void begin_body(const BeginArgs& a, int bid) {
 #pragma unroll
         for (int c = 6; c < 9; c++) a.ddg32[(size_t)c * N + v] = 0.0f;
     }
-    if (!P.crystal) return;
-    double R[3][3];
-#pragma unroll
-    for (int i = 0; i < 3; i++)
-#pragma unroll
-        for (int j = 0; j < 3; j++) R[i][j] = a.tranmat[(size_t)(3 * i + j) * N + v];
-    for (int s = 0; s < P.n_sys; s++) {
-        // R sym(n (x) b) R^T = sym(Rn (x) Rb): the rotated Schmid tensor from the
-        // rotated slip normal and direction (kinematics.c:430-463 rotates the
-        // tensor of Schm_xt, which is sym(n (x) b), init.c:205-212)
-        double bs[3], ns[3], w[3][3];
-#pragma unroll
-        for (int i = 0; i < 3; i++) {
-            bs[i] = R[i][0] * P.bb[s][0] + R[i][1] * P.bb[s][1] + R[i][2] * P.bb[s][2];
-            ns[i] = R[i][0] * P.bn[s][0] + R[i][1] * P.bn[s][1] + R[i][2] * P.bn[s][2];
-        }
-#pragma unroll
-        for (int i = 0; i < 3; i++) w[i][i] = ns[i] * bs[i];
-        w[1][2] = w[2][1] = 0.5 * (ns[1] * bs[2] + ns[2] * bs[1]);
-        w[0][2] = w[2][0] = 0.5 * (ns[0] * bs[2] + ns[2] * bs[0]);
-        w[0][1] = w[1][0] = 0.5 * (ns[0] * bs[1] + ns[1] * bs[0]);
-        double o6[6];
-        sym_to_b6<double>(w, o6);
-#pragma unroll
-        for (int q = 0; q < 5; q++) {
-            a.schm64[(size_t)(s * 5 + q) * N + v] = o6[q];
-            if (a.schm32) a.schm32[(size_t)(s * 5 + q) * N + v] = (float)o6[q];
-        }
-    }
-    double rs[NS];
-#pragma unroll
-    for (int i = 0; i < NS; i++) rs[i] = (i < P.n_sys) ? a.rho_s[(size_t)i * N + v] : 0.0;
-    double g1[NS], g2[NS];
-    const double* gp = a.rho_g ? a.gproj + (size_t)(ph - 1) * GP_STRIDE : nullptr;
-    if (gp) load_gnd(a.rho_g, N, v, P.n_sys, g1, g2);
-    for (int i = 0; i < P.n_sys; i++) {
-        double rP = 0.0, rf = 0.0;
-        if (gp) {
-            forest_parallel_gnd(P, gp, i, rs, g1, g2, rP, rf);
-        } else {
-#pragma unroll
-            for (int j = 0; j < NS; j++) {
-                rP += P.chi[i][j] * rs[j];
-                rf += P.chi1[i][j] * rs[j];
-            }
-        }
-        const double rm_stale = a.rho_m[(size_t)i * N + v];
-        const double rm = P.k_rhom[i] * sqrt(rP * rf);
-        const double tp = P.k_tpass[i] * sqrt(fabs(rP + rm)) + drx;
-        const double tps = P.k_tpass[i] * sqrt(fabs(rP + rm_stale)) + drx;
-        const double itc = 1.0 / (P.tau0 + P.k_tcut[i] * sqrt(rf));
-        const double go = P.k_gamo[i] * rm / sqrt(rf);
-        const double f4[4] = {tp, itc, go, tps};
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-            a.fc64[(size_t)(12 * q + i) * N + v] = f4[q];
-            if (a.fc32) a.fc32[(size_t)(12 * q + i) * N + v] = (float)f4[q];
-        }
-    }
+    if (!a.mat.ph[ph - 1].crystal) return;
+    if (a.rates32 && !a.rho_g) begin_rates<float>(a, v, ph, a.ph32[ph - 1]);
+    else begin_rates<double>(a, v, ph, P);
 }
 
 __global__ void __launch_bounds__(128) k_begin(const __grid_constant__ BeginArgs a) {
@@ -1118,6 +1135,31 @@ __device__ void reorient(double tran[3][3], const double rot[3][3]) {
         for (int j = 0; j < 3; j++) tran[i][j] = tn[i][j];
 }
 
+// The same update from an FP32 rotation increment: the small part
+// D = 2 (om + om^2) / (1 + wt^2) of r = I + D in FP32, tran += D tran with the
+// sum in FP64 (D is of the order of the rotation, so its FP32 rounding is far
+// below the FP64 resolution of tran's entries).
+__device__ void reorient(double tran[3][3], const float rot[3][3]) {
+    float w[3] = {rot[2][1], rot[0][2], rot[1][0]};
+    float wn = sqrtf(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+    float wt = tanf(wn / 2.0f);
+    if (fabsf(wn) < 1E-6f) wn = 1.0f;
+    for (int i = 0; i < 3; i++) w[i] *= wt / wn;
+    const float om[3][3] = {{0.f, -w[2], w[1]}, {w[2], 0.f, -w[0]}, {-w[1], w[0], 0.f}};
+    float d[3][3];
+    const float sc = 2.f / (1.f + wt * wt);
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++)
+            d[i][j] = sc * (om[i][j] + om[i][0] * om[0][j] + om[i][1] * om[1][j] + om[i][2] * om[2][j]);
+    double tn[3][3];
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++)
+            tn[i][j] = tran[i][j] + (double)(d[i][0] * (float)tran[0][j] + d[i][1] * (float)tran[1][j] +
+                                             d[i][2] * (float)tran[2][j]);
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) tran[i][j] = tn[i][j];
+}
+
 // One directional derivative of Gradient_ShearRate (constitutive.c:881-1112)
 // from the same-grain bits of the plus and minus neighbours: backward,
 // forward or central difference, zero with no neighbour in the grain.
@@ -1142,21 +1184,164 @@ __device__ __forceinline__ void slip_rate_gradient(const EndArgs& a, int v, int 
     gr[2] = gb_diff(gd[v], gd[(x * n1 + y) * n2 + zp], gd[(x * n1 + y) * n2 + zm], m & 16u, m & 32u);
 }
 
-__device__ __forceinline__ void end_body(const EndArgs& a, int bid) {
-    const int v = bid * END_BLOCK + threadIdx.x;
-    const int reorient_on = a.macro->ctl.tail & 1;
-    const int grad_on = a.macro->ctl.tail & 2;
+// update_orient and DislocationEvolution of one crystal voxel in arithmetic
+// type R (FP64, or FP32 for the FP32-bulk form without GND: the rates in
+// FP32, the state updates -- rho_s, gam_acum, the orientation -- added in
+// FP64). q: the block's partial sums.
+template <typename R>
+__device__ __forceinline__ void end_crystal(const EndArgs& a, int v, int ph, const PhaseK<R>& P, const double (&vg)[9],
+                                            double (&q)[NPART_END]) {
     const int N = a.g.N;
     const double dt = a.mat.dt;
+    const int reorient_on = a.macro->ctl.tail & 1;
+    const int grad_on = a.macro->ctl.tail & 2;
+    R gd[NS];
+#pragma unroll
+    for (int i = 0; i < NS; i++) gd[i] = (i < P.n_sys) ? (R)a.gamdot[(size_t)i * N + v] : (R)0;
+    if (reorient_on) {
+        // update_orient (constitutive.c:196-273)
+        double tr[3][3];
+        R trr[3][3], Lp[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, rot[3][3];
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) {
+                tr[i][j] = a.tranmat[(size_t)(3 * i + j) * N + v];
+                trr[i][j] = (R)tr[i][j];
+            }
+        for (int s = 0; s < P.n_sys; s++) {
+            R bs[3], ns[3];
+            for (int i = 0; i < 3; i++) {
+                bs[i] = trr[i][0] * P.bb[s][0] + trr[i][1] * P.bb[s][1] + trr[i][2] * P.bb[s][2];
+                ns[i] = trr[i][0] * P.bn[s][0] + trr[i][1] * P.bn[s][1] + trr[i][2] * P.bn[s][2];
+            }
+            for (int i = 0; i < 3; i++)
+                for (int j = 0; j < 3; j++) Lp[i][j] += bs[i] * ns[j] * gd[s];
+        }
+        // antisymmetric VelGrad: A12 = vg[6], A13 = vg[7], A23 = vg[8]
+        const R rl[3][3] = {{(R)0, (R)vg[6], (R)vg[7]}, {-(R)vg[6], (R)0, (R)vg[8]}, {-(R)vg[7], -(R)vg[8], (R)0}};
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++)
+                rot[i][j] = ((R)a.udot_a[i][j] + rl[i][j] - (Lp[i][j] - Lp[j][i]) / (R)2) * (R)dt;
+        reorient(tr, rot);
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) a.tranmat[(size_t)(3 * i + j) * N + v] = tr[i][j];
+    }
+    // DislocationEvolution (constitutive.c:1373-1426), with rho_F and
+    // rho_m of the increment's flow-rule calls and the stored rho_m
+    // (the value before this increment) in rho_tot.
+    double rs64[NS];
+    R rs[NS], rf[NS], rP[NS], rm[NS], rtot = (R)0;
+#pragma unroll
+    for (int i = 0; i < NS; i++) {
+        rs64[i] = (i < P.n_sys) ? a.rho_s[(size_t)i * N + v] : 0.0;
+        rs[i] = (R)rs64[i];
+    }
+    // GND densities before this increment's update (the flow rule's
+    // trial values and rho_tot, evolution.c:1041-1045); FP64 form only
+    double g1[NS], g2[NS];
+    const double* gp = a.rho_g ? a.gproj + (size_t)(ph - 1) * GP_STRIDE : nullptr;
+    if constexpr (sizeof(R) == 8)
+        if (gp) load_gnd(a.rho_g, N, v, P.n_sys, g1, g2);
+    for (int i = 0; i < P.n_sys; i++) {
+        R x = (R)0, y = (R)0;
+        bool done = false;
+        if constexpr (sizeof(R) == 8)
+            if (gp) {
+                forest_parallel_gnd(P, gp, i, rs, g1, g2, x, y);
+                done = true;
+            }
+        if (!done) {
+#pragma unroll
+            for (int j = 0; j < NS; j++) {
+                x += P.chi[i][j] * rs[j];
+                y += P.chi1[i][j] * rs[j];
+            }
+        }
+        rP[i] = x;
+        rf[i] = y;
+        rm[i] = P.k_rhom[i] * sqrt(x * y);
+        const R rmo = (R)a.rho_m[(size_t)i * N + v];
+        if constexpr (sizeof(R) == 8)
+            rtot += gp ? rs[i] + rmo + sqrt(g1[i] * g1[i] + g2[i] * g2[i]) : rs[i] + rmo;
+        else
+            rtot += rs[i] + rmo;
+    }
+    R s6[6];
+#pragma unroll
+    for (int c = 0; c < 6; c++) s6[c] = (R)a.sig64[(size_t)c * N + v];
+    const R eqb = exp(-(R)1 * P.q_bulk);
+    const R dtr = (R)dt;
+    // the voxel's sums of q[0, 1, 3..6] in type R (q[2] takes the FP64 rho_s)
+    R qa[7] = {(R)0, (R)0, (R)0, (R)0, (R)0, (R)0, (R)0};
+    for (int i = 0; i < P.n_sys; i++) {
+        // Schmid vectors: the FP32 copy in the FP32 form (its FP64 copy is the
+        // same values widened)
+        R sc[5];
+#pragma unroll
+        for (int k = 0; k < 5; k++) {
+            if constexpr (sizeof(R) == 4) sc[k] = a.schm32[(size_t)(i * 5 + k) * N + v];
+            else sc[k] = a.schm64[(size_t)(i * 5 + k) * N + v];
+        }
+        const R rss = sc[0] * s6[0] + sc[1] * s6[1] + sc[2] * s6[2] + sc[3] * s6[3] + sc[4] * s6[4];
+        const R b = P.burgers[i];
+        const R den = fabs(rss) + (R)1.0E-4;
+        const R ddip = P.k_ddip[i] / den;
+        const R hyd = P.k_hydr[i] * den;  // k_hyd / ddip
+        const R clim = (R)1E-17 * rtot * (R)0.5 * (R)1E24 * ddip * P.k_d0b[i] * (rs[i] * rs[i]) *
+                       (exp(fabs(hyd) * P.k_hexp[i]) - (R)1) * eqb;
+        const R ag = fabs(gd[i]);
+        const R sq = sqrt(rf[i]);
+        qa[4] += clim * dtr;
+        qa[5] += ag * (P.c4 * sq) * dtr;
+        qa[6] += ag * (P.c5 * rs[i]) * dtr;
+        const R dot = ag * (P.c4 * sq + P.c6 * ddip * rm[i] - P.c5 * rs[i]) - clim;
+        // the state update in FP64 (the same expression in the FP64 form)
+        const double rn = rs64[i] + (double)dot * dt;
+        a.rho_s[(size_t)i * N + v] = rn;
+        a.rho_m[(size_t)i * N + v] = (double)rm[i];
+        a.gam_acum[(size_t)i * N + v] += (double)gd[i] * dt;
+        if constexpr (sizeof(R) == 8)
+            if (gp) {
+                // first-order GND rates (constitutive.c:1428-1522): screw
+                // grad(gamdot).p / b / L0, edge type I -grad(gamdot).b / b / L0
+                double gr[3] = {0.0, 0.0, 0.0};
+                if (grad_on) slip_rate_gradient(a, v, i, gr);
+                const double* bp = gp + GP_BP + 3 * i;
+                const double d1 = (gr[0] * bp[0] + gr[1] * bp[1] + gr[2] * bp[2]) / b / a.l0;
+                const double d2 =
+                    -1.0 * (gr[0] * P.bb[i][0] + gr[1] * P.bb[i][1] + gr[2] * P.bb[i][2]) / b / a.l0;
+                const double n1 = g1[i] + d1 * dt, n2 = g2[i] + d2 * dt;
+                a.rho_g[(size_t)i * N + v] = n1;
+                a.rho_g[(size_t)(NS + i) * N + v] = n2;
+                q[18] += sqrt(n1 * n1 + n2 * n2);
+            }
+        qa[0] += rf[i];
+        qa[1] += rP[i];
+        q[2] += rn;
+        qa[3] += rm[i];
+    }
+    q[0] += (double)qa[0];
+    q[1] += (double)qa[1];
+#pragma unroll
+    for (int k = 3; k < 7; k++) q[k] += (double)qa[k];
+}
+
+__device__ __forceinline__ void end_body(const EndArgs& a, int bid) {
+    const int v = bid * END_BLOCK + threadIdx.x;
+    const int N = a.g.N;
+    const double dt = a.mat.dt;
+    const bool r32 = a.rates32 && !a.rho_g;
     double q[NPART_END];
 #pragma unroll
     for (int i = 0; i < NPART_END; i++) q[i] = 0.0;
     if (v < N) {
-        // VelGrad = (DisGrad - DisGrad_old)/dt (evolution.c:1268-1272)
+        // VelGrad = (DisGrad - DisGrad_old)/dt (evolution.c:1268-1272); the
+        // FP32-bulk form multiplies by 1/dt
         double vg[9];
+        const double idt = 1.0 / dt;
 #pragma unroll
         for (int c = 0; c < 9; c++) {
-            vg[c] = (a.dg64[(size_t)c * N + v] - a.dg_old[(size_t)c * N + v]) / dt;
+            const double d = a.dg64[(size_t)c * N + v] - a.dg_old[(size_t)c * N + v];
+            vg[c] = r32 ? d * idt : d / dt;
             a.dg_old[(size_t)c * N + v] = vg[c];
         }
         // Eps += Edot dt (evolution.c:1297-1301)
@@ -1175,105 +1360,9 @@ __device__ __forceinline__ void end_body(const EndArgs& a, int bid) {
 #pragma unroll
             for (int c = 0; c < 6; c++) a.sig32[(size_t)c * N + v] = (float)a.sig64[(size_t)c * N + v];
         const int ph = a.phase[v];
-        const PhaseK<double>& P = a.mat.ph[ph - 1];
-        if (P.crystal) {
-            double gd[NS];
-#pragma unroll
-            for (int i = 0; i < NS; i++) gd[i] = (i < P.n_sys) ? a.gamdot[(size_t)i * N + v] : 0.0;
-            if (reorient_on) {
-                // update_orient (constitutive.c:196-273)
-                double tr[3][3], Lp[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, rot[3][3];
-                for (int i = 0; i < 3; i++)
-                    for (int j = 0; j < 3; j++) tr[i][j] = a.tranmat[(size_t)(3 * i + j) * N + v];
-                for (int s = 0; s < P.n_sys; s++) {
-                    double bs[3], ns[3];
-                    for (int i = 0; i < 3; i++) {
-                        bs[i] = tr[i][0] * P.bb[s][0] + tr[i][1] * P.bb[s][1] + tr[i][2] * P.bb[s][2];
-                        ns[i] = tr[i][0] * P.bn[s][0] + tr[i][1] * P.bn[s][1] + tr[i][2] * P.bn[s][2];
-                    }
-                    for (int i = 0; i < 3; i++)
-                        for (int j = 0; j < 3; j++) Lp[i][j] += bs[i] * ns[j] * gd[s];
-                }
-                // antisymmetric VelGrad: A12 = vg[6], A13 = vg[7], A23 = vg[8]
-                const double rl[3][3] = {{0.0, vg[6], vg[7]}, {-vg[6], 0.0, vg[8]}, {-vg[7], -vg[8], 0.0}};
-                for (int i = 0; i < 3; i++)
-                    for (int j = 0; j < 3; j++)
-                        rot[i][j] = (a.udot_a[i][j] + rl[i][j] - (Lp[i][j] - Lp[j][i]) / 2.) * dt;
-                reorient(tr, rot);
-                for (int i = 0; i < 3; i++)
-                    for (int j = 0; j < 3; j++) a.tranmat[(size_t)(3 * i + j) * N + v] = tr[i][j];
-            }
-            // DislocationEvolution (constitutive.c:1373-1426), with rho_F and
-            // rho_m of the increment's flow-rule calls and the stored rho_m
-            // (the value before this increment) in rho_tot.
-            double rs[NS], rf[NS], rP[NS], rm[NS], rtot = 0.0;
-#pragma unroll
-            for (int i = 0; i < NS; i++) rs[i] = (i < P.n_sys) ? a.rho_s[(size_t)i * N + v] : 0.0;
-            // GND densities before this increment's update (the flow rule's
-            // trial values and rho_tot, evolution.c:1041-1045)
-            double g1[NS], g2[NS];
-            const double* gp = a.rho_g ? a.gproj + (size_t)(ph - 1) * GP_STRIDE : nullptr;
-            if (gp) load_gnd(a.rho_g, N, v, P.n_sys, g1, g2);
-            for (int i = 0; i < P.n_sys; i++) {
-                double x = 0.0, y = 0.0;
-                if (gp) {
-                    forest_parallel_gnd(P, gp, i, rs, g1, g2, x, y);
-                } else {
-#pragma unroll
-                    for (int j = 0; j < NS; j++) {
-                        x += P.chi[i][j] * rs[j];
-                        y += P.chi1[i][j] * rs[j];
-                    }
-                }
-                rP[i] = x;
-                rf[i] = y;
-                rm[i] = P.k_rhom[i] * sqrt(x * y);
-                rtot += gp ? rs[i] + a.rho_m[(size_t)i * N + v] + sqrt(g1[i] * g1[i] + g2[i] * g2[i])
-                           : rs[i] + a.rho_m[(size_t)i * N + v];
-            }
-            double s6[6];
-#pragma unroll
-            for (int c = 0; c < 6; c++) s6[c] = a.sig64[(size_t)c * N + v];
-            const double eqb = exp(-1.0 * P.q_bulk);
-            for (int i = 0; i < P.n_sys; i++) {
-                const double* sc = a.schm64 + (size_t)(i * 5) * N + v;
-                const double rss = sc[0] * s6[0] + sc[(size_t)N] * s6[1] + sc[2 * (size_t)N] * s6[2] +
-                                   sc[3 * (size_t)N] * s6[3] + sc[4 * (size_t)N] * s6[4];
-                const double b = P.burgers[i];
-                const double den = fabs(rss) + 1.0E-4;
-                const double ddip = P.k_ddip[i] / den;
-                const double hyd = P.k_hydr[i] * den;  // k_hyd / ddip
-                const double clim = 1E-17 * rtot * 0.5 * 1E24 * ddip * P.k_d0b[i] * (rs[i] * rs[i]) *
-                                    (exp(fabs(hyd) * P.k_hexp[i]) - 1.0) * eqb;
-                const double ag = fabs(gd[i]);
-                const double sq = sqrt(rf[i]);
-                q[4] += clim * dt;
-                q[5] += ag * (P.c4 * sq) * dt;
-                q[6] += ag * (P.c5 * rs[i]) * dt;
-                const double dot = ag * (P.c4 * sq + P.c6 * ddip * rm[i] - P.c5 * rs[i]) - clim;
-                const double rn = rs[i] + dot * dt;
-                a.rho_s[(size_t)i * N + v] = rn;
-                a.rho_m[(size_t)i * N + v] = rm[i];
-                a.gam_acum[(size_t)i * N + v] += gd[i] * dt;
-                if (gp) {
-                    // first-order GND rates (constitutive.c:1428-1522): screw
-                    // grad(gamdot).p / b / L0, edge type I -grad(gamdot).b / b / L0
-                    double gr[3] = {0.0, 0.0, 0.0};
-                    if (grad_on) slip_rate_gradient(a, v, i, gr);
-                    const double* bp = gp + GP_BP + 3 * i;
-                    const double d1 = (gr[0] * bp[0] + gr[1] * bp[1] + gr[2] * bp[2]) / b / a.l0;
-                    const double d2 =
-                        -1.0 * (gr[0] * P.bb[i][0] + gr[1] * P.bb[i][1] + gr[2] * P.bb[i][2]) / b / a.l0;
-                    const double n1 = g1[i] + d1 * dt, n2 = g2[i] + d2 * dt;
-                    a.rho_g[(size_t)i * N + v] = n1;
-                    a.rho_g[(size_t)(NS + i) * N + v] = n2;
-                    q[18] += sqrt(n1 * n1 + n2 * n2);
-                }
-                q[0] += rf[i];
-                q[1] += rP[i];
-                q[2] += rn;
-                q[3] += rm[i];
-            }
+        if (a.mat.ph[ph - 1].crystal) {
+            if (r32) end_crystal<float>(a, v, ph, a.ph32[ph - 1], vg, q);
+            else end_crystal<double>(a, v, ph, a.mat.ph[ph - 1], vg, q);
         }
     }
     block_reduce_store<NPART_END>(q, a.part + (size_t)bid * NPART_END);
@@ -1379,6 +1468,8 @@ void build_solver_sets(Ctx& c) {
     b.rho_m = c.rho_m; b.phase = c.phase; b.schm64 = c.schm64; b.fc64 = c.fc64;
     b.schm32 = c.schm32; b.fc32 = c.fc32; b.b6_32 = c.b6_32; b.ddg32 = c.ddg32; b.epsp = c.epsp;
     b.rho_g = c.rho_g; b.gproj = c.gproj;
+    b.rates32 = c.precision != 0;
+    for (int p = 0; p < 2; p++) b.ph32[p] = c.m32.ph[p];
     k.grid_begin = (c.g.N + 127) / 128;
     FoldArgs& f = k.fold;
     f.g = c.g; f.macro = c.macro; f.gate = GATE_ENDING; f.dg64 = c.dg64; f.ddg32 = c.ddg32;
@@ -1393,6 +1484,9 @@ void build_solver_sets(Ctx& c) {
     e.gam_acum = c.gam_acum; e.sig64 = c.sig64; e.schm64 = c.schm64; e.phase = c.phase;
     e.sig32 = c.sig32; e.part = c.part_end;
     e.rho_g = c.rho_g; e.gproj = c.gproj; e.gbm = c.gbm; e.l0 = c.l0;
+    e.rates32 = c.precision != 0;
+    e.schm32 = c.schm32;
+    for (int p = 0; p < 2; p++) e.ph32[p] = c.m32.ph[p];
     k.grid_end = c.nb_end;
     EndReduceArgs& r = k.endr;
     r.macro = c.macro; r.gate = GATE_ENDING; r.part = c.part_end; r.nblocks = c.nb_end; r.wgt = c.cfg.wgt;
