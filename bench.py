@@ -45,7 +45,7 @@ METRIC = "voxel-iters/s 128^3 FP32-bulk vs FP64 (<=1e-4 sigma err)"
 # dram__bytes_read.sum + dram__bytes_write.sum of one FP32 NR sweep per voxel, from an
 # ncu capture of the 96^3 / 422-grain case (traffic grows with N: every voxel's state is
 # read and written once); scaled by N for the roofline's "traffic".
-NR_DRAM_BYTES_PER_VOXEL = 488.5
+NR_DRAM_BYTES_PER_VOXEL = 487.8
 UNIT = "voxel-iterations/s"
 
 
@@ -447,7 +447,7 @@ def gpu_arm(a, ws, rank, local):
            "nr": N * ((6 + 6 + 6 + 60 + 36 + 6) * 4 + 8)}
     # DRAM bytes per voxel of one launch, from one ncu capture of the kernel
     # (dram__bytes_read.sum + dram__bytes_write.sum on the 96^3 RVE, scaled
-    # by voxels; profiles/k_nr_x_green_inv_z_fp32_96cube.md)
+    # by voxels; profiles/k_nr_fp32_96cube.md)
     traffic_per_voxel = {"nr": NR_DRAM_BYTES_PER_VOXEL}
     for k, b in alg.items():
         if prof[k]["ms_per_launch"]:
