@@ -135,13 +135,24 @@ __device__ __forceinline__ void flow_eval(const NrArgs<T>& a, int nsys, int v, c
 #pragma unroll
     for (int q = 0; q < 15; q++) dd[q] = (T)0;
     unsigned act = 0;
-#pragma unroll 1
-    for (int i = 0; i < nsys; i++) {
+    auto pass1 = [&](int i) {
         T sc[5];
         const T rss = resolved_shear<T>(cs, s, i, sc);
         const T tp = stale ? __ldg(a.fc + (size_t)(36 + i) * N + v) : cs[(60 + i) * NR_BLOCK];
         if (fabs(rss) > tp) act |= 1u << i;
         if (gam) gam[i * NR_BLOCK] = (T)0;  // only sweeps that output gamdot keep them
+    };
+    // FP32: unrolled over the system bound (the loop overhead was a sixth of
+    // the pass); FP64 keeps it rolled (its registers are at the limit)
+    if constexpr (sizeof(T) == 4) {
+#pragma unroll
+        for (int i = 0; i < NS; i++) {
+            if (i >= nsys) break;
+            pass1(i);
+        }
+    } else {
+#pragma unroll 1
+        for (int i = 0; i < nsys; i++) pass1(i);
     }
 #pragma unroll 1
     while (act) {
