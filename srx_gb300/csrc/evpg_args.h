@@ -145,10 +145,9 @@ struct BeginArgs {
     // first-order GND densities (nullptr when off): [24][N] rho_g1, rho_g2
     const double* rho_g;
     const double* gproj;  // [2][GP_STRIDE]
-    // FP32 bulk without GND: Schmid vectors and flow constants computed in FP32
-    // from these phase constants (their FP64 copies, for the refinement sweep
-    // and the increment tail, are the FP32 values widened)
-    int rates32;
+    // FP32 bulk without GND (k_begin<float>): Schmid vectors and flow constants
+    // computed in FP32 from these phase constants (their FP64 copies, for the
+    // refinement sweep and the increment tail, are the FP32 values widened)
     PhaseK<float> ph32[2];
 };
 
@@ -187,9 +186,8 @@ struct EndArgs {
     const double* gproj;  // [2][GP_STRIDE]
     const uint8_t* gbm;   // [N] same-grain neighbour bits (x+, x-, y+, y-, z+, "z-")
     double l0;            // L0
-    // FP32 bulk without GND: orientation and density rates in FP32 from these
-    // phase constants, the state updates in FP64
-    int rates32;
+    // FP32 bulk without GND (k_end<float>): orientation and density rates in
+    // FP32 from these phase constants, the state updates in FP64
     const float* schm32;  // FP32 Schmid vectors [60][N]
     PhaseK<float> ph32[2];
 };

@@ -259,28 +259,33 @@ static cudaError_t build_tables_t(Batch& b) {
     }
     {
         std::vector<MacroArgs> m;
-        std::vector<BeginArgs> bg;
-        std::vector<EndArgs> en;
+        // head and tail tables per arithmetic type: [0] FP64, [1] FP32 (FP32 bulk
+        // without GND)
+        std::vector<BeginArgs> bg[2];
+        std::vector<EndArgs> en[2];
         std::vector<EndReduceArgs> er;
         std::vector<Macro*> mp;
-        std::vector<int> gm, gb, ge, g1;
+        std::vector<int> gm, gb[2], ge[2], g1;
         for (Ctx* c : b.slots) {
+            const int t = head_tail_fp32(*c) ? 1 : 0;
             m.push_back(c->ks->mac);
             gm.push_back(MACRO_BLOCKS);
-            bg.push_back(c->ks->beg);
-            bg.back().gate = GATE_BEGIN;
-            gb.push_back(c->ks->grid_begin);
-            en.push_back(c->ks->end);
-            en.back().gate = GATE_ENDING;
-            ge.push_back(c->ks->grid_end);
+            bg[t].push_back(c->ks->beg);
+            bg[t].back().gate = GATE_BEGIN;
+            gb[t].push_back(c->ks->grid_begin);
+            en[t].push_back(c->ks->end);
+            en[t].back().gate = GATE_ENDING;
+            ge[t].push_back(c->ks->grid_end);
             er.push_back(c->ks->endr);
             er.back().gate = GATE_ENDING;
             g1.push_back(1);
             mp.push_back(c->macro);
         }
         if (e == cudaSuccess) e = put_table(b, BL_MACRO, m, gm, 0);
-        if (e == cudaSuccess) e = put_table(b, BL_BEGIN, bg, gb, 0);
-        if (e == cudaSuccess) e = put_table(b, BL_END, en, ge, 0);
+        if (e == cudaSuccess) e = put_table(b, BL_BEGIN, bg[0], gb[0], 0);
+        if (e == cudaSuccess) e = put_table(b, BL_BEGIN32, bg[1], gb[1], 0);
+        if (e == cudaSuccess) e = put_table(b, BL_END, en[0], ge[0], 0);
+        if (e == cudaSuccess) e = put_table(b, BL_END32, en[1], ge[1], 0);
         if (e == cudaSuccess) e = put_table(b, BL_ENDR, er, g1, 0);
         if (e == cudaSuccess) e = put_table(b, BL_MBEGIN, mp, g1, 0);
         // BL_MBEGIN: nblk counts the slots
@@ -316,8 +321,7 @@ static int build_graph(Batch& b) {
         c0->stream = cs;
         np = 2;
     } else {
-        launch_begin_batch(b.L, b.stream);
-        np = 2;
+        np = launch_begin_batch(b.L, b.stream);
     }
     k_round_start<<<1, ADVANCE_THREADS, 0, b.stream>>>(dm, n, b.dtk, b.dtk + 1, h);
     np++;
@@ -397,8 +401,7 @@ static int build_graph(Batch& b) {
         nt += 2;
         c0->stream = cs;
     } else {
-        launch_end_batch(b.precision, b.nr_mode, b.L, b.stream);
-        nt += (b.precision != 0) ? 4 : 2;
+        nt += launch_end_batch(b.precision, b.nr_mode, b.L, b.stream);
     }
     {
         cudaGraph_t g_out = nullptr;

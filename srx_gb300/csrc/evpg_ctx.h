@@ -122,7 +122,7 @@ struct BatchLaunch {
 };
 enum BatchKind { BL_Z, BL_YF, BL_X, BL_YI, BL_NR, BL_MACRO, BL_MBEGIN, BL_BEGIN, BL_FOLD,
                  BL_REFINE, BL_END, BL_ENDR, BL_PF1, BL_PF2, BL_PF4, BL_PI1, BL_PI2, BL_PI4,
-                 BL_XW1, BL_XW2, BL_XW4, BL_COUNT };
+                 BL_XW1, BL_XW2, BL_XW4, BL_BEGIN32, BL_END32, BL_COUNT };
 // Spectral chain of a batch: the separate z and y passes over the slots in
 // BL_Z/BL_YF/BL_YI, the fused plane kernels over the slots in BL_PF*/BL_PI*
 // (1, 2, 4 elements per lane), the X pass as the warp-register kernel over the
@@ -135,9 +135,15 @@ int plane_epl(const Grid& g, size_t elem_bytes);
 cudaError_t launch_nr_batch(int precision, int nr_mode, const BatchLaunch& L, cudaStream_t st);
 cudaError_t launch_macro_batch(const BatchLaunch& L, cudaStream_t st);
 // increment head (macro reset + k_begin), gated per slot
-cudaError_t launch_begin_batch(const BatchLaunch* L, cudaStream_t st);
+// increment head over the slots of BL_BEGIN (FP64 arithmetic) and BL_BEGIN32
+// (FP32-bulk without GND); returns the number of kernels launched
+int launch_begin_batch(const BatchLaunch* L, cudaStream_t st);
 // increment tail (fold + FP64 refinement for FP32 bulk, k_end, k_end_reduce)
-cudaError_t launch_end_batch(int precision, int nr_mode, const BatchLaunch* L, cudaStream_t st);
+// increment tail (FP32 fold and FP64 refinement first in the FP32-bulk form);
+// returns the number of kernels launched
+int launch_end_batch(int precision, int nr_mode, const BatchLaunch* L, cudaStream_t st);
+// the head and tail of this context compute in FP32 (FP32 bulk without GND)
+bool head_tail_fp32(const Ctx& c);
 
 // Launchers of one RVE's kernels on its stream; `gate` selects when a launch
 // does work (Gate).

@@ -1056,6 +1056,10 @@ __device__ __forceinline__ void begin_rates(const BeginArgs& a, int v, int ph, c
     }
 }
 
+// R: arithmetic type of the Schmid vectors and flow constants (float in the
+// FP32-bulk form without GND, else double); one kernel per type keeps the
+// FP32 kernel's registers its own.
+template <typename R>
 __device__ __forceinline__ void begin_body(const BeginArgs& a, int bid) {
     const int v = bid * 128 + threadIdx.x;
     const int N = a.g.N;
@@ -1080,20 +1084,22 @@ __device__ __forceinline__ void begin_body(const BeginArgs& a, int bid) {
         for (int c = 6; c < 9; c++) a.ddg32[(size_t)c * N + v] = 0.0f;
     }
     if (!a.mat.ph[ph - 1].crystal) return;
-    if (a.rates32 && !a.rho_g) begin_rates<float>(a, v, ph, a.ph32[ph - 1]);
+    if constexpr (sizeof(R) == 4) begin_rates<float>(a, v, ph, a.ph32[ph - 1]);
     else begin_rates<double>(a, v, ph, P);
 }
 
+template <typename R>
 __global__ void __launch_bounds__(128) k_begin(const __grid_constant__ BeginArgs a) {
     if (!gate_open(a.macro, a.gate)) return;
-    begin_body(a, blockIdx.x);
+    begin_body<R>(a, blockIdx.x);
 }
 
+template <typename R>
 __global__ void __launch_bounds__(128) kb_begin(const BeginArgs* __restrict__ tab, const int2* __restrict__ map) {
     const int2 m = map[blockIdx.x];
     const BeginArgs& a = tab[m.x];
     if (!gate_open(a.macro, a.gate)) return;
-    begin_body(a, m.y);
+    begin_body<R>(a, m.y);
 }
 
 // FP32 bulk: fold the FP32 displacement-gradient increment into the FP64
@@ -1336,11 +1342,13 @@ __device__ __forceinline__ void end_crystal(const EndArgs& a, int v, int ph, con
     for (int k = 3; k < 7; k++) q[k] += (double)qa[k];
 }
 
+// R as in the head: float in the FP32-bulk form without GND, else double.
+template <typename R>
 __device__ __forceinline__ void end_body(const EndArgs& a, int bid) {
     const int v = bid * END_BLOCK + threadIdx.x;
     const int N = a.g.N;
     const double dt = a.mat.dt;
-    const bool r32 = a.rates32 && !a.rho_g;
+    constexpr bool r32 = sizeof(R) == 4;
     double q[NPART_END];
 #pragma unroll
     for (int i = 0; i < NPART_END; i++) q[i] = 0.0;
@@ -1372,23 +1380,25 @@ __device__ __forceinline__ void end_body(const EndArgs& a, int bid) {
             for (int c = 0; c < 6; c++) a.sig32[(size_t)c * N + v] = (float)a.sig64[(size_t)c * N + v];
         const int ph = a.phase[v];
         if (a.mat.ph[ph - 1].crystal) {
-            if (r32) end_crystal<float>(a, v, ph, a.ph32[ph - 1], vg, q);
+            if constexpr (r32) end_crystal<float>(a, v, ph, a.ph32[ph - 1], vg, q);
             else end_crystal<double>(a, v, ph, a.mat.ph[ph - 1], vg, q);
         }
     }
     block_reduce_store<NPART_END>(q, a.part + (size_t)bid * NPART_END);
 }
 
+template <typename R>
 __global__ void __launch_bounds__(END_BLOCK) k_end(const __grid_constant__ EndArgs a) {
     if (!gate_open(a.macro, a.gate)) return;
-    end_body(a, blockIdx.x);
+    end_body<R>(a, blockIdx.x);
 }
 
+template <typename R>
 __global__ void __launch_bounds__(END_BLOCK) kb_end(const EndArgs* __restrict__ tab, const int2* __restrict__ map) {
     const int2 m = map[blockIdx.x];
     const EndArgs& a = tab[m.x];
     if (!gate_open(a.macro, a.gate)) return;
-    end_body(a, m.y);
+    end_body<R>(a, m.y);
 }
 
 
@@ -1479,7 +1489,6 @@ void build_solver_sets(Ctx& c) {
     b.rho_m = c.rho_m; b.phase = c.phase; b.schm64 = c.schm64; b.fc64 = c.fc64;
     b.schm32 = c.schm32; b.fc32 = c.fc32; b.b6_32 = c.b6_32; b.ddg32 = c.ddg32; b.epsp = c.epsp;
     b.rho_g = c.rho_g; b.gproj = c.gproj;
-    b.rates32 = c.precision != 0;
     for (int p = 0; p < 2; p++) b.ph32[p] = c.m32.ph[p];
     k.grid_begin = (c.g.N + 127) / 128;
     FoldArgs& f = k.fold;
@@ -1495,7 +1504,6 @@ void build_solver_sets(Ctx& c) {
     e.gam_acum = c.gam_acum; e.sig64 = c.sig64; e.schm64 = c.schm64; e.phase = c.phase;
     e.sig32 = c.sig32; e.part = c.part_end;
     e.rho_g = c.rho_g; e.gproj = c.gproj; e.gbm = c.gbm; e.l0 = c.l0;
-    e.rates32 = c.precision != 0;
     e.schm32 = c.schm32;
     for (int p = 0; p < 2; p++) e.ph32[p] = c.m32.ph[p];
     k.grid_end = c.nb_end;
@@ -1555,11 +1563,14 @@ cudaError_t launch_phase(Ctx& c, int from, int to) {
     return cudaGetLastError();
 }
 
+bool head_tail_fp32(const Ctx& c) { return c.precision != 0 && !c.rho_g; }
+
 cudaError_t launch_begin(Ctx& c, int gate) {
     BeginArgs a = c.ks->beg;
     a.gate = gate;
     prof_mark(c, PG_BEGIN, true);
-    k_begin<<<c.ks->grid_begin, 128, 0, c.stream>>>(a);
+    if (head_tail_fp32(c)) k_begin<float><<<c.ks->grid_begin, 128, 0, c.stream>>>(a);
+    else k_begin<double><<<c.ks->grid_begin, 128, 0, c.stream>>>(a);
     prof_mark(c, PG_BEGIN, false);
     return cudaGetLastError();
 }
@@ -1576,7 +1587,8 @@ cudaError_t launch_end(Ctx& c, int gate) {
     EndArgs a = c.ks->end;
     a.gate = gate;
     prof_mark(c, PG_END, true);
-    k_end<<<c.ks->grid_end, END_BLOCK, 0, c.stream>>>(a);
+    if (head_tail_fp32(c)) k_end<float><<<c.ks->grid_end, END_BLOCK, 0, c.stream>>>(a);
+    else k_end<double><<<c.ks->grid_end, END_BLOCK, 0, c.stream>>>(a);
     prof_mark(c, PG_END, false);
     EndReduceArgs r = c.ks->endr;
     r.gate = gate;
@@ -1603,27 +1615,44 @@ cudaError_t launch_macro_batch(const BatchLaunch& L, cudaStream_t st) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_begin_batch(const BatchLaunch* L, cudaStream_t st) {
+int launch_begin_batch(const BatchLaunch* L, cudaStream_t st) {
     const BatchLaunch& mb = L[BL_MBEGIN];
     kb_macro_begin<<<(mb.nblk + 127) / 128, 128, 0, st>>>((Macro* const*)mb.tab, mb.nblk, GATE_BEGIN);
-    const BatchLaunch& b = L[BL_BEGIN];
-    kb_begin<<<b.nblk, 128, 0, st>>>((const BeginArgs*)b.tab, b.map);
-    return cudaGetLastError();
+    int n = 1;
+    const BatchLaunch &b = L[BL_BEGIN], &b32 = L[BL_BEGIN32];
+    if (b.nblk) {
+        kb_begin<double><<<b.nblk, 128, 0, st>>>((const BeginArgs*)b.tab, b.map);
+        n++;
+    }
+    if (b32.nblk) {
+        kb_begin<float><<<b32.nblk, 128, 0, st>>>((const BeginArgs*)b32.tab, b32.map);
+        n++;
+    }
+    return n;
 }
 
-cudaError_t launch_end_batch(int precision, int nr_mode, const BatchLaunch* L, cudaStream_t st) {
+int launch_end_batch(int precision, int nr_mode, const BatchLaunch* L, cudaStream_t st) {
+    int n = 1;
     if (precision != 0) {
         const BatchLaunch& f = L[BL_FOLD];
         kb_fold<<<f.nblk, 256, 0, st>>>((const FoldArgs*)f.tab, f.map);
         const BatchLaunch& r = L[BL_REFINE];
         if (nr_mode) kb_nr<double, 1><<<r.nblk, NR_BLOCK, nrb_smem<double>(), st>>>((const NrArgs<double>*)r.tab, r.map);
         else kb_nr<double, 0><<<r.nblk, NR_BLOCK, nrb_smem<double>(), st>>>((const NrArgs<double>*)r.tab, r.map);
+        n += 2;
     }
-    const BatchLaunch& e = L[BL_END];
-    kb_end<<<e.nblk, END_BLOCK, 0, st>>>((const EndArgs*)e.tab, e.map);
+    const BatchLaunch &e = L[BL_END], &e32 = L[BL_END32];
+    if (e.nblk) {
+        kb_end<double><<<e.nblk, END_BLOCK, 0, st>>>((const EndArgs*)e.tab, e.map);
+        n++;
+    }
+    if (e32.nblk) {
+        kb_end<float><<<e32.nblk, END_BLOCK, 0, st>>>((const EndArgs*)e32.tab, e32.map);
+        n++;
+    }
     const BatchLaunch& er = L[BL_ENDR];
     kb_end_reduce<<<er.nblk, 256, 0, st>>>((const EndReduceArgs*)er.tab);
-    return cudaGetLastError();
+    return n;
 }
 
 }  // namespace evpg
