@@ -820,12 +820,14 @@ template <typename T> static void spec_attributes() {
     cudaFuncSetAttribute(kb_y<T, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
     cudaFuncSetAttribute(kb_y<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
     cudaFuncSetAttribute(kb_x_green<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx - 2048);
-    cudaFuncSetAttribute(k_x_warp<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-    cudaFuncSetAttribute(k_x_warp<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-    cudaFuncSetAttribute(k_x_warp<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-    cudaFuncSetAttribute(kb_x_warp<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx - 2048);
-    cudaFuncSetAttribute(kb_x_warp<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx - 2048);
-    cudaFuncSetAttribute(kb_x_warp<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx - 2048);
+    if constexpr (sizeof(T) == 4) {  // the warp-register X pass is FP32 only
+        cudaFuncSetAttribute(k_x_warp<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+        cudaFuncSetAttribute(k_x_warp<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+        cudaFuncSetAttribute(k_x_warp<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+        cudaFuncSetAttribute(kb_x_warp<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx - 2048);
+        cudaFuncSetAttribute(kb_x_warp<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx - 2048);
+        cudaFuncSetAttribute(kb_x_warp<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx - 2048);
+    }
     cudaFuncSetAttribute(k_plane_fwd<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
     cudaFuncSetAttribute(k_plane_fwd<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
     cudaFuncSetAttribute(k_plane_fwd<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
@@ -870,10 +872,13 @@ static void plane_launch_batch(int fwd, int E, const BatchLaunch& L, cudaStream_
 // The X pass of the single-RVE chain: warp-register kernel when chosen.
 template <typename T>
 static void x_launch(const SpecSet<T>& s, const XArgs<T>& xa, cudaStream_t st) {
-    if (s.xw == 1) k_x_warp<T, 1><<<s.grid_xw, XW_THREADS, s.sm_xw, st>>>(xa);
-    else if (s.xw == 2) k_x_warp<T, 2><<<s.grid_xw, XW_THREADS, s.sm_xw, st>>>(xa);
-    else if (s.xw == 4) k_x_warp<T, 4><<<s.grid_xw, XW_THREADS, s.sm_xw, st>>>(xa);
-    else k_x_green<T><<<s.grid_x, SPEC_THREADS, s.sm_x, st>>>(xa);
+    if constexpr (sizeof(T) == 4) {
+        if (s.xw == 1) k_x_warp<T, 1><<<s.grid_xw, XW_THREADS, s.sm_xw, st>>>(xa);
+        else if (s.xw == 2) k_x_warp<T, 2><<<s.grid_xw, XW_THREADS, s.sm_xw, st>>>(xa);
+        else if (s.xw == 4) k_x_warp<T, 4><<<s.grid_xw, XW_THREADS, s.sm_xw, st>>>(xa);
+        if (s.xw) return;
+    }
+    k_x_green<T><<<s.grid_x, SPEC_THREADS, s.sm_x, st>>>(xa);
 }
 
 void spectral_attributes() {
@@ -940,14 +945,16 @@ static int spectral_batch_t(const BatchLaunch* L, cudaStream_t st) {
         kb_y<T, -1><<<yf.nblk, SPEC_THREADS, yf.smem, st>>>((const YArgs<T>*)yf.tab, yf.map);
         n += 2;
     }
-    for (int q = 0; q < 3; q++) {
-        const BatchLaunch& w = L[BL_XW1 + q];
-        if (!w.nblk) continue;
-        const XArgs<T>* tab = (const XArgs<T>*)w.tab;
-        if (q == 0) kb_x_warp<T, 1><<<w.nblk, XW_THREADS, w.smem, st>>>(tab, w.map);
-        else if (q == 1) kb_x_warp<T, 2><<<w.nblk, XW_THREADS, w.smem, st>>>(tab, w.map);
-        else kb_x_warp<T, 4><<<w.nblk, XW_THREADS, w.smem, st>>>(tab, w.map);
-        n++;
+    if constexpr (sizeof(T) == 4) {  // the warp-register X pass is FP32 only
+        for (int q = 0; q < 3; q++) {
+            const BatchLaunch& w = L[BL_XW1 + q];
+            if (!w.nblk) continue;
+            const XArgs<T>* tab = (const XArgs<T>*)w.tab;
+            if (q == 0) kb_x_warp<T, 1><<<w.nblk, XW_THREADS, w.smem, st>>>(tab, w.map);
+            else if (q == 1) kb_x_warp<T, 2><<<w.nblk, XW_THREADS, w.smem, st>>>(tab, w.map);
+            else kb_x_warp<T, 4><<<w.nblk, XW_THREADS, w.smem, st>>>(tab, w.map);
+            n++;
+        }
     }
     if (x.nblk) {
         kb_x_green<T><<<x.nblk, SPEC_THREADS, x.smem, st>>>((const XArgs<T>*)x.tab, x.map);
