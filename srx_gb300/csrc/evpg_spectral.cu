@@ -185,7 +185,7 @@ __device__ __forceinline__ void x_green_body(const XArgs<T>& a, const GreenK<T>&
 // global loads and stores. The [component][x][pencil] tile has padded rows
 // (8-byte column reads without bank conflicts), and every warp reads and
 // writes its own column, so no barrier separates the forward and inverse work.
-constexpr int XW_PEN = 4;
+constexpr int XW_PEN = 8;
 constexpr int XW_ROW = XW_PEN + 1;
 constexpr int XW_THREADS = 32 * XW_PEN;
 
