@@ -258,6 +258,12 @@ int evpg_set_xpass(void *ctx, int32_t mode);
  * x axis only) applied in the given order. The autotuner chooses among such
  * orders. */
 int evpg_set_radix(void *ctx, int32_t axis, const int32_t *radix, int32_t nstages);
+/* Spectral kernels the context runs (no counterpart in the reference):
+ * variant[0] = values per lane of the fused z+y plane kernels (1, 2 or 4 for
+ * 32-, 64- or 128-point planes; 0 = separate z and y passes), variant[1] =
+ * values per lane of the warp-register X pass (0 = the shared-memory
+ * Stockham X pass). */
+int evpg_get_variant(void *ctx, int32_t variant[2]);
 /* Device bytes evpg_create allocates for an n[0] x n[1] x n[2] RVE with
  * n_orient distinct orientations (for admission by HBM footprint); GND
  * densities add 193 bytes per voxel. */
@@ -293,8 +299,10 @@ int evpg_launch_count(void *ctx, int64_t *n);
  * Limits: every n_i <= 64 and n0*n1*(n2/2+1) <= 17408 (e.g. 32^3); larger
  * grids return EVPG_ERR_ARG. Scratch is a static device array of ~2.5 MB that
  * every GPU loading the library keeps until exit; nothing is allocated. The
- * first call on a device looks up that array's device address, so make that
- * first call outside any stream capture. Calls whose work overlaps on the GPU
+ * first call on a device looks up that array's device address and writes the
+ * twiddle tables of every axis length into it (a synchronous copy), so make
+ * that first call outside any stream capture; later calls issue only memsets
+ * and kernel launches on the given stream. Calls whose work overlaps on the GPU
  * share the array and race: serialise them. stream: a cudaStream_t or NULL. */
 int evpg_green_correction_noalloc(const double *sig6, double *du9, int32_t n0, int32_t n1,
                                   int32_t n2, const double c0[81], const double s0[81],
@@ -418,7 +426,7 @@ typedef struct evpg_request_info {
     int64_t device_bytes;  /* footprint reserved while loaded */
 } evpg_request_info;
 
-typedef struct evpg_server_stats {
+typedef struct evpg_serve_stats {
     int32_t completed, failed;
     int64_t increments, iterations, rounds, ticks;
     double solve_p50, solve_p99;   /* submit -> done [s] */

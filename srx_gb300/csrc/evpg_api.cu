@@ -2,6 +2,7 @@
 // equilibrium-loop orchestration on the context's stream.
 #include "evpg.h"
 #include "evpg_ctx.h"
+#include "evpg_plan.h"
 
 #include <math.h>
 #include <stdarg.h>
@@ -36,61 +37,6 @@ int record_error(int st, const char* msg) {
             return fail(EVPG_ERR_CUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), \
                         __FILE__, __LINE__);                                            \
     } while (0)
-
-// -------------------------------------------------------------- FFT plans
-
-static void make_plan(int n, FftPlan& p) {
-    memset(&p, 0, sizeof p);
-    p.n = n;
-    int m = n, nf = 0;
-    const int pref[] = {8, 4, 2, 3, 5};
-    for (int r : pref)
-        while (m % r == 0 && nf < 12) {
-            p.radix[nf++] = r;
-            m /= r;
-        }
-    for (int q = 7; m > 1 && nf < 12; q += 2)
-        while (m % q == 0 && nf < 12) {
-            p.radix[nf++] = q;
-            m /= q;
-        }
-    p.nf = nf;
-    int ns = 1;
-    for (int s = 0; s < nf; s++) {
-        p.ns[s] = ns;
-        ns *= p.radix[s];
-    }
-    plan_divisors(p);
-}
-
-// exp(-2 pi i t / n) with exact axis values and quadrant symmetry
-static void unit_root(long t, long n, double* c, double* s) {
-    t %= n;
-    if (t < 0) t += n;
-    const long q = (4 * t) / n, r = 4 * t - q * n;
-    long double c0, s0;
-    if (r == 0) {
-        c0 = 1.0L;
-        s0 = 0.0L;
-    } else if (2 * r <= n) {
-        const long double th = 1.57079632679489661923132169163975144L * ((long double)r / (long double)n);
-        c0 = cosl(th);
-        s0 = sinl(th);
-    } else {
-        const long double th = 1.57079632679489661923132169163975144L * ((long double)(n - r) / (long double)n);
-        c0 = sinl(th);
-        s0 = cosl(th);
-    }
-    long double cc, ss;
-    switch (q & 3) {
-        case 0: cc = c0; ss = s0; break;
-        case 1: cc = -s0; ss = c0; break;
-        case 2: cc = -c0; ss = -s0; break;
-        default: cc = s0; ss = -c0; break;
-    }
-    *c = (double)cc;
-    *s = -(double)ss;  // forward sign
-}
 
 // ------------------------------------------------------------- materials
 
@@ -907,6 +853,14 @@ int evpg_get_schedule(void* ctx, int32_t pencils[3], int32_t radix[3][12], int32
         if (radix)
             for (int s = 0; s < 12; s++) radix[a][s] = s < c->pl[a].nf ? c->pl[a].radix[s] : 0;
     }
+    return EVPG_OK;
+}
+
+int evpg_get_variant(void* ctx, int32_t variant[2]) {
+    Ctx* c = (Ctx*)ctx;
+    if (!c || !variant) return fail(EVPG_ERR_ARG, "bad argument");
+    variant[0] = c->precision ? c->ks->s32.epl : c->ks->s64.epl;
+    variant[1] = c->precision ? c->ks->s32.xw : c->ks->s64.xw;
     return EVPG_OK;
 }
 

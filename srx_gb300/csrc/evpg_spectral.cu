@@ -1,6 +1,7 @@
 // Spectral-chain kernels (see evpg_spectral.cuh) and their launcher.
 #include "evpg_ctx.h"
 #include "evpg_spectral.cuh"
+#include "evpg_plan.h"
 
 #include <string.h>
 
@@ -1226,8 +1227,10 @@ namespace evpg {
 constexpr int NOALLOC_MAX_LEN = 64;               // per axis
 constexpr long long NOALLOC_MAX_HALF = 32 * 32 * 17;  // n0*n1*(n2/2+1), e.g. 32^3
 constexpr size_t NOALLOC_SPEC_BYTES = 9 * NOALLOC_MAX_HALF * sizeof(double2);
+// twiddles of every axis length 1..NOALLOC_MAX_LEN, length n at entry n(n-1)/2
+constexpr int NOALLOC_TW_ENTRIES = NOALLOC_MAX_LEN * (NOALLOC_MAX_LEN + 1) / 2;
 constexpr size_t NOALLOC_TW_OFF = NOALLOC_SPEC_BYTES;
-constexpr size_t NOALLOC_ZERO_OFF = NOALLOC_TW_OFF + 3 * NOALLOC_MAX_LEN * sizeof(double2);
+constexpr size_t NOALLOC_ZERO_OFF = NOALLOC_TW_OFF + ((NOALLOC_TW_ENTRIES * sizeof(double2) + 255) / 256) * 256;
 constexpr size_t NOALLOC_BYTES = NOALLOC_ZERO_OFF + 256;  // 9 zero doubles, padded
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
@@ -1235,54 +1238,27 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
 static std::mutex g_noalloc_mu;
 static void* g_noalloc_ptr[128];  // device address of the array, per device
 
-static void na_plan(int n, FftPlan& p) {
-    memset(&p, 0, sizeof p);
-    p.n = n;
-    int m = n, nf = 0;
-    const int pref[] = {8, 4, 2, 3, 5};
-    for (int r : pref)
-        while (m % r == 0 && nf < 12) {
-            p.radix[nf++] = r;
-            m /= r;
-        }
-    for (int q = 7; m > 1 && nf < 12; q += 2)
-        while (m % q == 0 && nf < 12) {
-            p.radix[nf++] = q;
-            m /= q;
-        }
-    p.nf = nf;
-    int ns = 1;
-    for (int s = 0; s < nf; s++) {
-        p.ns[s] = ns;
-        ns *= p.radix[s];
+// Once per device, with that device current: look up the device address of
+// the static array (its host-side name is not a device pointer) and write the
+// twiddle tables of every axis length into it. Calls never overwrite them.
+static int noalloc_setup(int dev, unsigned char** base) {
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return EVPG_ERR_CUDA;
+        static double2 tw[NOALLOC_TW_ENTRIES];
+        for (int n = 1; n <= NOALLOC_MAX_LEN; n++)
+            for (int t = 0; t < n; t++) {
+                double cc, ss;
+                unit_root(t, n, &cc, &ss);
+                tw[n * (n - 1) / 2 + t] = make_double2(cc, ss);
+            }
+        if (cudaMemcpy((unsigned char*)p + NOALLOC_TW_OFF, tw, sizeof tw, cudaMemcpyHostToDevice) != cudaSuccess)
+            return EVPG_ERR_CUDA;
+        g_noalloc_ptr[dev] = p;
     }
-    plan_divisors(p);
-}
-
-// exp(-2 pi i t/n) with exact axis values (same table as the context path)
-static double2 na_root(long t, long n) {
-    const long q = (4 * t) / n, r = 4 * t - q * n;
-    long double c0, s0;
-    if (r == 0) {
-        c0 = 1.0L;
-        s0 = 0.0L;
-    } else if (2 * r <= n) {
-        const long double th = 1.57079632679489661923132169163975144L * ((long double)r / (long double)n);
-        c0 = cosl(th);
-        s0 = sinl(th);
-    } else {
-        const long double th = 1.57079632679489661923132169163975144L * ((long double)(n - r) / (long double)n);
-        c0 = sinl(th);
-        s0 = cosl(th);
-    }
-    long double cc, ss;
-    switch (q & 3) {
-        case 0: cc = c0; ss = s0; break;
-        case 1: cc = -s0; ss = c0; break;
-        case 2: cc = -c0; ss = -s0; break;
-        default: cc = s0; ss = -c0; break;
-    }
-    return make_double2((double)cc, -(double)ss);
+    *base = (unsigned char*)g_noalloc_ptr[dev];
+    return EVPG_OK;
 }
 
 }  // namespace evpg
@@ -1299,36 +1275,21 @@ extern "C" int evpg_green_correction_noalloc(const double* sig6, double* du9, in
     if (half > NOALLOC_MAX_HALF) return EVPG_ERR_ARG;  // beyond the static scratch
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 128) return EVPG_ERR_CUDA;
-    unsigned char* base;
-    {
-        // once per device, with that device current: the device address of the
-        // static array (its host-side name is not a device pointer)
-        std::lock_guard<std::mutex> lk(g_noalloc_mu);
-        if (!g_noalloc_ptr[dev]) {
-            void* p = nullptr;
-            if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return EVPG_ERR_CUDA;
-            g_noalloc_ptr[dev] = p;
-        }
-        base = (unsigned char*)g_noalloc_ptr[dev];
-    }
+    unsigned char* base = nullptr;
+    if (noalloc_setup(dev, &base) != EVPG_OK) return EVPG_ERR_CUDA;
     cudaStream_t st = (cudaStream_t)stream;
     Grid g;
     g.n0 = n0; g.n1 = n1; g.n2 = n2; g.nh = n2 / 2 + 1; g.N = n0 * n1 * n2; g.Nh = half;
     FftPlan pl[3];
-    double2 tw[3][NOALLOC_MAX_LEN];
-    for (int a = 0; a < 3; a++) {
-        na_plan(n[a], pl[a]);
-        for (int t = 0; t < n[a]; t++) tw[a][t] = na_root(t, n[a]);
-    }
+    for (int a = 0; a < 3; a++) make_plan(n[a], pl[a]);
     double2* spec = (double2*)base;
-    double2* twd = (double2*)(base + NOALLOC_TW_OFF);
+    const double2* twd = (const double2*)(base + NOALLOC_TW_OFF);
     double* zero9 = (double*)(base + NOALLOC_ZERO_OFF + 16);
-    const double2* twp[3] = {twd, twd + NOALLOC_MAX_LEN, twd + 2 * NOALLOC_MAX_LEN};
+    const double2* twp[3] = {twd + n0 * (n0 - 1) / 2, twd + n1 * (n1 - 1) / 2, twd + n2 * (n2 - 1) / 2};
     // the macro correction must read zero; the output is accumulated into,
     // so it starts at zero too
     if (cudaMemsetAsync(base + NOALLOC_ZERO_OFF, 0, 256, st) != cudaSuccess) return EVPG_ERR_CUDA;
     if (cudaMemsetAsync(du9, 0, (size_t)9 * g.N * sizeof(double), st) != cudaSuccess) return EVPG_ERR_CUDA;
-    if (cudaMemcpyAsync(twd, tw, sizeof tw, cudaMemcpyHostToDevice, st) != cudaSuccess) return EVPG_ERR_CUDA;
 
     const size_t es = sizeof(double2), budget = 72 * 1024;
     ZArgs<double> za;

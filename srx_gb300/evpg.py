@@ -225,6 +225,14 @@ class Job:
         check(lib().evpg_get_schedule(self.ctx, P, R, S))
         return {"pencils_zyx": list(P), "radix_xyz": [list(R[12 * a:12 * a + S[a]]) for a in range(3)]}
 
+    def variant(self) -> tuple:
+        """(plane-kernel values per lane, warp X-pass values per lane); 0 means
+        the separate Stockham passes run instead."""
+        lib().evpg_get_variant.argtypes = [C.c_void_p, C.POINTER(C.c_int32)]
+        v = (C.c_int32 * 2)()
+        check(lib().evpg_get_variant(self.ctx, v))
+        return (v[0], v[1])
+
     def set_load_from(self, input_path: str) -> None:
         """Switch to the boundary conditions of another namelist."""
         lib().evpg_job_set_load_from.argtypes = [C.c_void_p, C.c_char_p]

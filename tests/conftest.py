@@ -96,6 +96,19 @@ def rel_err(a, b):
     return float(np.max(np.abs(a - b)) / s) if s > 0 else float(np.max(np.abs(a)))
 
 
+def col_err(a, b):
+    """Largest per-column error of two tables, each column normalised by its
+    own largest |b| (a column of zeros by 1): small columns (strains ~1e-4
+    beside stresses ~1e2 MPa, dipole densities ~1e-10 beside SSD densities
+    ~10) are checked at the same relative precision as the large ones."""
+    a = np.asarray(a, float)
+    b = np.asarray(b, float)
+    assert a.shape == b.shape, (a.shape, b.shape)
+    s = np.max(np.abs(b), axis=0)
+    s = np.where(s > 0, s, 1.0)
+    return float(np.max(np.abs(a - b) / s)) if a.size else 0.0
+
+
 def read_iters(d):
     return [int(l.split()[1]) for l in open(os.path.join(str(d), "iters.txt")) if l.strip()]
 

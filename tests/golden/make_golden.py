@@ -18,6 +18,14 @@ ref`` from the reference tree) on small cases and stores what it writes:
                    gradients start in the third increment (istep > 1) and reach
                    the flow rule in the fourth; full final fields including
                    the GND densities;
+* ``cfg0_32_run``  the 32^3 / 27-grain configuration over all 50 increments:
+                   iteration counts, vm.out and dd.out of every increment,
+                   fields at increments 0, 14, 28, 49 on every 7th voxel;
+* ``cfg1_64_ls``   the 64^3 / 125-grain configuration, first 5 increments,
+                   fields at increments 0 and 4 on every 31st voxel;
+* ``cfg2_128_ls``  the 128^3 / 1000-grain precision-form configuration with
+                   per-grain log-uniform initial density (the benchmark's RVE),
+                   first 2 increments, fields of both on every 251st voxel;
 * ``setup16``      the set-up state of ``voronoi16_ls`` (C066, S066, Schmid
                    tensors, interaction matrices, shear modulus, Burgers length);
 * ``nrprobe8``     one UpdateStress sweep of the reference on the bicrystal
@@ -61,6 +69,27 @@ def cfg0_32_spec():
 def gnd12_spec():
     return dict(kind="voronoi", n=[12, 12, 12], grains=6, seed=1212, steps=5, nr="ls",
                 rho0=None, gnd=True)
+
+
+def cfg0_32_run_spec():
+    """The 32^3 / 27-grain configuration over its whole load path (50
+    increments of 2e-4 strain)."""
+    return dict(kind="voronoi", n=[32, 32, 32], grains=27, seed=1027, steps=50, nr="ls",
+                rho0=None, keep=[0, 14, 28, 49], print_every=7, stride=7)
+
+
+def cfg1_64_spec():
+    """The 64^3 / 125-grain configuration, first five increments."""
+    return dict(kind="voronoi", n=[64, 64, 64], grains=125, seed=1125, steps=5, nr="ls",
+                rho0=None, keep=[0, 4], print_every=2, stride=31)
+
+
+def cfg2_128_spec():
+    """The 128^3 / 1000-grain precision-form configuration (per-grain initial
+    density log-uniform in [5e11, 5e12] m^-2, seed 2025: the benchmark's own
+    RVE), first two increments."""
+    return dict(kind="voronoi", n=[128, 128, 128], grains=1000, seed=2025, steps=2, nr="ls",
+                rho0=[0.5, 5.0], keep=[0, 1], print_every=1, stride=251)
 
 
 def make_input(spec: dict, d: str, print_every: int = 1) -> dict:
@@ -146,6 +175,24 @@ def gen_voronoi(spec: dict, out: str, stride: int = 1) -> None:
             keys += ["Sig", "rho_s", "rho_g1", "rho_g2"]
         for k in keys:
             data["final_" + k] = fin[k][idx]
+    np.savez_compressed(out, spec=json.dumps(spec), **data)
+
+
+def gen_run(spec: dict, out: str) -> None:
+    """A multi-increment run: iteration counts, vm.out and dd.out of every
+    increment, and the .iout fields of the increments in spec["keep"] on every
+    spec["stride"]-th voxel (keys "<field>_<increment>")."""
+    with tempfile.TemporaryDirectory() as t:
+        case = make_input(spec, t, print_every=spec["print_every"])
+        iters = run_ref(REF_LS, case)
+        N = int(np.prod(spec["n"]))
+        idx = np.arange(0, N, spec["stride"])
+        data = {"iters": np.array(iters), "vm": read_table(os.path.join(t, "vm.out")),
+                "dd": read_table(os.path.join(t, "dd.out")), "idx": idx,
+                "keep": np.array(spec["keep"])}
+        for s in spec["keep"]:
+            for k, v in read_fields(t, s, N).items():
+                data["%s_%d" % (k, s)] = v[idx]
     np.savez_compressed(out, spec=json.dumps(spec), **data)
 
 
@@ -245,6 +292,9 @@ GENS = {
     "voronoi16_ls": lambda o: gen_voronoi(voronoi16_spec(), o),
     "cfg0_32_ls": lambda o: gen_voronoi(cfg0_32_spec(), o, stride=7),
     "gnd12_ls": lambda o: gen_voronoi(gnd12_spec(), o),
+    "cfg0_32_run": lambda o: gen_run(cfg0_32_run_spec(), o),
+    "cfg1_64_ls": lambda o: gen_run(cfg1_64_spec(), o),
+    "cfg2_128_ls": lambda o: gen_run(cfg2_128_spec(), o),
     "setup16": lambda o: gen_setup16(o),
     "nrprobe8": lambda o: gen_nrprobe8(o),
 }

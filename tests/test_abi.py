@@ -31,6 +31,25 @@ def test_library_builds_and_exports_every_symbol():
     assert os.path.exists(build.RUN)
 
 
+def test_header_compiles_as_c_with_struct_tags(tmp_path):
+    """A C caller may name every structure of the header by its tag
+    (struct evpg_x) or by its typedef (evpg_x): each typedef's tag is its
+    own name."""
+    import subprocess
+    src = open(os.path.join(ROOT, "include", "evpg.h")).read()
+    tags, names = [], []
+    for m in re.finditer(r"typedef\s+struct\s+(\w+)\s*\{", src):
+        tags.append(m.group(1))
+        names.append(re.compile(r"\}\s*(\w+)\s*;").search(src, m.end()).group(1))
+    assert tags and tags == names, list(zip(tags, names))
+    c = tmp_path / "use.c"
+    c.write_text('#include "evpg.h"\n' + "".join(
+        "struct %s a%d; %s b%d;\n" % (t, i, t, i) for i, t in enumerate(tags)) +
+        "int main(void) { return 0; }\n")
+    subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"),
+                    "-c", str(c), "-o", str(tmp_path / "use.o")], check=True)
+
+
 def test_no_cpu_fallback_without_device(tmp_path):
     import torch
     if torch.cuda.is_available():

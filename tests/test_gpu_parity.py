@@ -3,7 +3,9 @@ fixtures) and against the oracle run on the same inputs.
 
 Tolerances (FP64 plain form): per-voxel fields within 1e-8 of the field's
 max magnitude, macroscopic stress within 1e-9 relative, identical equilibrium
-iteration counts. vm.out/dd.out are compared at their print precision (%e).
+iteration counts. vm.out/dd.out are compared column by column at their print
+precision (%e, 7 significant digits), each column against its own largest
+entry.
 FP32-bulk form: macroscopic stress within 1e-4 relative and field L2 within
 1e-3 of the FP64 result."""
 import os
@@ -11,7 +13,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import (golden, read_iout_fields, read_iters, read_table, rel_err,
+from conftest import (col_err, golden, read_iout_fields, read_iters, read_table, rel_err,
                       write_spec_case)
 
 pytestmark = pytest.mark.gpu
@@ -39,8 +41,8 @@ def test_bicrystal8_matches_reference(tmp_path):
     case = write_spec_case(spec, tmp_path / "case")
     _run_gpu(case, tmp_path / "out", spec["steps"], nr_mode=0)
     assert read_iters(tmp_path / "out") == list(z["iters"])
-    assert rel_err(read_table(tmp_path / "out" / "vm.out"), z["vm"]) < PRINT_TOL
-    assert rel_err(read_table(tmp_path / "out" / "dd.out")[:, :2], z["dd"][:, :2]) < PRINT_TOL
+    assert col_err(read_table(tmp_path / "out" / "vm.out"), z["vm"]) < PRINT_TOL
+    assert col_err(read_table(tmp_path / "out" / "dd.out"), z["dd"]) < PRINT_TOL
     for s in z["keep"]:
         f = read_iout_fields(tmp_path / "out", int(s), 512)
         for k in ("sig", "eps", "els", "rho_s", "gam_acum", "newpos"):
@@ -53,7 +55,8 @@ def test_line_search_cases_match_reference(tmp_path, name):
     case = write_spec_case(spec, tmp_path / "case")
     _run_gpu(case, tmp_path / "out", spec["steps"], nr_mode=1)
     assert read_iters(tmp_path / "out") == list(z["iters"])
-    assert rel_err(read_table(tmp_path / "out" / "vm.out"), z["vm"]) < PRINT_TOL
+    assert col_err(read_table(tmp_path / "out" / "vm.out"), z["vm"]) < PRINT_TOL
+    assert col_err(read_table(tmp_path / "out" / "dd.out"), z["dd"]) < PRINT_TOL
     N = int(np.prod(spec["n"]))
     f = read_iout_fields(tmp_path / "out", spec["steps"] - 1, N)
     idx = z["idx"]
@@ -80,7 +83,8 @@ def test_gnd_densities_match_reference(tmp_path):
         g2 = j.download(evpg.F_RHO_G2)
         rm = j.download(evpg.F_RHO_M)
     assert read_iters(out) == list(z["iters"])
-    assert rel_err(read_table(out / "vm.out"), z["vm"]) < PRINT_TOL
+    assert col_err(read_table(out / "vm.out"), z["vm"]) < PRINT_TOL
+    assert col_err(read_table(out / "dd.out"), z["dd"]) < PRINT_TOL
     f = read_iout_fields(out, spec["steps"] - 1, N)
     for k in ("sig", "eps", "els", "rho_s", "gam_acum", "newpos"):
         assert rel_err(f[k], z[k]) < FIELD_TOL, k
@@ -176,19 +180,35 @@ def test_solve_path_matches_iteration_path(tmp_path):
     assert np.array_equal(sig, f["sig"])
 
 
-def test_fp32_bulk_within_stated_error(tmp_path):
+def _l2(a, b):
+    return float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / np.linalg.norm(np.asarray(b)))
+
+
+@pytest.mark.parametrize("name,variant", [("voronoi16_ls", (0, 0)), ("cfg0_32_ls", (1, 1))])
+def test_fp32_bulk_within_stated_error(tmp_path, name, variant):
     """FP32 NR/FFT/Green with FP64 macro update, norms, state and a final FP64
-    NR refinement, against the FP64 reference result."""
-    z, spec = golden("voronoi16_ls")
+    NR refinement, against the reference's FP64 result: macroscopic von Mises
+    stress within 1e-4 relative in every increment, stress and SSD density
+    fields within 1e-3 (L2), the same equilibrium iteration counts. At 32^3 the
+    FP32 defaults run the fused z+y plane kernels and the warp-register X pass
+    (32-point lane layout); at 16^3 neither is eligible and the Stockham
+    passes run."""
+    evpg = _evpg()
+    z, spec = golden(name)
     case = write_spec_case(spec, tmp_path / "case")
-    _run_gpu(case, tmp_path / "out", spec["steps"], nr_mode=1, precision=1)
-    vm = read_table(tmp_path / "out" / "vm.out")
-    # s_vm (macroscopic von Mises stress) per increment
-    assert rel_err(vm[:, 5], z["vm"][:, 5]) < 1e-4
-    f = read_iout_fields(tmp_path / "out", spec["steps"] - 1, 4096)
-    for k in ("sig", "rho_s"):
-        l2 = np.linalg.norm(f[k] - z[k]) / np.linalg.norm(z[k])
-        assert l2 < 1e-3, (k, l2)
+    idx = z["idx"]
+    with evpg.Job(case["input"], case.get("rho0"), precision=1, nr_mode=1) as j:
+        assert j.variant() == variant
+        its, svm = [], []
+        for k in range(spec["steps"]):
+            its.append(j.increment(k))
+            svm.append(j.scalars()[5])
+        sig = j.download(evpg.F_SIG6)[idx]
+        rho = j.download(evpg.F_RHO_S)[idx]
+    assert its == list(z["iters"])
+    assert rel_err(svm, z["vm"][:, 5]) < 1e-4
+    assert _l2(sig, z["sig"]) < 1e-3
+    assert _l2(rho, z["rho_s"]) < 1e-3
 
 
 def test_download_paths_agree(tmp_path):

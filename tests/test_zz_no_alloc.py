@@ -46,7 +46,23 @@ def _from_9(q):
     return t
 
 
-def test_noalloc_green_correction_matches_context_path(tmp_path):
+def _case(tmp_path, grid, elast_bc):
+    """The 16^3 golden RVE, or a seeded Voronoi RVE on another grid: 32^3 is
+    the largest half spectrum the scratch holds, 64x16x8 puts an axis at the
+    length limit (where the x pass takes its largest shared-memory tile),
+    12x10x9 has radix-3/5 stages and odd lengths. elast_bc 0 sets the k = 0
+    term to -S0:sigma_hat(0) instead of zero."""
+    if grid == "golden16":
+        z, spec = golden("voronoi16_ls")
+        return write_spec_case(spec, tmp_path / "case"), list(spec["n"])
+    from srx_gb300 import rve
+    job = rve.Job(n=grid, n_steps=1, elast_bc=elast_bc)
+    return rve.make_case(str(tmp_path / "case"), grid, 6, 31, job), list(grid)
+
+
+@pytest.mark.parametrize("grid,elast_bc", [("golden16", 1), ((32, 32, 32), 1), ((64, 16, 8), 0),
+                                           ((12, 10, 9), 0), ((12, 10, 9), 1)])
+def test_noalloc_green_correction_matches_context_path(tmp_path, grid, elast_bc):
     import torch
     from srx_gb300 import build, evpg
     build.build()
@@ -54,9 +70,7 @@ def test_noalloc_green_correction_matches_context_path(tmp_path):
     L.evpg_green_correction_noalloc.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32,
                                                 C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int32,
                                                 C.c_void_p]
-    z, spec = golden("voronoi16_ls")
-    case = write_spec_case(spec, tmp_path / "case")
-    n = spec["n"]
+    case, n = _case(tmp_path, grid, elast_bc)
     N = int(np.prod(n))
     with evpg.Job(case["input"], nr_mode=1) as j:
         # reference-stiffness tensors of this RVE, from the oracle's set-up
@@ -99,7 +113,7 @@ def test_noalloc_green_correction_matches_context_path(tmp_path):
     for sig, ref in ((sig_before, ref1), (sig1, ref2)):
         s6 = torch.from_numpy(np.ascontiguousarray(_to_b6(sig)).reshape(-1)).to(dev)
         st = L.evpg_green_correction_noalloc(s6.data_ptr(), du.data_ptr(), n[0], n[1], n[2], c0p, s0p,
-                                             1, C.c_void_p(stream.cuda_stream))
+                                             elast_bc, C.c_void_p(stream.cuda_stream))
         assert st == 0, st
         torch.cuda.synchronize()
         got = _from_9(du.cpu().numpy().reshape(9, N))
