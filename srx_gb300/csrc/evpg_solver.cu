@@ -427,122 +427,45 @@ __device__ __forceinline__ void nr_body(const NrArgs<T>& a, int bid, unsigned ch
         for (int c = 0; c < 6; c++) signorm += lam[c] * lam[c];
         signorm = sqrt(signorm);
         T ed[5], dd[15], edot_out[5] = {0, 0, 0, 0, 0};
-        T erral = (T)10 * a.tol, ce = 0, cs = 0;
+        // NR convergence: |sig - old| / |lambda| <= tol (evolution.c:386-391); the
+        // FP32 form compares the squared step with (tol |lambda|)^2 instead
+        T erral, tolc;
+        if constexpr (sizeof(T) == 4) {
+            tolc = (a.tol * signorm) * (a.tol * signorm);
+            erral = (T)100 * tolc + (T)1e-30;
+        } else {
+            tolc = fabs(a.tol);
+            erral = (T)10 * a.tol;
+        }
+        T ce = 0, cs = 0;
         T f_old = 0, slope = 0, alam = 1, alam2 = 0, alamin = 0;
-        bool have = false, trial = false;
+        bool trial = false;
         int it = 0, guard = 0;
+        // end of a Newton or line-search step: the NR convergence measure
+        // (evolution.c:386-391); the voxel's error terms of its last step are
+        // formed after the loop
+        auto finish_step = [&]() {
+            T cnr = 0;
+#pragma unroll
+            for (int c = 0; c < 6; c++) cnr += (sig[c] - old[c]) * (sig[c] - old[c]);
+            if constexpr (sizeof(T) == 4) erral = cnr;  // squared step, against tolc
+            else erral = fdiv(sqrt(cnr), signorm);
+        };
+        // One flow-rule evaluation per pass. A pass at a line-search trial
+        // point evaluates its merit; when the point is accepted, the Newton step
+        // that starts there runs in the same pass with that evaluation (the
+        // reference's next iteration reuses it too), so lanes of a warp that
+        // accept trial points stay with lanes that take plain Newton steps.
         for (;;) {
             if (!trial) {
-                if (!(it < a.itmax && fabs(erral) > fabs(a.tol))) break;
+                if (!(it < a.itmax && fabs(erral) > tolc)) break;
                 it++;
 #pragma unroll
                 for (int c = 0; c < 6; c++) old[c] = sig[c];
             }
-            if (!have) flow_eval<T>(a, nsys, v, stg, sig, !trial && stale0 && it == 1, ed, dd, a.gamdot ? gam : nullptr, bad);
-            have = false;
+            flow_eval<T>(a, nsys, v, stg, sig, !trial && stale0 && it == 1, ed, dd, a.gamdot ? gam : nullptr, bad);
             if (bad) break;
-            bool finish = false;
-            if (!trial) {
-#pragma unroll
-                for (int q = 0; q < 5; q++) edot_out[q] = ed[q];
-                // te = tot_eps - strain = (Eps - strain) + edot dt + S sig
-                T Ss[6];
-                sgr_v<T>(sg, sig, Ss);
-#pragma unroll
-                for (int c = 0; c < 6; c++) te[c] = av[c] + (c < 5 ? ed[c] * dt : (T)0) + Ss[c];
-                // M = S066 + sym(S) + dt d_edot (the first two per orientation);
-                // rhs = S066 R = S066 (sig - lam) + te
-                T m[21];
-                nr_matrix_base<T>(sg, S66, m);
-                {
-                    int k = 0;
-#pragma unroll
-                    for (int p = 0; p < 5; p++)
-#pragma unroll
-                        for (int q = p; q < 5; q++) m[sidx(p, q)] += dt * dd[k++];
-                }
-                T dl[6], rhs[6];
-#pragma unroll
-                for (int c = 0; c < 6; c++) dl[c] = sig[c] - lam[c];
-                mat6v<T>(S66, dl, rhs);
-#pragma unroll
-                for (int c = 0; c < 6; c++) rhs[c] += te[c];
-                if (!ldl_solve<T>(m, rhs, step)) { sing = true; break; }
-                if (!LS) {
-#pragma unroll
-                    for (int c = 0; c < 6; c++) sig[c] -= step[c];
-                    finish = true;
-                } else {
-                    // NR_MODIFIED (evolution.c:284-336). slope = (J^T R).step with
-                    // step = -J^-1 R capped at length 10, i.e. -|R|^2 times the cap
-                    // factor; used directly because through an ill-conditioned J
-                    // the rounded product can change sign.
-                    T nrm = 0;
-#pragma unroll
-                    for (int c = 0; c < 6; c++) {
-                        step[c] = -step[c];
-                        nrm += step[c] * step[c];
-                    }
-                    nrm = sqrt(nrm);
-                    bool whole = false;
-                    if (a.quick_accept && nrm <= (T)10) {
-                        // a step below the NR tolerance ends the NR whatever the line
-                        // search would pick (a shorter step only lowers erral): take it
-                        // whole; the trial's merit would decide a change below the
-                        // tolerance. FP32-bulk form only. A NaN step fails the test and
-                        // takes the line search's error path.
-                        T cnr = 0;
-#pragma unroll
-                        for (int c = 0; c < 6; c++) {
-                            const T d = (old[c] + step[c]) - old[c];
-                            cnr += d * d;
-                        }
-                        if (fdiv(sqrt(cnr), signorm) <= a.tol) {
-#pragma unroll
-                            for (int c = 0; c < 6; c++) sig[c] = old[c] + step[c];
-                            whole = true;
-                            finish = true;
-                        }
-                    }
-                    if (!whole) {
-                        T CR[6];
-                        mat6v<T>(C66, te, CR);
-                        f_old = 0;
-#pragma unroll
-                        for (int c = 0; c < 6; c++) {
-                            const T r = dl[c] + CR[c];
-                            f_old += r * r;
-                        }
-                        slope = -f_old;
-                        f_old *= (T)0.5;
-                        if (nrm > (T)10) {
-                            const T cap = fdiv((T)10, nrm);
-#pragma unroll
-                            for (int c = 0; c < 6; c++) step[c] *= cap;
-                            slope *= cap;
-                        }
-                    }
-                    if (whole) {
-                    } else if (!(slope < (T)0)) {
-                        if (slope != (T)0) { lsfail = true; break; }
-                        finish = true;  // R == 0: at the root already
-                    } else {
-                        T test = 0;
-#pragma unroll
-                        for (int c = 0; c < 6; c++) {
-                            const T tt = fdiv(fabs(step[c]), fmax(fabs(old[c]), (T)1));
-                            if (tt > test) test = tt;
-                        }
-                        alamin = fdiv((T)1e-7, test);
-                        alam = 1;
-                        alam2 = 0;
-#pragma unroll
-                        for (int c = 0; c < 6; c++) sig[c] = old[c] + step[c];
-                        trial = true;
-                        guard = 0;
-                    }
-                }
-            } else {
+            if (trial) {
                 // TRIAL: merit at sig = old + alam step (NR_quality, evolution.c:115-154)
                 T Ss[6], tt6[6], Rt[6], fnew = 0;
                 sgr_v<T>(sg, sig, Ss);
@@ -556,15 +479,15 @@ __device__ __forceinline__ void nr_body(const NrArgs<T>& a, int bid, unsigned ch
                 }
                 fnew *= (T)0.5;
                 if (alam < alamin) {
+                    // no acceptable point: back to the base point, which the next
+                    // pass evaluates again (evolution.c:345-349)
 #pragma unroll
                     for (int c = 0; c < 6; c++) sig[c] = old[c];
                     trial = false;
-                    finish = true;
-                } else if (fnew <= f_old + (T)1e-4 * alam * slope) {
-                    have = true;  // this evaluation serves the next MAIN step
-                    trial = false;
-                    finish = true;
-                } else {
+                    finish_step();
+                    continue;
+                }
+                if (!(fnew <= f_old + (T)1e-4 * alam * slope)) {
                     T tmplam;
                     if (fabs(alam - (T)1) < (T)1e-4) {
                         tmplam = -slope / ((T)2 * (fnew - f_old - slope));
@@ -590,35 +513,143 @@ __device__ __forceinline__ void nr_body(const NrArgs<T>& a, int bid, unsigned ch
 #pragma unroll
                     for (int c = 0; c < 6; c++) sig[c] = old[c] + alam * step[c];
                     if (++guard > 200) { lsfail = true; break; }
+                    continue;
                 }
+                // accepted: the Newton step from this point uses this evaluation
+                trial = false;
+                finish_step();
+                if (!(it < a.itmax && fabs(erral) > tolc)) break;
+                it++;
+#pragma unroll
+                for (int c = 0; c < 6; c++) old[c] = sig[c];
             }
-            if (finish) {
-                T cnr = 0;
-                ce = 0;
-                cs = 0;
+            // MAIN: Newton step at sig
+            bool finish = false;
+#pragma unroll
+            for (int q = 0; q < 5; q++) edot_out[q] = ed[q];
+            // te = tot_eps - strain = (Eps - strain) + edot dt + S sig
+            {
+                T Ss[6];
+                sgr_v<T>(sg, sig, Ss);
+#pragma unroll
+                for (int c = 0; c < 6; c++) te[c] = av[c] + (c < 5 ? ed[c] * dt : (T)0) + Ss[c];
+            }
+            // M = S066 + sym(S) + dt d_edot (the first two per orientation);
+            // rhs = S066 R = S066 (sig - lam) + te
+            T m[21];
+            nr_matrix_base<T>(sg, S66, m);
+            {
+                int k = 0;
+#pragma unroll
+                for (int p = 0; p < 5; p++)
+#pragma unroll
+                    for (int q = p; q < 5; q++) m[sidx(p, q)] += dt * dd[k++];
+            }
+            T dl[6], rhs[6];
+#pragma unroll
+            for (int c = 0; c < 6; c++) dl[c] = sig[c] - lam[c];
+            mat6v<T>(S66, dl, rhs);
+#pragma unroll
+            for (int c = 0; c < 6; c++) rhs[c] += te[c];
+            if (!ldl_solve<T>(m, rhs, step)) { sing = true; break; }
+            if (!LS) {
+#pragma unroll
+                for (int c = 0; c < 6; c++) sig[c] -= step[c];
+                finish = true;
+            } else {
+                // NR_MODIFIED (evolution.c:284-336). slope = (J^T R).step with
+                // step = -J^-1 R capped at length 10, i.e. -|R|^2 times the cap
+                // factor; used directly because through an ill-conditioned J
+                // the rounded product can change sign.
+                T nrm = 0;
 #pragma unroll
                 for (int c = 0; c < 6; c++) {
-                    cnr += (sig[c] - old[c]) * (sig[c] - old[c]);
-                    ce += te[c] * te[c];
-                    cs += (sig[c] - lam[c]) * (sig[c] - lam[c]);
+                    step[c] = -step[c];
+                    nrm += step[c] * step[c];
                 }
-                erral = fdiv(sqrt(cnr), signorm);
-                if (sizeof(T) == 4) {
-                    // FP32 form: at the NR solution tot_eps - eps = -S066 (sig - lambda);
-                    // evaluated at the final stress it carries no lag of the last
-                    // Newton step (the reference takes tot_eps before that step, which
-                    // at the FP32 NR tolerance would floor Err_e near 1e-5).
-                    T d6[6], q6[6];
+                nrm = sqrt(nrm);
+                bool whole = false;
+                if (a.quick_accept && nrm <= (T)10) {
+                    // a step below the NR tolerance ends the NR whatever the line
+                    // search would pick (a shorter step only lowers erral): take it
+                    // whole; the trial's merit would decide a change below the
+                    // tolerance. FP32-bulk form only. A NaN step fails the test and
+                    // takes the line search's error path.
+                    T cnr = 0;
 #pragma unroll
-                    for (int c = 0; c < 6; c++) d6[c] = sig[c] - lam[c];
-                    mat6v<T>(S66, d6, q6);
-                    ce = 0;
+                    for (int c = 0; c < 6; c++) {
+                        const T d = (old[c] + step[c]) - old[c];
+                        cnr += d * d;
+                    }
+                    if (sizeof(T) == 4 ? cnr <= tolc : fdiv(sqrt(cnr), signorm) <= a.tol) {
 #pragma unroll
-                    for (int c = 0; c < 6; c++) ce += q6[c] * q6[c];
+                        for (int c = 0; c < 6; c++) sig[c] = old[c] + step[c];
+                        whole = true;
+                        finish = true;
+                    }
                 }
-                ce = sqrt(ce);
-                cs = sqrt(cs);
+                if (!whole) {
+                    T CR[6];
+                    mat6v<T>(C66, te, CR);
+                    f_old = 0;
+#pragma unroll
+                    for (int c = 0; c < 6; c++) {
+                        const T r = dl[c] + CR[c];
+                        f_old += r * r;
+                    }
+                    slope = -f_old;
+                    f_old *= (T)0.5;
+                    if (nrm > (T)10) {
+                        const T cap = fdiv((T)10, nrm);
+#pragma unroll
+                        for (int c = 0; c < 6; c++) step[c] *= cap;
+                        slope *= cap;
+                    }
+                }
+                if (whole) {
+                } else if (!(slope < (T)0)) {
+                    if (slope != (T)0) { lsfail = true; break; }
+                    finish = true;  // R == 0: at the root already
+                } else {
+                    T test = 0;
+#pragma unroll
+                    for (int c = 0; c < 6; c++) {
+                        const T tt = fdiv(fabs(step[c]), fmax(fabs(old[c]), (T)1));
+                        if (tt > test) test = tt;
+                    }
+                    alamin = fdiv((T)1e-7, test);
+                    alam = 1;
+                    alam2 = 0;
+#pragma unroll
+                    for (int c = 0; c < 6; c++) sig[c] = old[c] + step[c];
+                    trial = true;
+                    guard = 0;
+                }
             }
+            if (finish) finish_step();
+        }
+        // the voxel's error terms at the end of its last step
+        {
+#pragma unroll
+            for (int c = 0; c < 6; c++) {
+                ce += te[c] * te[c];
+                cs += (sig[c] - lam[c]) * (sig[c] - lam[c]);
+            }
+            if constexpr (sizeof(T) == 4) {
+                // FP32 form: at the NR solution tot_eps - eps = -S066 (sig - lambda);
+                // evaluated at the final stress it carries no lag of the last
+                // Newton step (the reference takes tot_eps before that step, which
+                // at the FP32 NR tolerance would floor Err_e near 1e-5).
+                T d6[6], q6[6];
+#pragma unroll
+                for (int c = 0; c < 6; c++) d6[c] = sig[c] - lam[c];
+                mat6v<T>(S66, d6, q6);
+                ce = 0;
+#pragma unroll
+                for (int c = 0; c < 6; c++) ce += q6[c] * q6[c];
+            }
+            ce = sqrt(ce);
+            cs = sqrt(cs);
         }
         nr = it;
 #pragma unroll
