@@ -53,7 +53,8 @@ typedef enum evpg_status {
     EVPG_ERR_LINESEARCH = 6, /* line search found no descent (reference: PError 1203, evolution.c:324-328) */
     EVPG_ERR_ITERMAX = 7,    /* equilibrium loop hit IterMax (the reference continues silently) */
     EVPG_ERR_IO = 8,         /* input file missing or malformed */
-    EVPG_ERR_NO_DEVICE = 9   /* no CUDA device */
+    EVPG_ERR_NO_DEVICE = 9,  /* no CUDA device */
+    EVPG_ERR_TIMEOUT = 10    /* a device-side wait for a copy exceeded its bound (the RVE stops) */
 } evpg_status;
 
 typedef enum evpg_precision {

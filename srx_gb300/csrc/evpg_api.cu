@@ -170,7 +170,7 @@ static void free_ctx(Ctx* c) {
     prof_free(*c);
     void* ptrs[] = {c->sig64, c->dg64, c->dg_old, c->epsp, c->edot64, c->rho_s, c->rho_m,
                     c->gamdot64, c->gam_acum, c->tranmat, c->schm64, c->fc64, c->sgr64, c->orient,
-                    c->phase, c->sig32, c->ddg32, c->b6_32, c->schm32, c->fc32, c->sgr32, c->spec,
+                    c->phase, c->sig32, c->ddg32, c->b6_32, c->schm32, c->fc32, c->sgr32, c->nrc32, c->spec,
                     c->part_nr, c->part_nr2, c->ticket, c->part_end, c->macro, c->tw64[0], c->tw64[1], c->tw64[2],
                     c->tw32[0], c->tw32[1], c->tw32[2], c->rho_g, c->gproj, c->gbm};
     for (void* p : ptrs)
@@ -225,6 +225,7 @@ const char* evpg_status_string(int st) {
         case EVPG_ERR_ITERMAX: return "equilibrium loop reached IterMax";
         case EVPG_ERR_IO: return "input file error";
         case EVPG_ERR_NO_DEVICE: return "no CUDA device";
+        case EVPG_ERR_TIMEOUT: return "device-side wait exceeded its bound";
         default: return "unknown status";
     }
 }
@@ -353,6 +354,7 @@ int evpg_create(const evpg_rve_desc* d, void** out) {
     if (f32) {
         AL(c->sig32, 6 * n); AL(c->ddg32, 9 * n); AL(c->b6_32, 6 * n); AL(c->schm32, 60 * n);
         AL(c->fc32, 48 * n); AL(c->sgr32, SGR_STRIDE * (size_t)(d->n_orient > 0 ? d->n_orient : 1));
+        AL(c->nrc32, (size_t)c->nb_nr * NRC_BLOCK_FLOATS);
         float2* sp = nullptr;
         AL(sp, 9 * (size_t)c->g.Nh);
         c->spec = sp;
@@ -871,7 +873,8 @@ int evpg_estimate_bytes(const int32_t n[3], int32_t precision, int32_t n_orient,
     const long long no = n_orient > 0 ? n_orient : 1;
     const long long nb_nr = (N + NR_BLOCK - 1) / NR_BLOCK, nb_end = (N + END_BLOCK - 1) / END_BLOCK;
     long long b = 8 * N * (6 + 9 + 9 + 6 + 5 + 12 + 12 + 12 + 12 + 9 + 60 + 48) + 8 * SGR_STRIDE * no + 4 * 2 * N;
-    if (precision == EVPG_FP32_BULK) b += 4 * N * (6 + 9 + 6 + 60 + 48) + 4 * SGR_STRIDE * no + 8 * 9 * Nh;
+    if (precision == EVPG_FP32_BULK)
+        b += 4 * N * (6 + 9 + 6 + 60 + 48) + 4 * SGR_STRIDE * no + 8 * 9 * Nh + 4 * nb_nr * NRC_BLOCK_FLOATS;
     else b += 16 * 9 * Nh;
     b += 8 * nb_nr * (NR_BLOCK / 32) * NPART_NR + 8 * MACRO_BLOCKS * NPART_NR + 4 + 8 * nb_end * NPART_END;
     b += (long long)sizeof(Macro) + 24LL * (n[0] + n[1] + n[2]);

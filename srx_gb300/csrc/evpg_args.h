@@ -16,6 +16,18 @@ constexpr int NPART_END = 19;  // rho_F, rho_P, rho_s, rho_m, d_dipole, d_forest
 constexpr int GP_COS1 = 0, GP_SIN1 = 144, GP_COS2 = 288, GP_SIN2 = 432, GP_BP = 576,
               GP_STRIDE = 612;
 constexpr int NR_BLOCK = 128;
+// FP32 NR constants, one 32-byte record per (voxel, slip system): Schmid
+// vector (5), passing stress, 1/(tau0 + tau_cut), gamma0_dot. Records of a
+// block of NR_BLOCK voxels are contiguous ([system][voxel in block][8]), so a
+// block's 48 KB arrive in shared memory by bulk copies; the two 16-byte
+// halves of a record are swapped for voxels with bit 2 of their position set,
+// which makes the 128-bit shared-memory reads of a warp conflict-free.
+constexpr int NRC_REC = 8;
+constexpr int NRC_BLOCK_FLOATS = NS * NR_BLOCK * NRC_REC;
+__host__ __device__ __forceinline__ size_t nrc_index(int v, int i, int half) {
+    const int b = v / NR_BLOCK, t = v - b * NR_BLOCK;
+    return (((size_t)b * NS + i) * NR_BLOCK + t) * NRC_REC + 4 * (half ^ ((t >> 2) & 1));
+}
 constexpr int MACRO_BLOCKS = 64;
 constexpr int END_BLOCK = 128;
 constexpr int SPEC_THREADS = 256;
@@ -96,6 +108,7 @@ template <typename T> struct NrArgs {
     const T* epsb;        // [6][N] a = epsb - dg: Eps (FP64) or Eps - eps_begin (FP32)
     const T* schm;        // [60][N]
     const T* fc;          // [48][N]
+    const float* nrc;     // FP32 sweeps: per-block NR constants (nrc_index)
     const int32_t* orient;
     const int32_t* phase;
     const T* sgr;         // [n_orient][SGR_STRIDE]
@@ -139,6 +152,7 @@ struct BeginArgs {
     // FP32 bulk
     float* schm32;
     float* fc32;
+    float* nrc32;        // FP32 NR constants (nrc_index), or null
     float* b6_32;
     float* ddg32;
     const double* epsp;

@@ -48,6 +48,7 @@ struct Ctx {
     double l0;
     // FP32 working set (FP32 bulk only)
     float *sig32, *ddg32, *b6_32, *schm32, *fc32, *sgr32;
+    float* nrc32;  // FP32 NR constants per block of NR_BLOCK voxels (nrc_index)
     void* spec;  // 9 * Nh complex of the working precision
     double* part_nr;   // [nb_nr * NR_BLOCK/32][NPART_NR] warp partials
     int nb_nr;

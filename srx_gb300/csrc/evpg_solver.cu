@@ -187,6 +187,94 @@ __device__ __forceinline__ void flow_eval(const NrArgs<T>& a, int nsys, int v, c
     bad = bad || nan;
 }
 
+// FP32 form: the flow rule with the voxel's slip-system constants read from
+// the block records in shared memory (two 128-bit reads per system: Schmid
+// vector 0..3 | Schmid vector 4, passing stress, 1/(tau0+tau_cut), gamma0_dot).
+// rb: this voxel's record of system 0 in float4 units, system i at
+// rb + 2 NR_BLOCK i; sw: the voxel's half swap. Same arithmetic as flow_eval.
+__device__ __forceinline__ void flow_eval_rec(const NrArgs<float>& a, int nsys, int v, const float4* rb, int sw,
+                                              const float (&s)[6], bool stale, float (&ed)[5], float (&dd)[15],
+                                              bool& bad) {
+    const size_t N = a.g.N;
+#pragma unroll
+    for (int q = 0; q < 5; q++) ed[q] = 0.f;
+#pragma unroll
+    for (int q = 0; q < 15; q++) dd[q] = 0.f;
+    unsigned act = 0;
+#pragma unroll
+    for (int i = 0; i < NS; i++) {
+        if (i >= nsys) break;
+        const float4 h0 = rb[2 * NR_BLOCK * i + sw], h1 = rb[2 * NR_BLOCK * i + (sw ^ 1)];
+        const float rss = h0.x * s[0] + h0.y * s[1] + h0.z * s[2] + h0.w * s[3] + h1.x * s[4];
+        const float tp = stale ? __ldg(a.fc + (size_t)(36 + i) * N + v) : h1.y;
+        if (fabsf(rss) > tp) act |= 1u << i;
+    }
+#pragma unroll 1
+    while (act) {
+        const int i = __ffs(act) - 1;
+        act &= act - 1;
+        const float4 h0 = rb[2 * NR_BLOCK * i + sw], h1 = rb[2 * NR_BLOCK * i + (sw ^ 1)];
+        const float sc[5] = {h0.x, h0.y, h0.z, h0.w, h1.x};
+        const float rss = sc[0] * s[0] + sc[1] * s[1] + sc[2] * s[2] + sc[3] * s[3] + sc[4] * s[4];
+        const float tp = stale ? __ldg(a.fc + (size_t)(36 + i) * N + v) : h1.y;
+        const float ar = fabsf(rss);
+        const float itc = h1.z;
+        const float go = h1.w;
+        float sh, ch;
+        sinh_cosh((ar - tp) * itc, sh, ch);
+        const float g = (rss > 0.f) ? go * sh : -(go * sh);
+        const float g2 = go * ch * itc;
+#pragma unroll
+        for (int q = 0; q < 5; q++) ed[q] += sc[q] * g;
+        int k = 0;
+#pragma unroll
+        for (int p = 0; p < 5; p++) {
+            const float w = sc[p] * g2;
+#pragma unroll
+            for (int q = p; q < 5; q++) dd[k++] += w * sc[q];
+        }
+    }
+    bool nan = false;
+#pragma unroll
+    for (int q = 0; q < 5; q++) nan = nan || isnan(ed[q]);
+#pragma unroll
+    for (int q = 0; q < 15; q++) nan = nan || isnan(dd[q]);
+    bad = bad || nan;
+}
+
+// Bulk copies global -> shared memory completing on an mbarrier (one phase).
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Waits for phase 0 of the barrier a bounded number of times (each try may
+// suspend the thread for a short, system-dependent time); false on timeout.
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar) {
+    for (int k = 0; k < (1 << 18); k++)
+        if (mbar_try_wait(bar, 0)) return true;
+    return false;
+}
+
 // Quotient in the working precision: IEEE division in FP64 (parity with the
 // reference), the fast reciprocal-based quotient in FP32 (within 2 ulp; the
 // FP32 form's tolerance is set by its own NR tolerance, far above that).
@@ -390,10 +478,26 @@ __device__ __forceinline__ void nr_body(const NrArgs<T>& a, int bid, unsigned ch
     const int N = a.g.N;
     const T dt = a.mat.dt;
     T* stg = s_stage + threadIdx.x;
-    T* gam = s_stage + NSTAGE * NR_BLOCK + threadIdx.x;
+    T* gam = sizeof(T) == 8 ? s_stage + NSTAGE * NR_BLOCK + threadIdx.x : nullptr;
     T pe = 0, ps = 0, ss[6] = {0, 0, 0, 0, 0, 0}, s1[6] = {0, 0, 0, 0, 0, 0};
     int nr = 0;
-    bool bad = false, sing = false, lsfail = false;
+    bool bad = false, sing = false, lsfail = false, tmo = false, waited = false;
+    // FP32 sweeps: the block's constant records (48 KB) arrive by bulk copies
+    // issued by one thread, overlapping the state loads of every thread
+    unsigned long long* cbar = nullptr;
+    if constexpr (sizeof(T) == 4) {
+        cbar = reinterpret_cast<unsigned long long*>(nr_smem + (size_t)NRC_BLOCK_FLOATS * sizeof(float));
+        if (threadIdx.x == 0) mbar_init(cbar, 1);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            constexpr unsigned SYS_BYTES = NR_BLOCK * NRC_REC * sizeof(float);
+            mbar_expect_tx(cbar, NS * SYS_BYTES);
+            const float* src = a.nrc + (size_t)bid * NRC_BLOCK_FLOATS;
+#pragma unroll 1
+            for (int i = 0; i < NS; i++)
+                bulk_g2s(nr_smem + (size_t)i * SYS_BYTES, src + (size_t)i * NR_BLOCK * NRC_REC, SYS_BYTES, cbar);
+        }
+    }
     const bool stale0 = a.stale_mode && a.macro->iter == 0;
     const int ph = (v < N) ? a.phase[v] : 1;
     const PhaseK<T>& P = a.mat.ph[ph - 1];
@@ -404,16 +508,20 @@ __device__ __forceinline__ void nr_body(const NrArgs<T>& a, int bid, unsigned ch
 #pragma unroll
             for (int c = 0; c < 5; c++) a.edot[(size_t)c * N + v] = (T)0;
     } else if (v < N) {
-        const int nsys = P.n_sys;
+        int nsys = P.n_sys;
         const T* sg = a.sgr + (size_t)a.orient[v] * SGR_STRIDE;
-        // the staging copies overlap the loads of the voxel's state below
-        for (int i = 0; i < nsys; i++) {
+        if constexpr (sizeof(T) == 8) {
+            // the staging copies overlap the loads of the voxel's state below
+            for (int i = 0; i < nsys; i++) {
 #pragma unroll
-            for (int q = 0; q < 5; q++) stage_async<T>(stg + (i * 5 + q) * NR_BLOCK, a.schm + (size_t)(i * 5 + q) * N + v);
+                for (int q = 0; q < 5; q++)
+                    stage_async<T>(stg + (i * 5 + q) * NR_BLOCK, a.schm + (size_t)(i * 5 + q) * N + v);
 #pragma unroll
-            for (int q = 0; q < 3; q++) stage_async<T>(stg + (60 + 12 * q + i) * NR_BLOCK, a.fc + (size_t)(12 * q + i) * N + v);
+                for (int q = 0; q < 3; q++)
+                    stage_async<T>(stg + (60 + 12 * q + i) * NR_BLOCK, a.fc + (size_t)(12 * q + i) * N + v);
+            }
+            stage_commit();
         }
-        stage_commit();
         T lam[6], sig[6], av[6], old[6], step[6], te[6];
 #pragma unroll
         for (int c = 0; c < 6; c++) {
@@ -421,7 +529,17 @@ __device__ __forceinline__ void nr_body(const NrArgs<T>& a, int bid, unsigned ch
             sig[c] = lam[c];
             av[c] = a.epsb[(size_t)c * N + v] - a.dg[(size_t)c * N + v];
         }
-        stage_wait();
+        if constexpr (sizeof(T) == 8) {
+            stage_wait();
+        } else {
+            // a copy that never completes stops the RVE with a timeout status;
+            // the voxel then runs without slip systems (its result is unused)
+            waited = true;
+            if (!mbar_wait_bounded(cbar)) {
+                tmo = true;
+                nsys = 0;
+            }
+        }
         T signorm = 0;
 #pragma unroll
         for (int c = 0; c < 6; c++) signorm += lam[c] * lam[c];
@@ -463,7 +581,12 @@ __device__ __forceinline__ void nr_body(const NrArgs<T>& a, int bid, unsigned ch
 #pragma unroll
                 for (int c = 0; c < 6; c++) old[c] = sig[c];
             }
-            flow_eval<T>(a, nsys, v, stg, sig, !trial && stale0 && it == 1, ed, dd, a.gamdot ? gam : nullptr, bad);
+            if constexpr (sizeof(T) == 4)
+                flow_eval_rec(a, nsys, v, reinterpret_cast<const float4*>(nr_smem) + 2 * threadIdx.x,
+                              (threadIdx.x >> 2) & 1, sig, !trial && stale0 && it == 1, ed, dd, bad);
+            else
+                flow_eval<T>(a, nsys, v, stg, sig, !trial && stale0 && it == 1, ed, dd, a.gamdot ? gam : nullptr,
+                             bad);
             if (bad) break;
             if (trial) {
                 // TRIAL: merit at sig = old + alam step (NR_quality, evolution.c:115-154)
@@ -667,6 +790,15 @@ __device__ __forceinline__ void nr_body(const NrArgs<T>& a, int bid, unsigned ch
             s1[c] = (ph == 1) ? sig[c] : (T)0;
         }
     }
+    if constexpr (sizeof(T) == 4) {
+        // every thread has seen the copies complete (or given up) before the
+        // block's shared memory is released
+        if (!waited && !mbar_wait_bounded(cbar)) tmo = true;
+        if (tmo) {
+            mbar_wait_bounded(cbar);
+            set_status(a.macro, 10);
+        }
+    }
     if (bad) set_status(a.macro, 4);
     if (sing) set_status(a.macro, 5);
     if (lsfail) set_status(a.macro, 6);
@@ -683,6 +815,11 @@ __device__ __forceinline__ void nr_body(const NrArgs<T>& a, int bid, unsigned ch
     warp_store(q, a.part + (size_t)warp * NPART_NR);
 }
 
+template <typename T> __device__ __forceinline__ constexpr size_t nr_smem_main() {
+    return sizeof(T) == 4 ? (size_t)NRC_BLOCK_FLOATS * sizeof(float) + 16
+                          : (size_t)(NSTAGE + NS) * NR_BLOCK * sizeof(T);
+}
+
 template <typename T, int LS>
 __global__ void __launch_bounds__(NR_BLOCK, NrMinBlocks<T>::v) k_nr(const __grid_constant__ NrArgs<T> a) {
     extern __shared__ __align__(16) unsigned char nr_smem[];
@@ -697,7 +834,7 @@ __global__ void __launch_bounds__(NR_BLOCK, NrMinBlocks<T>::v) kb_nr(const NrArg
     const int2 m = map[blockIdx.x];
     const NrArgs<T>& a = tab[m.x];
     if (!gate_open(a.macro, a.gate)) return;
-    T* sm = reinterpret_cast<T*>(nr_smem) + (NSTAGE + NS) * NR_BLOCK;
+    T* sm = reinterpret_cast<T*>(nr_smem + nr_smem_main<T>());
     for (int i = threadIdx.x; i < 36; i += NR_BLOCK) {
         sm[i] = (&a.mat.s066[0][0])[i];
         sm[36 + i] = (&a.mat.c066[0][0])[i];
@@ -1046,6 +1183,7 @@ __device__ __forceinline__ void begin_rates(const BeginArgs& a, int v, int ph, c
         for (int q = 0; q < 5; q++) {
             a.schm64[(size_t)(s * 5 + q) * N + v] = (double)o6[q];
             if (a.schm32) a.schm32[(size_t)(s * 5 + q) * N + v] = (float)o6[q];
+            if (a.nrc32) a.nrc32[nrc_index(v, s, q >> 2) + (q & 3)] = (float)o6[q];
         }
     }
     R rs[NS];
@@ -1084,6 +1222,9 @@ __device__ __forceinline__ void begin_rates(const BeginArgs& a, int v, int ph, c
             a.fc64[(size_t)(12 * q + i) * N + v] = (double)f4[q];
             if (a.fc32) a.fc32[(size_t)(12 * q + i) * N + v] = (float)f4[q];
         }
+        if (a.nrc32)
+#pragma unroll
+            for (int q = 0; q < 3; q++) a.nrc32[nrc_index(v, i, 1) + 1 + q] = (float)f4[q];
     }
 }
 
@@ -1487,6 +1628,7 @@ static void nr_set(Ctx& c, NrSet<T>& S, const Material<T>& mat, T* sig, const T*
     a.mat = mat;
     a.g = c.g;
     a.sig = sig; a.dg = dg; a.epsb = epsb; a.schm = schm; a.fc = fc;
+    a.nrc = sizeof(T) == 4 ? c.nrc32 : nullptr;
     a.orient = c.orient; a.phase = c.phase; a.sgr = sgr; a.edot = edot; a.gamdot = gamdot;
     a.macro = c.macro; a.part = c.part_nr; a.tol = tol; a.itmax = c.nr_itmax;
     a.nr_mode = c.nr_mode; a.stale_mode = stale_mode; a.gate = gate;
@@ -1519,6 +1661,7 @@ void build_solver_sets(Ctx& c) {
     b.dg64 = c.dg64; b.dg_old = c.dg_old; b.tranmat = c.tranmat; b.rho_s = c.rho_s;
     b.rho_m = c.rho_m; b.phase = c.phase; b.schm64 = c.schm64; b.fc64 = c.fc64;
     b.schm32 = c.schm32; b.fc32 = c.fc32; b.b6_32 = c.b6_32; b.ddg32 = c.ddg32; b.epsp = c.epsp;
+    b.nrc32 = c.nrc32;
     b.rho_g = c.rho_g; b.gproj = c.gproj;
     for (int p = 0; p < 2; p++) b.ph32[p] = c.m32.ph[p];
     k.grid_begin = (c.g.N + 127) / 128;
@@ -1542,7 +1685,12 @@ void build_solver_sets(Ctx& c) {
     r.macro = c.macro; r.gate = GATE_ENDING; r.part = c.part_end; r.nblocks = c.nb_end; r.wgt = c.cfg.wgt;
 }
 
-template <typename T> static constexpr size_t nr_smem() { return (size_t)(NSTAGE + NS) * NR_BLOCK * sizeof(T); }
+// FP32 sweeps: the block's constant records and the copy barrier; FP64
+// sweeps: the per-element staging columns and the slip-rate columns
+template <typename T> static constexpr size_t nr_smem() {
+    return sizeof(T) == 4 ? (size_t)NRC_BLOCK_FLOATS * sizeof(float) + 16
+                          : (size_t)(NSTAGE + NS) * NR_BLOCK * sizeof(T);
+}
 template <typename T> static constexpr size_t nrb_smem() { return nr_smem<T>() + 72 * sizeof(T); }
 
 template <typename T> static void nr_attributes() {
