@@ -52,8 +52,8 @@ NR_DRAM_BYTES_PER_VOXEL = 487.8
 NR_ALG_VALUES_PER_VOXEL = 69
 # FP32 operations (2 per FFMA, 1 per FADD/FMUL) per Newton step of the FP32 NR sweep,
 # from the thread-level instruction counters of an ncu capture of every NR sweep of one
-# increment of the 96^3 / 422-grain RVE (2404 per voxel-sweep at 1.956 Newton steps)
-NR_FP32_FLOP_PER_NEWTON_STEP = 1229.0
+# increment of the 96^3 / 422-grain RVE (2267 per voxel-sweep at 1.956 Newton steps)
+NR_FP32_FLOP_PER_NEWTON_STEP = 1158.7
 # 152 SMs x 128 FP32 lanes x 2 FLOP x 2.07 GHz (maximum SM clock)
 FP32_PEAK_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
 FP32_PEAK_SOURCE = "derived: 152 SMs x 128 FP32 lanes x 2 FLOP/FFMA x 2070 MHz"
