@@ -134,6 +134,7 @@ struct MacroArgs {
     double* part2;        // [MACRO_BLOCKS][NPART_NR]
     unsigned int* ticket; // last-block detection, reset by the last block
     int f32rows;          // 1: rows hold float pairs (hi, lo) of the FP32 sweep, else doubles
+    int nblk;             // blocks of the first level (<= MACRO_BLOCKS, ~32 rows per block)
 };
 
 struct BeginArgs {

@@ -269,7 +269,7 @@ static cudaError_t build_tables_t(Batch& b) {
         for (Ctx* c : b.slots) {
             const int t = head_tail_fp32(*c) ? 1 : 0;
             m.push_back(c->ks->mac);
-            gm.push_back(MACRO_BLOCKS);
+            gm.push_back(c->ks->mac.nblk);
             bg[t].push_back(c->ks->beg);
             bg[t].back().gate = GATE_BEGIN;
             gb[t].push_back(c->ks->grid_begin);

@@ -1016,7 +1016,7 @@ __device__ __forceinline__ void macro_body_t(const MacroArgs& a, int bid) {
     Macro* m = a.macro;
     __shared__ A red[NPART_NR][8];
     __shared__ bool last;
-    const int nb = MACRO_BLOCKS;
+    const int nb = a.nblk;
     const int per = (a.nrows + nb - 1) / nb;
     const int r0 = bid * per, r1 = min(a.nrows, r0 + per);
     A v[NPART_NR];
@@ -1183,7 +1183,6 @@ __device__ __forceinline__ void begin_rates(const BeginArgs& a, int v, int ph, c
         for (int q = 0; q < 5; q++) {
             a.schm64[(size_t)(s * 5 + q) * N + v] = (double)o6[q];
             if (a.schm32) a.schm32[(size_t)(s * 5 + q) * N + v] = (float)o6[q];
-            if (a.nrc32) a.nrc32[nrc_index(v, s, q >> 2) + (q & 3)] = (float)o6[q];
         }
     }
     R rs[NS];
@@ -1222,9 +1221,15 @@ __device__ __forceinline__ void begin_rates(const BeginArgs& a, int v, int ph, c
             a.fc64[(size_t)(12 * q + i) * N + v] = (double)f4[q];
             if (a.fc32) a.fc32[(size_t)(12 * q + i) * N + v] = (float)f4[q];
         }
-        if (a.nrc32)
-#pragma unroll
-            for (int q = 0; q < 3; q++) a.nrc32[nrc_index(v, i, 1) + 1 + q] = (float)f4[q];
+        // the voxel's NR constant record of this system, both 16-byte halves
+        // together (a whole 32-byte sector): the Schmid vector stored above by
+        // this thread, passing stress, 1/(tau0 + tau_cut), gamma0_dot
+        if (a.nrc32) {
+            const float* sc = a.schm32 + (size_t)(i * 5) * N + v;
+            *reinterpret_cast<float4*>(a.nrc32 + nrc_index(v, i, 0)) = make_float4(sc[0], sc[N], sc[2 * (size_t)N], sc[3 * (size_t)N]);
+            *reinterpret_cast<float4*>(a.nrc32 + nrc_index(v, i, 1)) =
+                make_float4(sc[4 * (size_t)N], (float)f4[0], (float)f4[1], (float)f4[2]);
+        }
     }
 }
 
@@ -1656,6 +1661,9 @@ void build_solver_sets(Ctx& c) {
     MacroArgs& m = k.mac;
     m.cfg = c.cfg; m.macro = c.macro; m.part = c.part_nr; m.nrows = c.nb_nr * (NR_BLOCK / 32);
     m.part2 = c.part_nr2; m.ticket = c.ticket; m.f32rows = c.precision != 0;
+    // first-level blocks: ~32 warp rows each, at most MACRO_BLOCKS (a small RVE
+    // does not pay for 64 blocks with a fence and a ticket each)
+    m.nblk = m.nrows / 32 < 1 ? 1 : (m.nrows / 32 > MACRO_BLOCKS ? MACRO_BLOCKS : m.nrows / 32);
     BeginArgs& b = k.beg;
     b.mat = c.m64; b.g = c.g; b.macro = c.macro; b.gate = GATE_BEGIN;
     b.dg64 = c.dg64; b.dg_old = c.dg_old; b.tranmat = c.tranmat; b.rho_s = c.rho_s;
@@ -1725,7 +1733,7 @@ cudaError_t launch_nr(Ctx& c, int refine, int gate) {
 
 cudaError_t launch_macro(Ctx& c) {
     prof_mark(c, PG_MACRO, true);
-    k_macro<<<MACRO_BLOCKS, 256, 0, c.stream>>>(c.ks->mac);
+    k_macro<<<c.ks->mac.nblk, 256, 0, c.stream>>>(c.ks->mac);
     prof_mark(c, PG_MACRO, false);
     return cudaGetLastError();
 }
