@@ -217,7 +217,8 @@ struct EndReduceArgs {
 
 // Fused z and y passes: one CTA per (x plane, component pair), warp-register
 // FFTs along z and y, the plane's half spectra staged in shared memory.
-constexpr int PLANE_THREADS = 1024;
+constexpr int PLANE_THREADS = 512;
+constexpr int PLANE_MIN_BLOCKS = 2;  // FP32: two CTAs (one plane of one component each) per SM
 constexpr int PLANE_WARPS = PLANE_THREADS / 32;
 
 template <typename T> struct PlaneArgs {

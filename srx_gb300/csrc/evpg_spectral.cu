@@ -318,18 +318,19 @@ __device__ __forceinline__ void inv_z_body(const ZArgs<T>& a, int bid, unsigned 
 
 // ---- fused z+y passes on x planes (power-of-two n1 == n2 = 32*E)
 //
-// Forward, CTA (x, pair p): every warp takes z rows of the plane, loads
-// sig[2p] + i sig[2p+1] (coalesced), transforms it in registers, splits the
-// two half spectra through a per-warp row buffer into the shared planes A and
-// B; then every warp takes kz columns of A and B and transforms them along y
-// in registers, in place; finally the planes are stored contiguously
-// (spec[c][x] is one n1*nh block). Inverse, CTA (plane x, components 2p and
-// 2p+1, p < 4) or (component 8, planes 2j and 2j+1), so no CTA carries a
-// single component except an odd last plane: load the two half planes,
-// inverse along y in place, then per z row the Hermitian pair is rebuilt,
-// inverse-transformed in registers and added to DisGrad (same update as the
-// separate inverse-z pass). No intermediate spectrum goes through global
-// memory between the z and y transforms.
+// One CTA per (x plane, component). Forward: every warp takes pairs of z rows
+// (2j, 2j+1) of the component, loads row 2j + i row 2j+1 (coalesced),
+// transforms it in registers and splits the two rows' half spectra through a
+// per-warp row buffer into the shared half-spectrum plane; then every warp
+// takes kz columns of the plane and transforms them along y in registers, in
+// place; finally the plane is stored contiguously (spec[c][x] is one n1*nh
+// block). Inverse: load the half plane, inverse along y in place, then per
+// pair of z rows the Hermitian spectra of both rows are combined, inverse-
+// transformed in registers (real part row 2j, imaginary part row 2j+1) and
+// added to DisGrad (same update as the separate inverse-z pass). No
+// intermediate spectrum goes through global memory between the z and y
+// transforms. Pairing rows of one component (instead of two components) keeps
+// one plane per CTA: ~88 KB of shared memory in FP32 at 128^2, two CTAs per SM.
 
 // Shared-memory row skew of the plane kernels: row r is stored at r + r/16.
 // The warp FFTs scatter their outputs to rows k2 + E*brev5(lane), which
@@ -342,53 +343,54 @@ template <typename T, int E>
 __device__ __forceinline__ void plane_fwd_body(const PlaneArgs<T>& a, int bid, unsigned char* smem) {
     const Grid& g = a.g;
     const int n = g.n2, nh = g.nh, nhp = a.nhp;
-    const int x = bid / 3, p = bid - 3 * x;
+    const int x = bid / 6, c = bid - 6 * x;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     C2<T>* twz = reinterpret_cast<C2<T>*>(smem);
     C2<T>* twy = twz + n;
-    C2<T>* SA = twy + g.n1;
-    C2<T>* SB = SA + (size_t)plane_rows(g.n1) * nhp;
-    C2<T>* R = SB + (size_t)plane_rows(g.n1) * nhp + (size_t)warp * plane_rows(n);
+    C2<T>* S = twy + g.n1;
+    C2<T>* R = S + (size_t)plane_rows(g.n1) * nhp + (size_t)warp * plane_rows(n);
     for (int i = threadIdx.x; i < n; i += blockDim.x) twz[i] = a.twz[i];
     for (int i = threadIdx.x; i < g.n1; i += blockDim.x) twy[i] = a.twy[i];
     __syncthreads();
     // one set of lane constants serves both axes (n1 == n2)
     WarpTw<T, E> wt;
     wt.init(twz, lane);
-    const T* sa = a.sig + (size_t)(2 * p) * g.N + (size_t)x * g.n1 * n;
-    const T* sb = a.sig + (size_t)(2 * p + 1) * g.N + (size_t)x * g.n1 * n;
-    // rows are software-pipelined: the next row's loads are in flight while
-    // the current row is transformed
+    const T* s0 = a.sig + (size_t)c * g.N + (size_t)x * g.n1 * n;
+    const int npair = g.n1 / 2;
+    // row pairs are software-pipelined: the next pair's loads are in flight
+    // while the current pair is transformed
     C2<T> nxt[E];
-    if (warp < g.n1)
+    if (warp < npair)
 #pragma unroll
-        for (int q = 0; q < E; q++) nxt[q] = mk<T>(sa[(size_t)warp * n + lane + 32 * q], sb[(size_t)warp * n + lane + 32 * q]);
-    for (int y = warp; y < g.n1; y += PLANE_WARPS) {
+        for (int q = 0; q < E; q++)
+            nxt[q] = mk<T>(s0[(size_t)(2 * warp) * n + lane + 32 * q], s0[(size_t)(2 * warp + 1) * n + lane + 32 * q]);
+    for (int j = warp; j < npair; j += PLANE_WARPS) {
         C2<T> v[E];
 #pragma unroll
         for (int q = 0; q < E; q++) v[q] = nxt[q];
-        const int yn = y + PLANE_WARPS;
-        if (yn < g.n1)
+        const int jn = j + PLANE_WARPS;
+        if (jn < npair)
 #pragma unroll
-            for (int q = 0; q < E; q++) nxt[q] = mk<T>(sa[(size_t)yn * n + lane + 32 * q], sb[(size_t)yn * n + lane + 32 * q]);
+            for (int q = 0; q < E; q++)
+                nxt[q] = mk<T>(s0[(size_t)(2 * jn) * n + lane + 32 * q], s0[(size_t)(2 * jn + 1) * n + lane + 32 * q]);
         warp_fft<T, E, -1>(v, wt);
         const int b = brev5(lane);
 #pragma unroll
         for (int k2 = 0; k2 < E; k2++) R[pskew(k2 + E * b)] = v[k2];
         __syncwarp();
+        C2<T>* r0 = S + (size_t)pskew(2 * j) * nhp;
+        C2<T>* r1 = S + (size_t)pskew(2 * j + 1) * nhp;
         for (int k = lane; k < nh; k += 32) {
             const C2<T> z = R[pskew(k)];
             const C2<T> w = R[pskew(k == 0 ? 0 : n - k)];
-            // A = (Z(k) + conj Z(n-k))/2, B = (Z(k) - conj Z(n-k))/(2i)
-            SA[pskew(y) * nhp + k] = mk<T>((T)0.5 * (z.x + w.x), (T)0.5 * (z.y - w.y));
-            SB[pskew(y) * nhp + k] = mk<T>((T)0.5 * (z.y + w.y), (T)-0.5 * (z.x - w.x));
+            // row 2j: (Z(k) + conj Z(n-k))/2, row 2j+1: (Z(k) - conj Z(n-k))/(2i)
+            r0[k] = mk<T>((T)0.5 * (z.x + w.x), (T)0.5 * (z.y - w.y));
+            r1[k] = mk<T>((T)0.5 * (z.y + w.y), (T)-0.5 * (z.x - w.x));
         }
         __syncwarp();
     }
     __syncthreads();
-    for (int c = warp; c < 2 * nh; c += PLANE_WARPS) {
-        C2<T>* S = (c < nh) ? SA : SB;
-        const int kz = (c < nh) ? c : c - nh;
+    for (int kz = warp; kz < nh; kz += PLANE_WARPS) {
         C2<T> v[E];
 #pragma unroll
         for (int q = 0; q < E; q++) v[q] = S[pskew(lane + 32 * q) * nhp + kz];
@@ -398,12 +400,10 @@ __device__ __forceinline__ void plane_fwd_body(const PlaneArgs<T>& a, int bid, u
         for (int k2 = 0; k2 < E; k2++) S[pskew(k2 + E * b) * nhp + kz] = v[k2];
     }
     __syncthreads();
-    C2<T>* oa = a.spec + (size_t)(2 * p) * g.Nh + (size_t)x * g.n1 * nh;
-    C2<T>* ob = a.spec + (size_t)(2 * p + 1) * g.Nh + (size_t)x * g.n1 * nh;
+    C2<T>* o = a.spec + (size_t)c * g.Nh + (size_t)x * g.n1 * nh;
     for (int i = threadIdx.x; i < g.n1 * nh; i += blockDim.x) {
         const int y = a.dnh.div(i), k = i - y * nh;
-        oa[i] = SA[pskew(y) * nhp + k];
-        ob[i] = SB[pskew(y) * nhp + k];
+        o[i] = S[pskew(y) * nhp + k];
     }
 }
 
@@ -411,46 +411,25 @@ template <typename T, int E>
 __device__ __forceinline__ void plane_inv_body(const PlaneArgs<T>& a, int bid, unsigned char* smem) {
     const Grid& g = a.g;
     const int n = g.n2, nh = g.nh, nhp = a.nhp;
-    // CTAs b < 4 n0: plane b/4, components (2p, 2p+1) with p = b % 4; then
-    // component 8 of planes (2j, 2j+1), j = b - 4 n0 (one plane when 2j+1 == n0)
-    int xa, xb, ca, cb;
-    bool hasb;
-    if (bid < 4 * g.n0) {
-        xa = xb = bid >> 2;
-        ca = 2 * (bid & 3);
-        cb = ca + 1;
-        hasb = true;
-    } else {
-        const int j = bid - 4 * g.n0;
-        xa = 2 * j;
-        xb = 2 * j + 1;
-        ca = cb = 8;
-        hasb = xb < g.n0;
-        if (!hasb) xb = xa;
-    }
+    const int x = bid / 9, c = bid - 9 * x;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     C2<T>* twz = reinterpret_cast<C2<T>*>(smem);
     C2<T>* twy = twz + n;
-    C2<T>* SA = twy + g.n1;
-    C2<T>* SB = SA + (size_t)plane_rows(g.n1) * nhp;
-    C2<T>* R = SB + (size_t)plane_rows(g.n1) * nhp + (size_t)warp * plane_rows(n);
+    C2<T>* S = twy + g.n1;
+    C2<T>* R = S + (size_t)plane_rows(g.n1) * nhp + (size_t)warp * plane_rows(n);
     for (int i = threadIdx.x; i < n; i += blockDim.x) twz[i] = a.twz[i];
     for (int i = threadIdx.x; i < g.n1; i += blockDim.x) twy[i] = a.twy[i];
-    const C2<T>* ia = a.spec + (size_t)ca * g.Nh + (size_t)xa * g.n1 * nh;
-    const C2<T>* ib = a.spec + (size_t)cb * g.Nh + (size_t)xb * g.n1 * nh;
+    const C2<T>* in = a.spec + (size_t)c * g.Nh + (size_t)x * g.n1 * nh;
     for (int i = threadIdx.x; i < g.n1 * nh; i += blockDim.x) {
         const int y = a.dnh.div(i), k = i - y * nh;
-        cp_async_elem<T>(SA + pskew(y) * nhp + k, ia + i);
-        if (hasb) cp_async_elem<T>(SB + pskew(y) * nhp + k, ib + i);
+        cp_async_elem<T>(S + pskew(y) * nhp + k, in + i);
     }
     cp_async_wait_all();
     __syncthreads();
     // one set of lane constants serves both axes (n1 == n2)
     WarpTw<T, E> wt;
     wt.init(twz, lane);
-    for (int c = warp; c < (hasb ? 2 : 1) * nh; c += PLANE_WARPS) {
-        C2<T>* S = (c < nh) ? SA : SB;
-        const int kz = (c < nh) ? c : c - nh;
+    for (int kz = warp; kz < nh; kz += PLANE_WARPS) {
         C2<T> v[E];
 #pragma unroll
         for (int q = 0; q < E; q++) v[q] = S[pskew(lane + 32 * q) * nhp + kz];
@@ -460,24 +439,27 @@ __device__ __forceinline__ void plane_inv_body(const PlaneArgs<T>& a, int bid, u
         for (int k2 = 0; k2 < E; k2++) S[pskew(k2 + E * b) * nhp + kz] = v[k2];
     }
     __syncthreads();
-    const T ea = (T)a.dE9[ca], eb = hasb ? (T)a.dE9[cb] : (T)0;
-    for (int y = warp; y < g.n1; y += PLANE_WARPS) {
-        T* da = a.dg + (size_t)ca * g.N + ((size_t)xa * g.n1 + y) * n;
-        T* db = a.dg + (size_t)cb * g.N + ((size_t)xb * g.n1 + y) * n;
-        // DisGrad of this row, loaded before the transform hides its latency
-        T pa[E], pb[E];
+    const T e = (T)a.dE9[c];
+    const int npair = g.n1 / 2;
+    for (int j = warp; j < npair; j += PLANE_WARPS) {
+        T* d0 = a.dg + (size_t)c * g.N + ((size_t)x * g.n1 + 2 * j) * n;
+        T* d1 = d0 + n;
+        // DisGrad of the two rows, loaded before the transform hides its latency
+        T p0[E], p1[E];
 #pragma unroll
         for (int q = 0; q < E; q++) {
-            pa[q] = da[lane + 32 * q];
-            pb[q] = hasb ? db[lane + 32 * q] : (T)0;
+            p0[q] = d0[lane + 32 * q];
+            p1[q] = d1[lane + 32 * q];
         }
+        const C2<T>* r0 = S + (size_t)pskew(2 * j) * nhp;
+        const C2<T>* r1 = S + (size_t)pskew(2 * j + 1) * nhp;
         C2<T> v[E];
 #pragma unroll
         for (int q = 0; q < E; q++) {
             const int m = lane + 32 * q;
             const int mm = m < nh ? m : n - m;
-            const C2<T> u = SA[pskew(y) * nhp + mm];
-            const C2<T> w = hasb ? SB[pskew(y) * nhp + mm] : mk<T>((T)0, (T)0);
+            const C2<T> u = r0[mm];
+            const C2<T> w = r1[mm];
             if (m < nh) v[q] = mk<T>(u.x - w.y, u.y + w.x);   // u + i w
             else v[q] = mk<T>(u.x + w.y, -u.y + w.x);         // conj u + i conj w
         }
@@ -490,29 +472,29 @@ __device__ __forceinline__ void plane_inv_body(const PlaneArgs<T>& a, int bid, u
         for (int q = 0; q < E; q++) {
             const int m = lane + 32 * q;
             const C2<T> z = R[pskew(m)];
-            da[m] = pa[q] + (ea + z.x * a.invN);
-            if (hasb) db[m] = pb[q] + (eb + z.y * a.invN);
+            d0[m] = p0[q] + (e + z.x * a.invN);
+            d1[m] = p1[q] + (e + z.y * a.invN);
         }
         __syncwarp();
     }
 }
 
 template <typename T, int E>
-__global__ void __launch_bounds__(PLANE_THREADS) k_plane_fwd(const __grid_constant__ PlaneArgs<T> a) {
+__global__ void __launch_bounds__(PLANE_THREADS, sizeof(T) == 4 ? PLANE_MIN_BLOCKS : 1) k_plane_fwd(const __grid_constant__ PlaneArgs<T> a) {
     extern __shared__ __align__(16) unsigned char smem[];
     if (!gate_open(a.macro, a.gate)) return;
     plane_fwd_body<T, E>(a, blockIdx.x, smem);
 }
 
 template <typename T, int E>
-__global__ void __launch_bounds__(PLANE_THREADS) k_plane_inv(const __grid_constant__ PlaneArgs<T> a) {
+__global__ void __launch_bounds__(PLANE_THREADS, sizeof(T) == 4 ? PLANE_MIN_BLOCKS : 1) k_plane_inv(const __grid_constant__ PlaneArgs<T> a) {
     extern __shared__ __align__(16) unsigned char smem[];
     if (!gate_open(a.macro, a.gate)) return;
     plane_inv_body<T, E>(a, blockIdx.x, smem);
 }
 
 template <typename T, int E>
-__global__ void __launch_bounds__(PLANE_THREADS) kb_plane_fwd(const PlaneArgs<T>* __restrict__ tab,
+__global__ void __launch_bounds__(PLANE_THREADS, sizeof(T) == 4 ? PLANE_MIN_BLOCKS : 1) kb_plane_fwd(const PlaneArgs<T>* __restrict__ tab,
                                                               const int2* __restrict__ map) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int2 m = map[blockIdx.x];
@@ -522,7 +504,7 @@ __global__ void __launch_bounds__(PLANE_THREADS) kb_plane_fwd(const PlaneArgs<T>
 }
 
 template <typename T, int E>
-__global__ void __launch_bounds__(PLANE_THREADS) kb_plane_inv(const PlaneArgs<T>* __restrict__ tab,
+__global__ void __launch_bounds__(PLANE_THREADS, sizeof(T) == 4 ? PLANE_MIN_BLOCKS : 1) kb_plane_inv(const PlaneArgs<T>* __restrict__ tab,
                                                               const int2* __restrict__ map) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int2 m = map[blockIdx.x];
@@ -704,7 +686,7 @@ int plane_epl(const Grid& g, size_t elem) {
     const int E = g.n2 / 32;
     if (E * 32 != g.n2 || (E != 1 && E != 2 && E != 4)) return 0;
     const int nhp = g.nh | 1;
-    const size_t sm = (size_t)(g.n2 + g.n1 + 2 * plane_rows(g.n1) * nhp + PLANE_WARPS * plane_rows(g.n2)) * elem;
+    const size_t sm = (size_t)(g.n2 + g.n1 + plane_rows(g.n1) * nhp + PLANE_WARPS * plane_rows(g.n2)) * elem;
     return sm <= PLANE_SMEM_MAX ? E : 0;
 }
 
@@ -779,9 +761,9 @@ static void fill_spec_t(Ctx& c, SpecSet<T>& s, const int P[3], const FftPlan pl[
     pa.g = g; pa.macro = c.macro; pa.gate = GATE_RUNNING; pa.sig = sig; pa.dg = dg; pa.spec = spec;
     pa.twz = tw[2]; pa.twy = tw[1]; pa.dE9 = za.dE9; pa.invN = za.invN; pa.nhp = g.nh | 1;
     pa.dnh.set(g.nh);
-    s.grid_pf = 3 * g.n0;
-    s.grid_pi = 4 * g.n0 + (g.n0 + 1) / 2;
-    s.sm_p = (size_t)(g.n2 + g.n1 + 2 * plane_rows(g.n1) * pa.nhp + PLANE_WARPS * plane_rows(g.n2)) * es;
+    s.grid_pf = 6 * g.n0;
+    s.grid_pi = 9 * g.n0;
+    s.sm_p = (size_t)(g.n2 + g.n1 + plane_rows(g.n1) * pa.nhp + PLANE_WARPS * plane_rows(g.n2)) * es;
 }
 
 template <typename T>
