@@ -192,8 +192,13 @@ def gen_run(spec: dict, out: str) -> None:
                 "keep": np.array(spec["keep"])}
         for s in spec["keep"]:
             for k, v in read_fields(t, s, N).items():
-                data["%s_%d" % (k, s)] = v[idx]
+                if k in RUN_FIELDS:
+                    data["%s_%d" % (k, s)] = v[idx]
     np.savez_compressed(out, spec=json.dumps(spec), **data)
+
+
+# fields a multi-increment fixture keeps (stress, SSD density, accumulated slip)
+RUN_FIELDS = ("sig", "rho_s", "gam_acum")
 
 
 def final_state(p: str) -> dict:
