@@ -106,6 +106,10 @@ struct Batch {
     int precision = 0, nr_mode = 0;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
+    // the macro update runs on a side branch of the round graph, beside the
+    // next iteration's forward transforms (captured through these)
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     std::vector<Ctx*> slots;
     std::vector<long long> versions;
     bool dirty = true;
@@ -325,6 +329,17 @@ static int build_graph(Batch& b) {
     }
     k_round_start<<<1, ADVANCE_THREADS, 0, b.stream>>>(dm, n, b.dtk, b.dtk + 1, h);
     np++;
+    // forward transforms of the round's first iteration (the body computes
+    // those of the next iteration)
+    if (one) {
+        cudaStream_t cs = c0->stream;
+        c0->stream = b.stream;
+        launch_spectral(*c0, GATE_RUNNING, SPEC_FWD);
+        c0->stream = cs;
+        np += (c0->precision ? c0->ks->s32.epl : c0->ks->s64.epl) ? 2 : 3;
+    } else {
+        np += launch_spectral_batch(b.precision, b.L, b.stream, SPEC_FWD);
+    }
     std::vector<cudaGraphNode_t> deps;
     {
         cudaStreamCaptureStatus cst;
@@ -348,20 +363,38 @@ static int build_graph(Batch& b) {
     BCK(cudaGraphConditionalHandleCreate(&hif, b.graph, 0, cudaGraphCondAssignDefault));
     // body: the equilibrium iteration of every running RVE ...
     BCK(cudaStreamBeginCaptureToGraph(b.stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    // inverse transforms (DisGrad update) and the NR sweep, then the macro
+    // update on a side branch while the main branch computes the next
+    // iteration's forward transforms: they read the new stress and write only
+    // the spectrum buffer, and the macro update's results (loop test, mixed-BC
+    // correction) are needed first by the next inverse transforms. Per RVE the
+    // arithmetic is that of the launch-by-launch iteration.
     int nb = 0, nt = 0;
     if (one) {
         cudaStream_t cs = c0->stream;
         c0->stream = b.stream;
-        launch_spectral(*c0, GATE_RUNNING);
+        launch_spectral(*c0, GATE_RUNNING, SPEC_INV);
         launch_nr(*c0, 0, GATE_RUNNING);
+        BCK(cudaEventRecord(b.ev_fork, b.stream));
+        BCK(cudaStreamWaitEvent(b.side, b.ev_fork, 0));
+        c0->stream = b.side;
         launch_macro(*c0);
+        BCK(cudaEventRecord(b.ev_join, b.side));
+        c0->stream = b.stream;
+        launch_spectral(*c0, GATE_RUNNING, SPEC_FWD);
+        BCK(cudaStreamWaitEvent(b.stream, b.ev_join, 0));
         const int fused = c0->precision ? c0->ks->s32.epl : c0->ks->s64.epl;
         nb = (fused ? 3 : 5) + 2;
         c0->stream = cs;
     } else {
-        nb = launch_spectral_batch(b.precision, b.L, b.stream) + 2;
+        nb = launch_spectral_batch(b.precision, b.L, b.stream, SPEC_INV) + 2;
         launch_nr_batch(b.precision, b.nr_mode, b.L[BL_NR], b.stream);
-        launch_macro_batch(b.L[BL_MACRO], b.stream);
+        BCK(cudaEventRecord(b.ev_fork, b.stream));
+        BCK(cudaStreamWaitEvent(b.side, b.ev_fork, 0));
+        launch_macro_batch(b.L[BL_MACRO], b.side);
+        BCK(cudaEventRecord(b.ev_join, b.side));
+        nb += launch_spectral_batch(b.precision, b.L, b.stream, SPEC_FWD);
+        BCK(cudaStreamWaitEvent(b.stream, b.ev_join, 0));
     }
     k_if_ending<<<1, ADVANCE_THREADS, 0, b.stream>>>(dm, n, b.dtk, hif);
     nb++;
@@ -530,6 +563,9 @@ static void destroy_batch(Batch* b) {
     if (b->htk) cudaFreeHost(b->htk);
     if (b->hctl) cudaFreeHost(b->hctl);
     if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
+    if (b->side) cudaStreamDestroy(b->side);
+    if (b->ev_fork) cudaEventDestroy(b->ev_fork);
+    if (b->ev_join) cudaEventDestroy(b->ev_join);
     delete b;
 }
 
@@ -544,6 +580,9 @@ static int create_batch(int precision, int nr_mode, cudaStream_t stream, Batch**
         e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
         b->own_stream = e == cudaSuccess;
     }
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc((void**)&b->dtk, 3 * sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(b->dtk, 0, 3 * sizeof(int));
     if (e == cudaSuccess) e = cudaMallocHost((void**)&b->htk, 3 * sizeof(int));

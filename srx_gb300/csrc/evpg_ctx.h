@@ -130,7 +130,10 @@ enum BatchKind { BL_Z, BL_YF, BL_X, BL_YI, BL_NR, BL_MACRO, BL_MBEGIN, BL_BEGIN,
 // slots in BL_XW* (1, 2, 4 elements per lane) and the shared-memory kernel over
 // those in BL_X; launches with no slot are skipped. Returns the number of
 // kernels launched.
-int launch_spectral_batch(int precision, const BatchLaunch* L, cudaStream_t st);
+// parts of the spectral chain: all passes, the forward transforms with the X
+// pass (they write only the spectrum buffer), the inverse transforms
+enum SpecPart { SPEC_ALL = 0, SPEC_FWD = 1, SPEC_INV = 2 };
+int launch_spectral_batch(int precision, const BatchLaunch* L, cudaStream_t st, int part = SPEC_ALL);
 int plane_epl(const Grid& g, size_t elem_bytes);
 // NR sweep, macro update for every slot
 cudaError_t launch_nr_batch(int precision, int nr_mode, const BatchLaunch& L, cudaStream_t st);
@@ -149,7 +152,7 @@ bool head_tail_fp32(const Ctx& c);
 // Launchers of one RVE's kernels on its stream; `gate` selects when a launch
 // does work (Gate).
 // spectral chain of one iteration in the working precision
-cudaError_t launch_spectral(Ctx& c, int gate);
+cudaError_t launch_spectral(Ctx& c, int gate, int part = SPEC_ALL);
 // NR sweep: refine = 0 inside the loop (working precision), 1 the FP64
 // refinement of the FP32-bulk form at the end of the loop
 cudaError_t launch_nr(Ctx& c, int refine, int gate);

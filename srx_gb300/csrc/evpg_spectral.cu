@@ -869,67 +869,80 @@ void spectral_attributes() {
     spec_attributes<float>();
 }
 
+// part: SPEC_ALL, SPEC_FWD (forward transforms and the X pass with the Green
+// contraction: they write only the spectrum buffer) or SPEC_INV (inverse
+// transforms with the DisGrad update).
 template <typename T>
-static cudaError_t spectral_t(Ctx& c, int gate) {
+static cudaError_t spectral_t(Ctx& c, int gate, int part) {
     SpecSet<T>& s = spec_of<T>(*c.ks);
     ZArgs<T> za = s.z;
     YArgs<T> yf = s.yf, yi = s.yi;
     XArgs<T> xa = s.x;
     za.gate = yf.gate = yi.gate = xa.gate = gate;
+    const bool fwd = part != SPEC_INV, inv = part != SPEC_FWD;
     if (s.epl) {
         PlaneArgs<T> pa = s.pl;
         pa.gate = gate;
+        if (fwd) {
+            prof_mark(c, PG_FWD_Z, true);
+            plane_launch<T>(1, s.epl, s.grid_pf, s.sm_p, c.stream, pa);
+            prof_mark(c, PG_FWD_Z, false);
+            prof_mark(c, PG_X_GREEN, true);
+            x_launch<T>(s, xa, c.stream);
+            prof_mark(c, PG_X_GREEN, false);
+        }
+        if (inv) {
+            prof_mark(c, PG_INV_Z, true);
+            plane_launch<T>(0, s.epl, s.grid_pi, s.sm_p, c.stream, pa);
+            prof_mark(c, PG_INV_Z, false);
+        }
+        return cudaGetLastError();
+    }
+    if (fwd) {
         prof_mark(c, PG_FWD_Z, true);
-        plane_launch<T>(1, s.epl, s.grid_pf, s.sm_p, c.stream, pa);
+        k_fwd_z<T><<<s.grid_z, SPEC_THREADS, s.sm_z, c.stream>>>(za);
         prof_mark(c, PG_FWD_Z, false);
+        prof_mark(c, PG_FWD_Y, true);
+        k_y<T, -1><<<s.grid_y, SPEC_THREADS, s.sm_y, c.stream>>>(yf);
+        prof_mark(c, PG_FWD_Y, false);
         prof_mark(c, PG_X_GREEN, true);
         x_launch<T>(s, xa, c.stream);
         prof_mark(c, PG_X_GREEN, false);
-        prof_mark(c, PG_INV_Z, true);
-        plane_launch<T>(0, s.epl, s.grid_pi, s.sm_p, c.stream, pa);
-        prof_mark(c, PG_INV_Z, false);
-        return cudaGetLastError();
     }
-    prof_mark(c, PG_FWD_Z, true);
-    k_fwd_z<T><<<s.grid_z, SPEC_THREADS, s.sm_z, c.stream>>>(za);
-    prof_mark(c, PG_FWD_Z, false);
-    prof_mark(c, PG_FWD_Y, true);
-    k_y<T, -1><<<s.grid_y, SPEC_THREADS, s.sm_y, c.stream>>>(yf);
-    prof_mark(c, PG_FWD_Y, false);
-    prof_mark(c, PG_X_GREEN, true);
-    x_launch<T>(s, xa, c.stream);
-    prof_mark(c, PG_X_GREEN, false);
-    prof_mark(c, PG_INV_Y, true);
-    k_y<T, 1><<<s.grid_y, SPEC_THREADS, s.sm_y, c.stream>>>(yi);
-    prof_mark(c, PG_INV_Y, false);
-    prof_mark(c, PG_INV_Z, true);
-    k_inv_z<T><<<s.grid_z, SPEC_THREADS, s.sm_z, c.stream>>>(za);
-    prof_mark(c, PG_INV_Z, false);
+    if (inv) {
+        prof_mark(c, PG_INV_Y, true);
+        k_y<T, 1><<<s.grid_y, SPEC_THREADS, s.sm_y, c.stream>>>(yi);
+        prof_mark(c, PG_INV_Y, false);
+        prof_mark(c, PG_INV_Z, true);
+        k_inv_z<T><<<s.grid_z, SPEC_THREADS, s.sm_z, c.stream>>>(za);
+        prof_mark(c, PG_INV_Z, false);
+    }
     return cudaGetLastError();
 }
 
-cudaError_t launch_spectral(Ctx& c, int gate) {
-    return c.precision == 0 ? spectral_t<double>(c, gate) : spectral_t<float>(c, gate);
+cudaError_t launch_spectral(Ctx& c, int gate, int part) {
+    return c.precision == 0 ? spectral_t<double>(c, gate, part) : spectral_t<float>(c, gate, part);
 }
 
 // One pass of the spectral chain for a batch (see launch_spectral_batch).
 template <typename T>
-static int spectral_batch_t(const BatchLaunch* L, cudaStream_t st) {
+static int spectral_batch_t(const BatchLaunch* L, cudaStream_t st, int part) {
     const BatchLaunch &z = L[BL_Z], &yf = L[BL_YF], &x = L[BL_X], &yi = L[BL_YI];
     const int E[3] = {1, 2, 4};
+    const bool fwd = part != SPEC_INV, inv = part != SPEC_FWD;
     int n = 0;
-    for (int q = 0; q < 3; q++)
+    for (int q = 0; q < 3 && fwd; q++)
         if (L[BL_PF1 + q].nblk) {
             plane_launch_batch<T>(1, E[q], L[BL_PF1 + q], st);
             n++;
         }
-    if (z.nblk) {
+    if (fwd && z.nblk) {
         kb_fwd_z<T><<<z.nblk, SPEC_THREADS, z.smem, st>>>((const ZArgs<T>*)z.tab, z.map);
         kb_y<T, -1><<<yf.nblk, SPEC_THREADS, yf.smem, st>>>((const YArgs<T>*)yf.tab, yf.map);
         n += 2;
     }
     if constexpr (sizeof(T) == 4) {  // the warp-register X pass is FP32 only
-        for (int q = 0; q < 3; q++) {
+        for (int q = 0; q < 3 && fwd; q++) {
             const BatchLaunch& w = L[BL_XW1 + q];
             if (!w.nblk) continue;
             const XArgs<T>* tab = (const XArgs<T>*)w.tab;
@@ -939,16 +952,16 @@ static int spectral_batch_t(const BatchLaunch* L, cudaStream_t st) {
             n++;
         }
     }
-    if (x.nblk) {
+    if (fwd && x.nblk) {
         kb_x_green<T><<<x.nblk, SPEC_THREADS, x.smem, st>>>((const XArgs<T>*)x.tab, x.map);
         n++;
     }
-    if (z.nblk) {
+    if (inv && z.nblk) {
         kb_y<T, 1><<<yi.nblk, SPEC_THREADS, yi.smem, st>>>((const YArgs<T>*)yi.tab, yi.map);
         kb_inv_z<T><<<z.nblk, SPEC_THREADS, z.smem, st>>>((const ZArgs<T>*)z.tab, z.map);
         n += 2;
     }
-    for (int q = 0; q < 3; q++)
+    for (int q = 0; q < 3 && inv; q++)
         if (L[BL_PI1 + q].nblk) {
             plane_launch_batch<T>(0, E[q], L[BL_PI1 + q], st);
             n++;
@@ -956,8 +969,8 @@ static int spectral_batch_t(const BatchLaunch* L, cudaStream_t st) {
     return n;
 }
 
-int launch_spectral_batch(int precision, const BatchLaunch* L, cudaStream_t st) {
-    return precision == 0 ? spectral_batch_t<double>(L, st) : spectral_batch_t<float>(L, st);
+int launch_spectral_batch(int precision, const BatchLaunch* L, cudaStream_t st, int part) {
+    return precision == 0 ? spectral_batch_t<double>(L, st, part) : spectral_batch_t<float>(L, st, part);
 }
 
 // ------------------------------------------------------------- autotuner

@@ -78,13 +78,18 @@ def test_graph_increment_launch_count(tmp_path):
     evpg = _evpg()
     c = _cases(tmp_path)[0]
     with evpg.Job(c["input"], c["rho0"], precision=1, nr_mode=1) as j:
+        fused = j.variant()[0] > 0
         n0 = j.launches()
         it = j.increment(0)
         n1 = j.launches()
-    # prologue 3 (macro reset, head, round start); body: 5 spectral + NR +
-    # macro + tail test + advance = 9 per iteration; tail: fold + FP64
-    # refinement + tail 2 = 4, once
-    assert n1 - n0 == 3 + 9 * it + 4
+    # prologue: macro reset, head, round start and the first iteration's
+    # forward transforms with the X pass (2 with the fused plane kernels, else
+    # 3); body: inverse transforms, NR, macro update, the next iteration's
+    # forward transforms, tail test, advance = 9 per iteration with the
+    # separate passes (7 fused); tail: fold + FP64 refinement + tail 2 = 4, once
+    fwd = 2 if fused else 3
+    body = (3 if fused else 5) + 4
+    assert n1 - n0 == 3 + fwd + body * it + 4
 
 
 def test_batch_rejects_mixed_precision(tmp_path):
