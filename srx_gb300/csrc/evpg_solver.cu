@@ -349,12 +349,26 @@ __device__ __forceinline__ void mat6v(const T (&m)[6][6], const T* x, T* y) {
 // grain share it). FP64 rows hold S_gr (36) and the packed NR matrix base
 // S066 + sym(S_gr) (21); FP32 rows hold the packed sym(S_gr) alone (21), which
 // serves both (36 + 21 loads per Newton step become 21).
+// The 21 packed values of an FP32 orientation row (rows are 256-byte aligned):
+// five 128-bit loads and one scalar load.
+__device__ __forceinline__ void load_sym21(const float* sg, float (&u)[21]) {
+    const float4* s4 = reinterpret_cast<const float4*>(sg);
+#pragma unroll
+    for (int k = 0; k < 5; k++) {
+        const float4 t = __ldg(s4 + k);
+        u[4 * k] = t.x;
+        u[4 * k + 1] = t.y;
+        u[4 * k + 2] = t.z;
+        u[4 * k + 3] = t.w;
+    }
+    u[20] = __ldg(sg + 20);
+}
+
 template <typename T>
 __device__ __forceinline__ void sgr_v(const T* sg, const T* x, T* y) {
     if constexpr (sizeof(T) == 4) {
         T u[21];
-#pragma unroll
-        for (int k = 0; k < 21; k++) u[k] = __ldg(sg + k);
+        load_sym21(sg, u);
 #pragma unroll
         for (int i = 0; i < 6; i++) {
             T s = (T)0;
@@ -377,11 +391,13 @@ __device__ __forceinline__ void sgr_v(const T* sg, const T* x, T* y) {
 template <typename T>
 __device__ __forceinline__ void nr_matrix_base(const T* sg, const T (&S66)[6][6], T (&m)[21]) {
     if constexpr (sizeof(T) == 4) {
+        T u[21];
+        load_sym21(sg, u);
 #pragma unroll
         for (int i = 0; i < 6; i++)
 #pragma unroll
             for (int j = 0; j < 6; j++)
-                if (j >= i) m[sidx(i, j)] = S66[i][j] + __ldg(sg + sidx(i, j));
+                if (j >= i) m[sidx(i, j)] = S66[i][j] + u[sidx(i, j)];
     } else {
 #pragma unroll
         for (int k = 0; k < 21; k++) m[k] = __ldg(sg + 36 + k);
