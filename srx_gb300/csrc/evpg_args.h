@@ -124,6 +124,9 @@ template <typename T> struct NrArgs {
     // that already meets the NR tolerance is taken whole, without the trial
     // evaluation of its merit
     int quick_accept;
+    // 1 (FP64 refinement of the FP32-bulk form): corrections with an FP32
+    // Jacobian from the FP32 constant records (nrc) on FP64 residuals
+    int mixed;
 };
 
 struct MacroArgs {

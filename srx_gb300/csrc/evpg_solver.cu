@@ -128,7 +128,7 @@ __device__ __forceinline__ T resolved_shear(const T* cs, const T* s, int i, T (&
 template <typename T>
 __device__ __forceinline__ void flow_eval(const NrArgs<T>& a, int nsys, int v, const T* cs,
                                           const T (&s)[6], bool stale, T (&ed)[5], T (&dd)[15], T* gam,
-                                          bool& bad) {
+                                          bool& bad, bool want_dd = true) {
     const size_t N = a.g.N;
 #pragma unroll
     for (int q = 0; q < 5; q++) ed[q] = (T)0;
@@ -167,15 +167,17 @@ __device__ __forceinline__ void flow_eval(const NrArgs<T>& a, int nsys, int v, c
         T sh, ch;
         sinh_cosh((ar - tp) * itc, sh, ch);
         const T g = (rss > (T)0) ? go * sh : -(go * sh);
-        const T g2 = go * ch * itc;
 #pragma unroll
         for (int q = 0; q < 5; q++) ed[q] += sc[q] * g;
-        int k = 0;
+        if (want_dd) {
+            const T g2 = go * ch * itc;
+            int k = 0;
 #pragma unroll
-        for (int p = 0; p < 5; p++) {
-            const T w = sc[p] * g2;
+            for (int p = 0; p < 5; p++) {
+                const T w = sc[p] * g2;
 #pragma unroll
-            for (int q = p; q < 5; q++) dd[k++] += w * sc[q];
+                for (int q = p; q < 5; q++) dd[k++] += w * sc[q];
+            }
         }
         if (gam) gam[i * NR_BLOCK] = g;
     }
@@ -242,6 +244,32 @@ __device__ __forceinline__ void flow_eval_rec(const NrArgs<float>& a, int nsys, 
     bad = bad || nan;
 }
 
+// FP32 Jacobian of the flow rule, d_edot/d_sigma (upper triangle of the 5x5
+// deviatoric block), at stress s from the voxel's FP32 constant records in
+// global memory (the FP64 refinement's correction matrix).
+__device__ __forceinline__ void jac_rec32(const float* nrc, int v, int nsys, const float (&s)[6], float (&dd)[15]) {
+#pragma unroll
+    for (int q = 0; q < 15; q++) dd[q] = 0.f;
+#pragma unroll 1
+    for (int i = 0; i < nsys; i++) {
+        const float4 h0 = __ldg(reinterpret_cast<const float4*>(nrc + nrc_index(v, i, 0)));
+        const float4 h1 = __ldg(reinterpret_cast<const float4*>(nrc + nrc_index(v, i, 1)));
+        const float sc[5] = {h0.x, h0.y, h0.z, h0.w, h1.x};
+        const float rss = sc[0] * s[0] + sc[1] * s[1] + sc[2] * s[2] + sc[3] * s[3] + sc[4] * s[4];
+        if (!(fabsf(rss) > h1.y)) continue;
+        float sh, ch;
+        sinh_cosh((fabsf(rss) - h1.y) * h1.z, sh, ch);
+        const float g2 = h1.w * ch * h1.z;
+        int k = 0;
+#pragma unroll
+        for (int p = 0; p < 5; p++) {
+            const float w = sc[p] * g2;
+#pragma unroll
+            for (int q = p; q < 5; q++) dd[k++] += w * sc[q];
+        }
+    }
+}
+
 // Bulk copies global -> shared memory completing on an mbarrier (one phase).
 __device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
 __device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
@@ -290,9 +318,8 @@ __host__ __device__ constexpr int sidx(int i, int j) { return i * 6 - i * (i - 1
 // loops unroll whole and m stays in registers (triangular bounds left the
 // packed matrix in local memory).
 template <typename T>
-__device__ __forceinline__ bool ldl_solve(T (&m)[21], const T (&b)[6], T (&x)[6]) {
+__device__ __forceinline__ bool ldl_factor(T (&m)[21], T (&id)[6]) {
     // in place: m[sidx(k,i)] holds L(i,k) for i > k and d_k on the diagonal
-    T id[6];
     bool ok = true;
 #pragma unroll
     for (int j = 0; j < 6; j++) {
@@ -314,6 +341,11 @@ __device__ __forceinline__ bool ldl_solve(T (&m)[21], const T (&b)[6], T (&x)[6]
             }
         }
     }
+    return ok;
+}
+
+template <typename T>
+__device__ __forceinline__ void ldl_subst(const T (&m)[21], const T (&id)[6], const T (&b)[6], T (&x)[6]) {
     T y[6];
 #pragma unroll
     for (int i = 0; i < 6; i++) {
@@ -331,6 +363,13 @@ __device__ __forceinline__ bool ldl_solve(T (&m)[21], const T (&b)[6], T (&x)[6]
             if (k > i) t -= m[sidx(i, k)] * x[k];
         x[i] = t;
     }
+}
+
+template <typename T>
+__device__ __forceinline__ bool ldl_solve(T (&m)[21], const T (&b)[6], T (&x)[6]) {
+    T id[6];
+    const bool ok = ldl_factor<T>(m, id);
+    ldl_subst<T>(m, id, b, x);
     return ok;
 }
 
@@ -585,12 +624,79 @@ __device__ __forceinline__ void nr_body(const NrArgs<T>& a, int bid, unsigned ch
             if constexpr (sizeof(T) == 4) erral = cnr;  // squared step, against tolc
             else erral = fdiv(sqrt(cnr), signorm);
         };
+        // FP64 refinement of the FP32-bulk form (mixed): from the converged FP32
+        // stress, corrections with an FP32 Jacobian and LDL^T (from the FP32
+        // constant records) applied to FP64 residuals with FP64 flow-rule rates,
+        // until the step meets the FP64 NR tolerance. The Jacobian is rebuilt at
+        // the current stress when a step does not shrink; a voxel still not
+        // converged after MIX_ITMAX corrections goes through the FP64 line-search
+        // NR below from where it stands. The rates and slip rates kept are those
+        // of the evaluation before the last step, as in the line-search loop.
+        bool mixed_done = false;
+        if constexpr (sizeof(T) == 8) {
+            if (a.mixed) {
+                constexpr int MIX_ITMAX = 8;
+                float mf[21], idf[6];
+                bool need_jac = true;
+                T prev = (T)0;
+                for (int k = 0; k < MIX_ITMAX && !mixed_done; k++) {
+                    T ed[5], dd[15];
+                    flow_eval<T>(a, nsys, v, stg, sig, false, ed, dd, a.gamdot ? gam : nullptr, bad, false);
+                    if (bad) break;
+#pragma unroll
+                    for (int q = 0; q < 5; q++) edot_out[q] = ed[q];
+                    T Ss[6], dl[6], rhs[6];
+                    sgr_v<T>(sg, sig, Ss);
+#pragma unroll
+                    for (int c = 0; c < 6; c++) {
+                        te[c] = av[c] + (c < 5 ? ed[c] * dt : (T)0) + Ss[c];
+                        dl[c] = sig[c] - lam[c];
+                    }
+                    mat6v<T>(S66, dl, rhs);
+                    if (need_jac) {
+                        float s32[6], dd32[15];
+#pragma unroll
+                        for (int c = 0; c < 6; c++) s32[c] = (float)sig[c];
+                        jac_rec32(a.nrc, v, nsys, s32, dd32);
+                        const float dtf = (float)dt;
+#pragma unroll
+                        for (int q = 0; q < 21; q++) mf[q] = (float)__ldg(sg + 36 + q);
+                        {
+                            int q = 0;
+#pragma unroll
+                            for (int p = 0; p < 5; p++)
+#pragma unroll
+                                for (int r = p; r < 5; r++) mf[sidx(p, r)] += dtf * dd32[q++];
+                        }
+                        if (!ldl_factor<float>(mf, idf)) { sing = true; break; }
+                        need_jac = false;
+                    }
+                    float r32[6], x32[6];
+#pragma unroll
+                    for (int c = 0; c < 6; c++) r32[c] = (float)(rhs[c] + te[c]);
+                    ldl_subst<float>(mf, idf, r32, x32);
+                    T cnr = 0;
+#pragma unroll
+                    for (int c = 0; c < 6; c++) {
+                        old[c] = sig[c];
+                        sig[c] -= (T)x32[c];
+                        const T d = sig[c] - old[c];
+                        cnr += d * d;
+                    }
+                    it++;
+                    const T st = sqrt(cnr);
+                    if (st <= a.tol * signorm) mixed_done = true;
+                    else if (k > 0 && st > (T)0.5 * prev) need_jac = true;
+                    prev = st;
+                }
+            }
+        }
         // One flow-rule evaluation per pass. A pass at a line-search trial
         // point evaluates its merit; when the point is accepted, the Newton step
         // that starts there runs in the same pass with that evaluation (the
         // reference's next iteration reuses it too), so lanes of a warp that
         // accept trial points stay with lanes that take plain Newton steps.
-        for (;;) {
+        if (!mixed_done) for (;;) {
             if (!trial) {
                 if (!(it < a.itmax && fabs(erral) > tolc)) break;
                 it++;
@@ -1654,6 +1760,7 @@ static void nr_set(Ctx& c, NrSet<T>& S, const Material<T>& mat, T* sig, const T*
     a.macro = c.macro; a.part = c.part_nr; a.tol = tol; a.itmax = c.nr_itmax;
     a.nr_mode = c.nr_mode; a.stale_mode = stale_mode; a.gate = gate;
     a.quick_accept = 0;
+    a.mixed = 0;
     S.grid = c.nb_nr;
 }
 
@@ -1673,6 +1780,9 @@ void build_solver_sets(Ctx& c) {
         // is below the tolerance, and the slip rates it keeps are those of the
         // evaluation before that step (a change below the NR tolerance)
         k.nr64.a.quick_accept = 1;
+        // corrections with the FP32 Jacobian of the FP32 constant records
+        k.nr64.a.mixed = 1;
+        k.nr64.a.nrc = c.nrc32;
     }
     MacroArgs& m = k.mac;
     m.cfg = c.cfg; m.macro = c.macro; m.part = c.part_nr; m.nrows = c.nb_nr * (NR_BLOCK / 32);
