@@ -370,31 +370,42 @@ static int build_graph(Batch& b) {
     // correction) are needed first by the next inverse transforms. Per RVE the
     // arithmetic is that of the launch-by-launch iteration.
     int nb = 0, nt = 0;
+    cudaError_t fe = cudaSuccess;  // fork/join of the side branch
     if (one) {
         cudaStream_t cs = c0->stream;
         c0->stream = b.stream;
         launch_spectral(*c0, GATE_RUNNING, SPEC_INV);
         launch_nr(*c0, 0, GATE_RUNNING);
-        BCK(cudaEventRecord(b.ev_fork, b.stream));
-        BCK(cudaStreamWaitEvent(b.side, b.ev_fork, 0));
-        c0->stream = b.side;
-        launch_macro(*c0);
-        BCK(cudaEventRecord(b.ev_join, b.side));
-        c0->stream = b.stream;
+        fe = cudaEventRecord(b.ev_fork, b.stream);
+        if (fe == cudaSuccess) fe = cudaStreamWaitEvent(b.side, b.ev_fork, 0);
+        if (fe == cudaSuccess) {
+            c0->stream = b.side;
+            launch_macro(*c0);
+            fe = cudaEventRecord(b.ev_join, b.side);
+            c0->stream = b.stream;
+        }
         launch_spectral(*c0, GATE_RUNNING, SPEC_FWD);
-        BCK(cudaStreamWaitEvent(b.stream, b.ev_join, 0));
+        if (fe == cudaSuccess) fe = cudaStreamWaitEvent(b.stream, b.ev_join, 0);
         const int fused = c0->precision ? c0->ks->s32.epl : c0->ks->s64.epl;
         nb = (fused ? 3 : 5) + 2;
         c0->stream = cs;
     } else {
         nb = launch_spectral_batch(b.precision, b.L, b.stream, SPEC_INV) + 2;
         launch_nr_batch(b.precision, b.nr_mode, b.L[BL_NR], b.stream);
-        BCK(cudaEventRecord(b.ev_fork, b.stream));
-        BCK(cudaStreamWaitEvent(b.side, b.ev_fork, 0));
-        launch_macro_batch(b.L[BL_MACRO], b.side);
-        BCK(cudaEventRecord(b.ev_join, b.side));
+        fe = cudaEventRecord(b.ev_fork, b.stream);
+        if (fe == cudaSuccess) fe = cudaStreamWaitEvent(b.side, b.ev_fork, 0);
+        if (fe == cudaSuccess) {
+            launch_macro_batch(b.L[BL_MACRO], b.side);
+            fe = cudaEventRecord(b.ev_join, b.side);
+        }
         nb += launch_spectral_batch(b.precision, b.L, b.stream, SPEC_FWD);
-        BCK(cudaStreamWaitEvent(b.stream, b.ev_join, 0));
+        if (fe == cudaSuccess) fe = cudaStreamWaitEvent(b.stream, b.ev_join, 0);
+    }
+    if (fe != cudaSuccess) {
+        cudaGraph_t g_out = nullptr;
+        cudaStreamEndCapture(b.stream, &g_out);
+        if (one) c0->launches = saved;
+        return bfail(EVPG_ERR_CUDA, "body fork/join: %s", cudaGetErrorString(fe));
     }
     k_if_ending<<<1, ADVANCE_THREADS, 0, b.stream>>>(dm, n, b.dtk, hif);
     nb++;

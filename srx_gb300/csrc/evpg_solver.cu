@@ -511,6 +511,10 @@ __device__ __forceinline__ void stage_async(T* dst, const T* src) {
 __device__ __forceinline__ void stage_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void stage_wait() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
+// FP32 loop sweep: a Newton step no longer than 30 tolerances of |lambda|
+// (3e-4 at the default 1e-5) ends the NR; squared ratio
+constexpr float NR32_ACCEPT2 = 900.0f;
+
 template <typename T> struct NrMinBlocks { static constexpr int v = 2; };
 template <> struct NrMinBlocks<float> { static constexpr int v = 4; };
 
@@ -612,7 +616,7 @@ __device__ __forceinline__ void nr_body(const NrArgs<T>& a, int bid, unsigned ch
         }
         T ce = 0, cs = 0;
         T f_old = 0, slope = 0, alam = 1, alam2 = 0, alamin = 0;
-        bool trial = false;
+        bool trial = false, accepted = false;
         int it = 0, guard = 0;
         // end of a Newton or line-search step: the NR convergence measure
         // (evolution.c:386-391); the voxel's error terms of its last step are
@@ -831,6 +835,17 @@ __device__ __forceinline__ void nr_body(const NrArgs<T>& a, int bid, unsigned ch
                         for (int c = 0; c < 6; c++) sig[c] = old[c] + step[c];
                         whole = true;
                         finish = true;
+                    } else if (sizeof(T) == 4 && cnr <= NR32_ACCEPT2 * tolc) {
+                        // FP32 loop: a Newton step of relative length s <= 30 tol
+                        // (3e-4) leaves an error ~K s^2 (quadratic convergence), below
+                        // the tolerance for K up to ~100; the step that would confirm
+                        // it is, in FP32 at that distance, dominated by the rounding of
+                        // the residual's large terms. Take the step and end the NR.
+#pragma unroll
+                        for (int c = 0; c < 6; c++) sig[c] = old[c] + step[c];
+                        whole = true;
+                        finish = true;
+                        accepted = true;
                     }
                 }
                 if (!whole) {
@@ -872,6 +887,7 @@ __device__ __forceinline__ void nr_body(const NrArgs<T>& a, int bid, unsigned ch
                 }
             }
             if (finish) finish_step();
+            if (accepted) erral = (T)0;
         }
         // the voxel's error terms at the end of its last step
         {
