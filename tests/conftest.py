@@ -19,6 +19,10 @@ GOLDEN = os.path.join(ROOT, "tests", "golden")
 ORACLE_LIB = os.path.join(ROOT, "oracle", "_build", "libevporacle.so")
 ORACLE_BIN = os.path.join(ROOT, "oracle", "_build", "evp_oracle")
 X86 = platform.machine() in ("x86_64", "AMD64")
+# The oracle's OpenMP threads sleep at barriers instead of spinning: with a
+# core taken by another process, spinning threads that wait on a descheduled
+# one made a two-second 16^3 run take many minutes.
+os.environ.setdefault("OMP_WAIT_POLICY", "PASSIVE")
 
 
 def pytest_configure(config):
