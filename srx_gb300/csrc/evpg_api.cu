@@ -355,8 +355,10 @@ int evpg_create(const evpg_rve_desc* d, void** out) {
         AL(c->sig32, 6 * n); AL(c->ddg32, 9 * n); AL(c->b6_32, 6 * n); AL(c->schm32, 60 * n);
         AL(c->fc32, 48 * n); AL(c->sgr32, SGR_STRIDE * (size_t)(d->n_orient > 0 ? d->n_orient : 1));
         AL(c->nrc32, (size_t)c->nb_nr * NRC_BLOCK_FLOATS);
+        // nine spectrum components, the sum of the deferred antisymmetric ones
+        // and their pending values of the current iteration
         float2* sp = nullptr;
-        AL(sp, 9 * (size_t)c->g.Nh);
+        AL(sp, 15 * (size_t)c->g.Nh);
         c->spec = sp;
     } else {
         double2* sp = nullptr;
@@ -874,7 +876,7 @@ int evpg_estimate_bytes(const int32_t n[3], int32_t precision, int32_t n_orient,
     const long long nb_nr = (N + NR_BLOCK - 1) / NR_BLOCK, nb_end = (N + END_BLOCK - 1) / END_BLOCK;
     long long b = 8 * N * (6 + 9 + 9 + 6 + 5 + 12 + 12 + 12 + 12 + 9 + 60 + 48) + 8 * SGR_STRIDE * no + 4 * 2 * N;
     if (precision == EVPG_FP32_BULK)
-        b += 4 * N * (6 + 9 + 6 + 60 + 48) + 4 * SGR_STRIDE * no + 8 * 9 * Nh + 4 * nb_nr * NRC_BLOCK_FLOATS;
+        b += 4 * N * (6 + 9 + 6 + 60 + 48) + 4 * SGR_STRIDE * no + 8 * 15 * Nh + 4 * nb_nr * NRC_BLOCK_FLOATS;
     else b += 16 * 9 * Nh;
     b += 8 * nb_nr * (NR_BLOCK / 32) * NPART_NR + 8 * MACRO_BLOCKS * NPART_NR + 4 + 8 * nb_end * NPART_END;
     b += (long long)sizeof(Macro) + 24LL * (n[0] + n[1] + n[2]);

@@ -98,7 +98,16 @@ template <typename T> struct XArgs {
     // index divisors: n0, and np, n0*np for full tiles ([0], np = P) and the
     // last tile ([1], np = nh - (tiles - 1) P); nh (warp-register pass)
     FastDiv dn, dnp[2], dnnp[2], dnh;
+    // warp-register pass only. XM_ALL: nine components inverse-transformed
+    // along x. XM_DEFER: the antisymmetric three (A12, A13, A23), needed only
+    // at the end of the increment, are stored untransformed in the pass's lane
+    // order (the pending buffer; the inverse plane pass adds it to the sum),
+    // six inverse-transformed. XM_FLUSH: the sum inverse-transformed along x
+    // into components 6..8 of spec.
+    int mode;
+    C2<T>* dbuf;         // [3][n1*nh pencils][n0] lane order: pending (XM_DEFER) or sum (XM_FLUSH)
 };
+enum XMode { XM_ALL = 0, XM_DEFER = 1, XM_FLUSH = 2 };
 
 template <typename T> struct NrArgs {
     Material<T> mat;
@@ -157,6 +166,8 @@ struct BeginArgs {
     float* schm32;
     float* fc32;
     float* nrc32;        // FP32 NR constants (nrc_index), or null
+    float* acc;          // deferred antisymmetric spectrum (zeroed here), or null
+    int acc_floats;
     float* b6_32;
     float* ddg32;
     const double* epsp;
@@ -237,6 +248,17 @@ template <typename T> struct PlaneArgs {
     T invN;
     int nhp;             // row length of the shared-memory planes (odd, >= nh)
     FastDiv dnh;         // divisor nh of the plane copy loops
+    // inverse pass: components c0 .. c0+nc-1 of every x plane (all nine, the
+    // six symmetric ones when the antisymmetric part is deferred, or the three
+    // deferred ones at the end of the increment). With the part deferred, the
+    // pass of each iteration also adds the X pass's pending antisymmetric
+    // spectrum to its sum (flat, in slices over the CTAs; ncommit complex
+    // values) and CTA 0 adds dE9[6..8] to dE9_acc (the uniform part).
+    int nc, c0;
+    double* dE9_acc;
+    C2<T>* acc;
+    const C2<T>* pend;
+    int ncommit;
 };
 
 // Everything one RVE context launches, with grid sizes and dynamic shared
@@ -255,6 +277,13 @@ template <typename T> struct SpecSet {
     // warp-register X pass (xw = n0/32 elements per lane; 0: shared-memory pass)
     int xw, grid_xw;
     size_t sm_xw;
+    // FP32 with the warp-register X pass and the fused plane kernels: the
+    // antisymmetric part of the correction is accumulated in the spectrum and
+    // transformed once, at the end of the increment (xfl, pfl)
+    int defer;
+    XArgs<T> xfl;
+    PlaneArgs<T> pfl;
+    int grid_pfl;
 };
 
 template <typename T> struct NrSet {

@@ -196,8 +196,24 @@ static cudaError_t build_tables_t(Batch& b) {
         std::vector<PlaneArgs<T>> pa[3];
         std::vector<int> gf[3], gi[3];
         size_t smp[3] = {0, 0, 0};
+        // end-of-increment flush of the slots that defer the antisymmetric part
+        std::vector<XArgs<T>> xfl[3];
+        std::vector<PlaneArgs<T>> pfl[3];
+        std::vector<int> gxfl[3], gpfl[3];
+        size_t smxfl[3] = {0, 0, 0}, smpfl[3] = {0, 0, 0};
         for (Ctx* c : b.slots) {
             const SpecSet<T>& s = sset<T>(*c);
+            if (s.defer) {
+                const int q = s.xw == 1 ? 0 : s.xw == 2 ? 1 : 2;
+                xfl[q].push_back(s.xfl);
+                xfl[q].back().gate = GATE_ENDING;
+                gxfl[q].push_back(s.grid_xw);
+                if (s.sm_xw > smxfl[q]) smxfl[q] = s.sm_xw;
+                pfl[q].push_back(s.pfl);
+                pfl[q].back().gate = GATE_ENDING;
+                gpfl[q].push_back(s.grid_pfl);
+                if (s.sm_p > smpfl[q]) smpfl[q] = s.sm_p;
+            }
             if (s.xw) {
                 const int q = s.xw == 1 ? 0 : s.xw == 2 ? 1 : 2;
                 xw[q].push_back(s.x);
@@ -235,6 +251,10 @@ static cudaError_t build_tables_t(Batch& b) {
         if (e == cudaSuccess) e = put_table(b, BL_YI, yi, gy, smy);
         if (e == cudaSuccess) e = put_table(b, BL_X, x, gx, smx);
         for (int q = 0; q < 3 && e == cudaSuccess; q++) e = put_table(b, BL_XW1 + q, xw[q], gxw[q], smxw[q]);
+        for (int q = 0; q < 3 && e == cudaSuccess; q++) {
+            e = put_table(b, BL_XFL1 + q, xfl[q], gxfl[q], smxfl[q]);
+            if (e == cudaSuccess) e = put_table(b, BL_PFL1 + q, pfl[q], gpfl[q], smpfl[q]);
+        }
     }
     {
         std::vector<NrArgs<T>> nr;
@@ -439,7 +459,7 @@ static int build_graph(Batch& b) {
         if (c0->precision != 0) {
             launch_fold(*c0, GATE_ENDING);
             launch_nr(*c0, 1, GATE_ENDING);
-            nt += 2;
+            nt += 2 + spectral_flush_kernels(*c0);
         }
         launch_end(*c0, GATE_ENDING);
         nt += 2;

@@ -114,6 +114,7 @@ struct Macro {
     IncrCtl ctl;
     double dE[3][3];        // dDisGradAvg of the last iteration (upper triangle)
     double dE9[9];          // the same in the field representation (B basis + A12,A13,A23)
+    double dE9_acc[9];      // deferred antisymmetric part: sum of the dE9[6..8] applied so far
     double dE_acum[3][3];   // dDisGradAvg_acum
     double sig_avg[3][3], sig_avg1[3][3];
     double err_e, err_s, err_e_sum, err_s_sum;

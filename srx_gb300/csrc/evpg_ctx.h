@@ -123,7 +123,8 @@ struct BatchLaunch {
 };
 enum BatchKind { BL_Z, BL_YF, BL_X, BL_YI, BL_NR, BL_MACRO, BL_MBEGIN, BL_BEGIN, BL_FOLD,
                  BL_REFINE, BL_END, BL_ENDR, BL_PF1, BL_PF2, BL_PF4, BL_PI1, BL_PI2, BL_PI4,
-                 BL_XW1, BL_XW2, BL_XW4, BL_BEGIN32, BL_END32, BL_COUNT };
+                 BL_XW1, BL_XW2, BL_XW4, BL_BEGIN32, BL_END32, BL_XFL1, BL_XFL2, BL_XFL4,
+                 BL_PFL1, BL_PFL2, BL_PFL4, BL_COUNT };
 // Spectral chain of a batch: the separate z and y passes over the slots in
 // BL_Z/BL_YF/BL_YI, the fused plane kernels over the slots in BL_PF*/BL_PI*
 // (1, 2, 4 elements per lane), the X pass as the warp-register kernel over the
@@ -134,6 +135,8 @@ enum BatchKind { BL_Z, BL_YF, BL_X, BL_YI, BL_NR, BL_MACRO, BL_MBEGIN, BL_BEGIN,
 // pass (they write only the spectrum buffer), the inverse transforms
 enum SpecPart { SPEC_ALL = 0, SPEC_FWD = 1, SPEC_INV = 2 };
 int launch_spectral_batch(int precision, const BatchLaunch* L, cudaStream_t st, int part = SPEC_ALL);
+// end-of-increment flush of the slots that defer the antisymmetric part
+int launch_flush_batch(const BatchLaunch* L, cudaStream_t st);
 int plane_epl(const Grid& g, size_t elem_bytes);
 // NR sweep, macro update for every slot
 cudaError_t launch_nr_batch(int precision, int nr_mode, const BatchLaunch& L, cudaStream_t st);
@@ -153,6 +156,10 @@ bool head_tail_fp32(const Ctx& c);
 // does work (Gate).
 // spectral chain of one iteration in the working precision
 cudaError_t launch_spectral(Ctx& c, int gate, int part = SPEC_ALL);
+// end of the increment (before the fold): the deferred antisymmetric part of
+// the correction into DisGrad; no launch when the context does not defer it
+cudaError_t launch_spectral_flush(Ctx& c, int gate);
+int spectral_flush_kernels(const Ctx& c);
 // NR sweep: refine = 0 inside the loop (working precision), 1 the FP64
 // refinement of the FP32-bulk form at the end of the loop
 cudaError_t launch_nr(Ctx& c, int refine, int gate);

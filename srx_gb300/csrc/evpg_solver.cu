@@ -1229,7 +1229,10 @@ __device__ __forceinline__ void macro_begin(Macro* m) {
             m->dE[i][j] = 0.0;
             m->dE_acum[i][j] = 0.0;
         }
-    for (int q = 0; q < 9; q++) m->dE9[q] = 0.0;
+    for (int q = 0; q < 9; q++) {
+        m->dE9[q] = 0.0;
+        m->dE9_acc[q] = 0.0;
+    }
     m->err_e = c.err0;
     m->err_s = c.err0;
     m->iter = 0;
@@ -1389,6 +1392,9 @@ __device__ __forceinline__ void begin_body(const BeginArgs& a, int bid) {
     }
     const int ph = a.phase[v];
     const PhaseK<double>& P = a.mat.ph[ph - 1];
+    // the deferred antisymmetric spectrum starts the increment at zero
+    if (a.acc)
+        for (int i = v; i < a.acc_floats; i += N) a.acc[i] = 0.0f;
     if (a.b6_32) {
 #pragma unroll
         for (int c = 0; c < 6; c++) {
@@ -1812,6 +1818,8 @@ void build_solver_sets(Ctx& c) {
     b.rho_m = c.rho_m; b.phase = c.phase; b.schm64 = c.schm64; b.fc64 = c.fc64;
     b.schm32 = c.schm32; b.fc32 = c.fc32; b.b6_32 = c.b6_32; b.ddg32 = c.ddg32; b.epsp = c.epsp;
     b.nrc32 = c.nrc32;
+    b.acc = c.precision != 0 && c.ks->s32.defer ? reinterpret_cast<float*>(c.spec) + 18 * (size_t)c.g.Nh : nullptr;
+    b.acc_floats = (int)(6 * (size_t)c.g.Nh);
     b.rho_g = c.rho_g; b.gproj = c.gproj;
     for (int p = 0; p < 2; p++) b.ph32[p] = c.m32.ph[p];
     k.grid_begin = (c.g.N + 127) / 128;
@@ -1905,6 +1913,8 @@ cudaError_t launch_begin(Ctx& c, int gate) {
 }
 
 cudaError_t launch_fold(Ctx& c, int gate) {
+    const cudaError_t e = launch_spectral_flush(c, gate);
+    if (e != cudaSuccess) return e;
     FoldArgs a = c.ks->fold;
     a.gate = gate;
     c.launches++;
@@ -1963,6 +1973,7 @@ int launch_begin_batch(const BatchLaunch* L, cudaStream_t st) {
 int launch_end_batch(int precision, int nr_mode, const BatchLaunch* L, cudaStream_t st) {
     int n = 1;
     if (precision != 0) {
+        n += launch_flush_batch(L, st);
         const BatchLaunch& f = L[BL_FOLD];
         kb_fold<<<f.nblk, 256, 0, st>>>((const FoldArgs*)f.tab, f.map);
         const BatchLaunch& r = L[BL_REFINE];

@@ -205,11 +205,15 @@ __device__ __forceinline__ void x_warp_body(const XArgs<T>& a, const GreenK<T>& 
     const int p0 = bid * XW_PEN, np = min(XW_PEN, g.n1 * nh - p0);
     const size_t xs = (size_t)g.n1 * nh;
     const T rn[3] = {gk.rn[0], gk.rn[1], gk.rn[2]};
+    const int mode = a.mode;
+    // components inverse-transformed along x and stored: [clo, chi)
+    const int clo = mode == XM_FLUSH ? 6 : 0, chi = mode == XM_DEFER ? 6 : 9;
     load_tw<T>(tw, a.tw, n);
-    for (int i = threadIdx.x; i < 6 * n * XW_PEN; i += blockDim.x) {
-        const int kk = i % XW_PEN, row = i / XW_PEN, c = row >> LOGN, x = row & (n - 1);
-        if (kk < np) cp_async_elem<T>(tile + row * XW_ROW + kk, a.spec + (size_t)c * g.Nh + x * xs + p0 + kk);
-    }
+    if (mode != XM_FLUSH)
+        for (int i = threadIdx.x; i < 6 * n * XW_PEN; i += blockDim.x) {
+            const int kk = i % XW_PEN, row = i / XW_PEN, c = row >> LOGN, x = row & (n - 1);
+            if (kk < np) cp_async_elem<T>(tile + row * XW_ROW + kk, a.spec + (size_t)c * g.Nh + x * xs + p0 + kk);
+        }
     cp_async_wait_all();
     __syncthreads();
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -218,27 +222,46 @@ __device__ __forceinline__ void x_warp_body(const XArgs<T>& a, const GreenK<T>& 
         C2<T>* col = tile + w;
         WarpTw<T, E> wt;
         wt.init(tw, lane);
-        C2<T> v[6][E];
+        // the deferred components of this pencil, in the lane order of du:
+        // written to the pending buffer (XM_DEFER), read from the sum (XM_FLUSH)
+        const size_t npen = (size_t)g.n1 * nh;
+        C2<T>* dbuf = a.dbuf ? a.dbuf + (size_t)p * n + lane : nullptr;
+        if (mode != XM_FLUSH) {
+            C2<T> v[6][E];
 #pragma unroll
-        for (int c = 0; c < 6; c++)
+            for (int c = 0; c < 6; c++)
 #pragma unroll
-            for (int q = 0; q < E; q++) v[c][q] = col[(c * n + lane + 32 * q) * XW_ROW];
+                for (int q = 0; q < E; q++) v[c][q] = col[(c * n + lane + 32 * q) * XW_ROW];
 #pragma unroll
-        for (int c = 0; c < 6; c++) warp_fft<T, E, -1>(v[c], wt);
-        // lane l holds kx = k2 + E brev5(l) in v[.][k2]; du goes to the lane's
-        // own slots, which its inverse transforms read back in that order
-        const int kb = E * brev5(lane);
+            for (int c = 0; c < 6; c++) warp_fft<T, E, -1>(v[c], wt);
+            // lane l holds kx = k2 + E brev5(l) in v[.][k2]; du goes to the lane's
+            // own slots, which its inverse transforms read back in that order
+            const int kb = E * brev5(lane);
 #pragma unroll
-        for (int k2 = 0; k2 < E; k2++) {
-            C2<T> sb[6], du[9];
+            for (int k2 = 0; k2 < E; k2++) {
+                C2<T> sb[6], du[9];
 #pragma unroll
-            for (int c = 0; c < 6; c++) sb[c] = v[c][k2];
-            green_point<T, SHARED_C0>(gk, g, rn, k2 + kb, ky, kz, sb, du);
+                for (int c = 0; c < 6; c++) sb[c] = v[c][k2];
+                green_point<T, SHARED_C0>(gk, g, rn, k2 + kb, ky, kz, sb, du);
+                if (mode == XM_DEFER) {
 #pragma unroll
-            for (int c = 0; c < 9; c++) col[(c * n + lane + 32 * k2) * XW_ROW] = du[c];
+                    for (int c = 0; c < 6; c++) col[(c * n + lane + 32 * k2) * XW_ROW] = du[c];
+#pragma unroll
+                    for (int c = 6; c < 9; c++) dbuf[(size_t)(c - 6) * npen * n + 32 * k2] = du[c];
+                } else {
+#pragma unroll
+                    for (int c = 0; c < 9; c++) col[(c * n + lane + 32 * k2) * XW_ROW] = du[c];
+                }
+            }
+        } else {
+#pragma unroll
+            for (int c = 6; c < 9; c++)
+#pragma unroll
+                for (int q = 0; q < E; q++)
+                    col[(c * n + lane + 32 * q) * XW_ROW] = dbuf[(size_t)(c - 6) * npen * n + 32 * q];
         }
 #pragma unroll 1
-        for (int c = 0; c < 9; c++) {
+        for (int c = clo; c < chi; c++) {
             C2<T> u[E];
 #pragma unroll
             for (int q = 0; q < E; q++) u[q] = col[(c * n + lane + 32 * q) * XW_ROW];
@@ -248,8 +271,8 @@ __device__ __forceinline__ void x_warp_body(const XArgs<T>& a, const GreenK<T>& 
         }
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < 9 * n * XW_PEN; i += blockDim.x) {
-        const int kk = i % XW_PEN, row = i / XW_PEN, c = row >> LOGN, x = row & (n - 1);
+    for (int i = threadIdx.x; i < (chi - clo) * n * XW_PEN; i += blockDim.x) {
+        const int kk = i % XW_PEN, row = clo * n + i / XW_PEN, c = row >> LOGN, x = row & (n - 1);
         if (kk < np) a.spec[(size_t)c * g.Nh + x * xs + p0 + kk] = tile[row * XW_ROW + kk];
     }
 }
@@ -390,14 +413,44 @@ __device__ __forceinline__ void plane_fwd_body(const PlaneArgs<T>& a, int bid, u
         __syncwarp();
     }
     __syncthreads();
-    for (int kz = warp; kz < nh; kz += PLANE_WARPS) {
+    // y transforms of the n/2 + 1 columns as n/2 work items (a whole number per
+    // warp): the columns kz = 0 and n/2 hold real values (the DC and Nyquist
+    // terms of real rows), so one complex transform takes both, z = c0 + i cN,
+    // and is split like the rows: C0 = (Z(k) + conj Z(-k))/2, CN = (Z(k) -
+    // conj Z(-k))/(2i)
+    for (int item = warp; item < nh - 1; item += PLANE_WARPS) {
+        const int kz = item;
         C2<T> v[E];
+        if (item == 0) {
 #pragma unroll
-        for (int q = 0; q < E; q++) v[q] = S[pskew(lane + 32 * q) * nhp + kz];
+            for (int q = 0; q < E; q++) {
+                const int r = pskew(lane + 32 * q) * nhp;
+                v[q] = mk<T>(S[r].x, S[r + nh - 1].x);
+            }
+        } else {
+#pragma unroll
+            for (int q = 0; q < E; q++) v[q] = S[pskew(lane + 32 * q) * nhp + kz];
+        }
         warp_fft<T, E, -1>(v, wt);
         const int b = brev5(lane);
+        if (item == 0) {
 #pragma unroll
-        for (int k2 = 0; k2 < E; k2++) S[pskew(k2 + E * b) * nhp + kz] = v[k2];
+            for (int k2 = 0; k2 < E; k2++) R[pskew(k2 + E * b)] = v[k2];
+            __syncwarp();
+#pragma unroll
+            for (int q = 0; q < E; q++) {
+                const int k = lane + 32 * q;
+                const C2<T> z = R[pskew(k)];
+                const C2<T> w = R[pskew(k == 0 ? 0 : g.n1 - k)];
+                const int r = pskew(k) * nhp;
+                S[r] = mk<T>((T)0.5 * (z.x + w.x), (T)0.5 * (z.y - w.y));
+                S[r + nh - 1] = mk<T>((T)0.5 * (z.y + w.y), (T)-0.5 * (z.x - w.x));
+            }
+            __syncwarp();
+        } else {
+#pragma unroll
+            for (int k2 = 0; k2 < E; k2++) S[pskew(k2 + E * b) * nhp + kz] = v[k2];
+        }
     }
     __syncthreads();
     C2<T>* o = a.spec + (size_t)c * g.Nh + (size_t)x * g.n1 * nh;
@@ -411,7 +464,7 @@ template <typename T, int E>
 __device__ __forceinline__ void plane_inv_body(const PlaneArgs<T>& a, int bid, unsigned char* smem) {
     const Grid& g = a.g;
     const int n = g.n2, nh = g.nh, nhp = a.nhp;
-    const int x = bid / 9, c = bid - 9 * x;
+    const int x = bid / a.nc, c = a.c0 + (bid - a.nc * x);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     C2<T>* twz = reinterpret_cast<C2<T>*>(smem);
     C2<T>* twy = twz + n;
@@ -424,19 +477,70 @@ __device__ __forceinline__ void plane_inv_body(const PlaneArgs<T>& a, int bid, u
         const int y = a.dnh.div(i), k = i - y * nh;
         cp_async_elem<T>(S + pskew(y) * nhp + k, in + i);
     }
+    // while the plane arrives: the deferred antisymmetric components of this
+    // iteration into their sum, and their uniform correction (this pass runs
+    // only in iterations whose correction is applied, while the X pass that
+    // fills the pending buffer may run once more after the loop ended)
+    if (a.acc) {
+        const int ncta = a.nc * g.n0, nb = (a.ncommit + ncta - 1) / ncta;
+        const int e0 = bid * nb, e1 = min(e0 + nb, a.ncommit);
+        // CU elements per thread and round, all loads issued before the stores
+        constexpr int CU = 4;
+        for (int i0 = e0 + threadIdx.x; i0 < e1; i0 += CU * blockDim.x) {
+            C2<T> s[CU], d[CU];
+#pragma unroll
+            for (int u = 0; u < CU; u++) {
+                const int i = i0 + u * blockDim.x;
+                if (i < e1) {
+                    s[u] = a.acc[i];
+                    d[u] = a.pend[i];
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < CU; u++) {
+                const int i = i0 + u * blockDim.x;
+                if (i < e1) a.acc[i] = mk<T>(s[u].x + d[u].x, s[u].y + d[u].y);
+            }
+        }
+        if (bid == 0 && threadIdx.x == 0)
+#pragma unroll
+            for (int q = 6; q < 9; q++) a.dE9_acc[q] += a.dE9[q];
+    }
     cp_async_wait_all();
     __syncthreads();
     // one set of lane constants serves both axes (n1 == n2)
     WarpTw<T, E> wt;
     wt.init(twz, lane);
-    for (int kz = warp; kz < nh; kz += PLANE_WARPS) {
+    // n/2 work items: the columns kz = 0 and n/2 are spectra of real rows
+    // (Hermitian along y), so one complex inverse transform of C0 + i CN gives
+    // both, c0 in the real and cN in the imaginary part
+    for (int item = warp; item < nh - 1; item += PLANE_WARPS) {
+        const int kz = item;
         C2<T> v[E];
+        if (item == 0) {
 #pragma unroll
-        for (int q = 0; q < E; q++) v[q] = S[pskew(lane + 32 * q) * nhp + kz];
+            for (int q = 0; q < E; q++) {
+                const int r = pskew(lane + 32 * q) * nhp;
+                const C2<T> u = S[r], w = S[r + nh - 1];
+                v[q] = mk<T>(u.x - w.y, u.y + w.x);
+            }
+        } else {
+#pragma unroll
+            for (int q = 0; q < E; q++) v[q] = S[pskew(lane + 32 * q) * nhp + kz];
+        }
         warp_fft<T, E, 1>(v, wt);
         const int b = brev5(lane);
+        if (item == 0) {
 #pragma unroll
-        for (int k2 = 0; k2 < E; k2++) S[pskew(k2 + E * b) * nhp + kz] = v[k2];
+            for (int k2 = 0; k2 < E; k2++) {
+                const int r = pskew(k2 + E * b) * nhp;
+                S[r] = mk<T>(v[k2].x, (T)0);
+                S[r + nh - 1] = mk<T>(v[k2].y, (T)0);
+            }
+        } else {
+#pragma unroll
+            for (int k2 = 0; k2 < E; k2++) S[pskew(k2 + E * b) * nhp + kz] = v[k2];
+        }
     }
     __syncthreads();
     const T e = (T)a.dE9[c];
@@ -762,9 +866,40 @@ static void fill_spec_t(Ctx& c, SpecSet<T>& s, const int P[3], const FftPlan pl[
     pa.twz = tw[2]; pa.twy = tw[1]; pa.dE9 = za.dE9; pa.invN = za.invN; pa.nhp = g.nh | 1;
     pa.dnh.set(g.nh);
     s.grid_pf = 6 * g.n0;
-    s.grid_pi = 9 * g.n0;
     s.sm_p = (size_t)(g.n2 + g.n1 + plane_rows(g.n1) * pa.nhp + PLANE_WARPS * plane_rows(g.n2)) * es;
+    // FP32 with both warp-register passes: the antisymmetric components
+    // (A12, A13, A23) of the correction feed nothing in the loop (the NR reads
+    // the symmetric strain), so they are summed in the spectrum, in the X
+    // pass's lane order (a linear operation: the sum of the transforms is the
+    // transform of the sum), and transformed once before the fold at the end
+    // of the increment; their uniform part is summed in Macro::dE9_acc
+    s.defer = (sizeof(T) == 4 && s.xw && s.epl) ? 1 : 0;
+    double* acc9 = macro_field<double>(c.macro, offsetof(Macro, dE9_acc));
+    C2<T>* acc = spec + 9 * (size_t)g.Nh;   // the sum, zeroed by the increment head
+    C2<T>* pend = spec + 12 * (size_t)g.Nh; // this iteration's X pass output
+    xa.mode = s.defer ? XM_DEFER : XM_ALL;
+    xa.dbuf = s.defer ? pend : nullptr;
+    pa.nc = s.defer ? 6 : 9;
+    pa.c0 = 0;
+    pa.dE9_acc = s.defer ? acc9 : nullptr;
+    pa.acc = s.defer ? acc : nullptr;
+    pa.pend = s.defer ? pend : nullptr;
+    pa.ncommit = s.defer ? (int)(3 * (size_t)g.Nh) : 0;
+    s.grid_pi = pa.nc * g.n0;
+    s.xfl = xa;
+    s.xfl.mode = XM_FLUSH;
+    s.xfl.dbuf = s.defer ? acc : nullptr;
+    s.pfl = pa;
+    s.pfl.nc = 3;
+    s.pfl.c0 = 6;
+    s.pfl.dE9 = acc9;
+    s.pfl.dE9_acc = nullptr;
+    s.pfl.acc = nullptr;
+    s.pfl.pend = nullptr;
+    s.pfl.ncommit = 0;
+    s.grid_pfl = 3 * g.n0;
 }
+
 
 template <typename T>
 static void build_spec_t(Ctx& c, T* sig, T* dg, const C2<T>* const* tw) {
@@ -924,6 +1059,29 @@ cudaError_t launch_spectral(Ctx& c, int gate, int part) {
     return c.precision == 0 ? spectral_t<double>(c, gate, part) : spectral_t<float>(c, gate, part);
 }
 
+// End of the increment of a context that defers the antisymmetric part: its
+// X pass flush and inverse plane pass over components 6..8 (before the fold).
+template <typename T>
+static cudaError_t flush_t(Ctx& c, int gate) {
+    SpecSet<T>& s = spec_of<T>(*c.ks);
+    if (!s.defer) return cudaSuccess;
+    XArgs<T> xa = s.xfl;
+    PlaneArgs<T> pa = s.pfl;
+    xa.gate = pa.gate = gate;
+    c.launches += 2;
+    x_launch<T>(s, xa, c.stream);
+    plane_launch<T>(0, s.epl, s.grid_pfl, s.sm_p, c.stream, pa);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_spectral_flush(Ctx& c, int gate) {
+    return c.precision == 0 ? flush_t<double>(c, gate) : flush_t<float>(c, gate);
+}
+
+int spectral_flush_kernels(const Ctx& c) {
+    return c.precision != 0 && c.ks->s32.defer ? 2 : 0;
+}
+
 // One pass of the spectral chain for a batch (see launch_spectral_batch).
 template <typename T>
 static int spectral_batch_t(const BatchLaunch* L, cudaStream_t st, int part) {
@@ -971,6 +1129,24 @@ static int spectral_batch_t(const BatchLaunch* L, cudaStream_t st, int part) {
 
 int launch_spectral_batch(int precision, const BatchLaunch* L, cudaStream_t st, int part) {
     return precision == 0 ? spectral_batch_t<double>(L, st, part) : spectral_batch_t<float>(L, st, part);
+}
+
+// The flush of the slots that defer the antisymmetric part (FP32 only), per
+// lane layout: X pass flush, then the inverse plane pass over components 6..8.
+int launch_flush_batch(const BatchLaunch* L, cudaStream_t st) {
+    const int E[3] = {1, 2, 4};
+    int n = 0;
+    for (int q = 0; q < 3; q++) {
+        const BatchLaunch& w = L[BL_XFL1 + q];
+        if (!w.nblk) continue;
+        const XArgs<float>* tab = (const XArgs<float>*)w.tab;
+        if (q == 0) kb_x_warp<float, 1><<<w.nblk, XW_THREADS, w.smem, st>>>(tab, w.map);
+        else if (q == 1) kb_x_warp<float, 2><<<w.nblk, XW_THREADS, w.smem, st>>>(tab, w.map);
+        else kb_x_warp<float, 4><<<w.nblk, XW_THREADS, w.smem, st>>>(tab, w.map);
+        plane_launch_batch<float>(0, E[q], L[BL_PFL1 + q], st);
+        n += 2;
+    }
+    return n;
 }
 
 // ------------------------------------------------------------- autotuner
@@ -1304,6 +1480,7 @@ extern "C" int evpg_green_correction_noalloc(const double* sig6, double* du9, in
     const int ntile_y = (g.nh + ya.P - 1) / ya.P;
     XArgs<double> xa;
     xa.g = g; xa.pl = pl[0]; xa.macro = nullptr; xa.gate = GATE_ALWAYS; xa.spec = spec; xa.tw = twp[0];
+    xa.mode = XM_ALL; xa.dbuf = nullptr;
     xa.P = pick_p(18 * x_pencil_stride(n0, es), es, 150 * 1024);
     if (xa.P > g.nh) xa.P = g.nh;
     for (int i = 0; i < 81; i++) {

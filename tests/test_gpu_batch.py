@@ -79,6 +79,9 @@ def test_graph_increment_launch_count(tmp_path):
     c = _cases(tmp_path)[0]
     with evpg.Job(c["input"], c["rho0"], precision=1, nr_mode=1) as j:
         fused = j.variant()[0] > 0
+        # with both warp-register passes the deferred antisymmetric part adds
+        # its X pass flush and inverse plane pass to the tail
+        flush = 2 if fused and j.variant()[1] > 0 else 0
         n0 = j.launches()
         it = j.increment(0)
         n1 = j.launches()
@@ -89,7 +92,7 @@ def test_graph_increment_launch_count(tmp_path):
     # separate passes (7 fused); tail: fold + FP64 refinement + tail 2 = 4, once
     fwd = 2 if fused else 3
     body = (3 if fused else 5) + 4
-    assert n1 - n0 == 3 + fwd + body * it + 4
+    assert n1 - n0 == 3 + fwd + body * it + 4 + flush
 
 
 def test_batch_rejects_mixed_precision(tmp_path):
@@ -171,7 +174,7 @@ def test_batch_with_fused_planes_equals_alone(tmp_path):
     evpg = _evpg()
     cases = []
     for i, (grid, load, sps) in enumerate((((8, 32, 32), "tension", 2e-4), ((16, 32, 32), "shear", 1e-4),
-                                           ((4, 32, 32), "compression", 2e-4))):
+                                           ((4, 32, 32), "compression", 2e-4), ((32, 32, 32), "shear", 1e-4))):
         job = rve.Job(n=grid, load=load, rate=1e-3, strain_per_step=sps, n_steps=2)
         cases.append(rve.make_case(str(tmp_path / ("f%d" % i)), grid, 5, 40 + i, job, rho0=(0.5, 5.0)))
     ref = []
@@ -181,7 +184,10 @@ def test_batch_with_fused_planes_equals_alone(tmp_path):
             ref.append(([j.increment(k) for k in range(2)], _state(evpg, j)))
     jobs = [evpg.Job(c["input"], c["rho0"], precision=1, nr_mode=1) for c in cases]
     try:
-        its, _ = evpg.run_batched(jobs, [2, 2, 2], max_ticks=19)
+        # the 32^3 slot also runs the warp-register X pass: its antisymmetric
+        # correction is deferred to the end of each increment
+        assert [j.variant()[1] > 0 for j in jobs] == [False, False, False, True]
+        its, _ = evpg.run_batched(jobs, [2, 2, 2, 2], max_ticks=19)
         assert its == [r[0] for r in ref]
         for j, (_, st) in zip(jobs, ref):
             got = _state(evpg, j)
@@ -319,3 +325,38 @@ def test_warp_x_pass_equals_shared_memory_pass(tmp_path, n0):
     assert rel_err(res[1][2][7:16], res[0][2][7:16]) < 1e-5
     l2 = np.linalg.norm(res[1][1] - res[0][1]) / np.linalg.norm(res[0][1])
     assert l2 < 1e-4, l2
+
+
+def test_deferred_antisymmetric_correction(tmp_path):
+    """FP32 bulk with both warp-register passes (32^3) sums the antisymmetric
+    part of the displacement-gradient correction (A12, A13, A23) in the
+    spectrum during the equilibrium loop and transforms it once, at the end of
+    the increment. Against the same shear increments with the shared-memory
+    X pass, which transforms all nine components every iteration: the
+    displacement gradient, the velocity gradient (whose antisymmetric part is
+    the spin that reorients the lattice), the orientation and the stress
+    within the form's tolerance."""
+    from conftest import rel_err
+    from srx_gb300 import rve
+    evpg = _evpg()
+    grid = (32, 32, 32)
+    job = rve.Job(n=grid, load="shear", rate=1e-3, strain_per_step=1e-4, n_steps=2)
+    c = rve.make_case(str(tmp_path / "c"), grid, 9, 77, job, rho0=(0.5, 5.0))
+    res = []
+    for mode in (1, 0):
+        with evpg.Job(c["input"], c["rho0"], precision=1, nr_mode=1) as j:
+            j.set_xpass(mode)
+            assert j.variant()[0] > 0 and (j.variant()[1] > 0) == bool(mode)
+            its = [j.increment(k) for k in range(2)]
+            res.append((its, [j.download(f) for f in (evpg.F_DISGRAD, evpg.F_VELGRAD, evpg.F_TRANMAT,
+                                                      evpg.F_SIG6)], j.scalars()))
+    assert abs(sum(res[0][0]) - sum(res[1][0])) <= 2
+    assert rel_err(res[0][2][7:16], res[1][2][7:16]) < 1e-5
+    for a, b in zip(res[0][1], res[1][1]):
+        l2 = np.linalg.norm(a - b) / np.linalg.norm(b)
+        assert l2 < 1e-4, l2
+    # the antisymmetric part is not negligible here: somewhere in the RVE the
+    # velocity gradient's spin reaches a percent of its symmetric part
+    vg = res[0][1][1].reshape(-1, 3, 3)
+    w = 0.5 * (vg - vg.transpose(0, 2, 1))
+    assert np.abs(w).max() > 0.01 * np.abs(0.5 * (vg + vg.transpose(0, 2, 1))).max()
