@@ -553,8 +553,11 @@ def gpu_arm(a, ws, rank, local):
                 "algorithmic_bytes_per_launch": alg[dom],
                 "traffic_over_algorithmic": traffic / alg[dom] if traffic else None}
     if dom == "nr":
-        roofline["note"] = ("the NR sweep is issue-bound (FP32 pipe); its HBM fraction is its distance "
-                            "from the memory roofline at %d B/voxel" % (NR_ALG_VALUES_PER_VOXEL * P))
+        roofline["note"] = ("the NR sweep is bound by the latency of its loads (ncu: long-scoreboard the "
+                            "largest stall, 56 %% of DRAM bandwidth, 44 %% of issue slots, 4 blocks of 4 "
+                            "warps per SM); its HBM fraction is its distance from the memory roofline at "
+                            "%d B/voxel, traffic the bytes its layout moves (per-system constant records)"
+                            % (NR_ALG_VALUES_PER_VOXEL * P))
         roofline["newton_steps_per_voxel_sweep"] = newton_per_sweep
         if NR_FP32_FLOP_PER_NEWTON_STEP and newton_per_sweep:
             fl = NR_FP32_FLOP_PER_NEWTON_STEP * newton_per_sweep * N / (pl["ms_per_launch"] / 1e3) / 1e12
