@@ -151,7 +151,11 @@ typedef struct evpg_incr_out {
 /* Fields for evpg_download / evpg_upload, [N][...] voxel-major, double. */
 typedef enum evpg_field {
     EVPG_F_SIG = 0,        /* [N][3][3] Sig */
-    EVPG_F_DISGRAD = 1,    /* [N][3][3] DisGrad */
+    EVPG_F_DISGRAD = 1,    /* [N][3][3] DisGrad (FP32-bulk contexts: the equilibrium loop's
+                              corrections, held in FP32 during the loop, their
+                              antisymmetric part summed in the spectrum, enter
+                              it at evpg_increment_end; between iterations the
+                              field holds the increment head's value) */
     EVPG_F_EPS = 2,        /* [N][3][3] Eps (plastic strain) */
     EVPG_F_EDOT = 3,       /* [N][3][3] Edot */
     EVPG_F_TRANMAT = 4,    /* [N][3][3] TranMat_xt2sa */
