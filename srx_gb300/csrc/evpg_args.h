@@ -15,11 +15,11 @@ constexpr int NPART_END = 19;  // rho_F, rho_P, rho_s, rho_m, d_dipole, d_forest
 // as [NS][NS] tables, then the sense vectors b x n (init.c:198-203).
 constexpr int GP_COS1 = 0, GP_SIN1 = 144, GP_COS2 = 288, GP_SIN2 = 432, GP_BP = 576,
               GP_STRIDE = 612;
-constexpr int NR_BLOCK = 32;
+constexpr int NR_BLOCK = 64;
 // FP32 NR constants, one 32-byte record per (voxel, slip system): Schmid
 // vector (5), passing stress, 1/(tau0 + tau_cut), gamma0_dot. Records of a
 // block of NR_BLOCK voxels are contiguous ([system][voxel in block][8]), so a
-// block's 12 KB arrive in shared memory by bulk copies; the two 16-byte
+// block's 24 KB arrive in shared memory by bulk copies; the two 16-byte
 // halves of a record are swapped for voxels with bit 2 of their position set,
 // which makes the 128-bit shared-memory reads of a warp conflict-free.
 constexpr int NRC_REC = 8;

@@ -515,12 +515,13 @@ __device__ __forceinline__ void stage_wait() { asm volatile("cp.async.wait_group
 // (3e-4 at the default 1e-5) ends the NR; squared ratio
 constexpr float NR32_ACCEPT2 = 900.0f;
 
-// Resident NR blocks per SM the register budget is set for: one-warp blocks,
-// 16 (FP32: 123 registers, 12 KB of records each) or 8 (FP64). Blocks of one
-// warp give the same FP32 sweep time as blocks of four (0.260 ms at 128^3),
-// an FP64 sweep 2.4 % and the FP64 refinement 4 % faster.
-template <typename T> struct NrMinBlocks { static constexpr int v = 8; };
-template <> struct NrMinBlocks<float> { static constexpr int v = 16; };
+// Resident NR blocks of two warps per SM the register budget is set for.
+// FP32: 9, as many as the 24 KB of constant records per block allow in
+// shared memory (18 warps per SM): the sweep then fits 96 registers without
+// spills, where an open budget took 123 and left 16 warps per SM (0.260 ->
+// 0.242 ms at 128^3). FP64: 4 (228 registers, 55 KB of staging per block).
+template <typename T> struct NrMinBlocks { static constexpr int v = 4; };
+template <> struct NrMinBlocks<float> { static constexpr int v = 9; };
 
 // One UpdateStress sweep (evolution.c:181-423). The line search of the
 // NR_MODIFIED build runs as a small state machine so the flow rule has a
@@ -545,7 +546,7 @@ __device__ __forceinline__ void nr_body(const NrArgs<T>& a, int bid, unsigned ch
     T pe = 0, ps = 0, ss[6] = {0, 0, 0, 0, 0, 0}, s1[6] = {0, 0, 0, 0, 0, 0};
     int nr = 0;
     bool bad = false, sing = false, lsfail = false, tmo = false, waited = false;
-    // FP32 sweeps: the block's constant records (12 KB) arrive by bulk copies
+    // FP32 sweeps: the block's constant records (24 KB) arrive by bulk copies
     // issued by one thread, overlapping the state loads of every thread
     unsigned long long* cbar = nullptr;
     if constexpr (sizeof(T) == 4) {
