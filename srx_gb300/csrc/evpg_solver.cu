@@ -1714,7 +1714,10 @@ __device__ __forceinline__ void end_body(const EndArgs& a, int bid) {
 }
 
 template <typename R>
-__global__ void __launch_bounds__(END_BLOCK) k_end(const __grid_constant__ EndArgs a) {
+// Register budget of six blocks per SM: 80 registers (48 bytes spilled)
+// instead of 96, 24 instead of 20 warps per SM; FP32-bulk tail 1.71 -> 1.52 ms
+// at 128^3.
+__global__ void __launch_bounds__(END_BLOCK, 6) k_end(const __grid_constant__ EndArgs a) {
     if (!gate_open(a.macro, a.gate)) return;
     end_body<R>(a, blockIdx.x);
 }
