@@ -1414,14 +1414,19 @@ __device__ __forceinline__ void begin_body(const BeginArgs& a, int bid) {
     else begin_rates<double>(a, v, ph, P);
 }
 
+// Register budget of the FP32 head: twelve blocks per SM (40 registers, 16
+// bytes spilled, 48 warps per SM instead of 32); the FP64 head keeps its own.
+template <typename R> struct BeginMinBlocks { static constexpr int v = 1; };
+template <> struct BeginMinBlocks<float> { static constexpr int v = 12; };
+
 template <typename R>
-__global__ void __launch_bounds__(128) k_begin(const __grid_constant__ BeginArgs a) {
+__global__ void __launch_bounds__(128, BeginMinBlocks<R>::v) k_begin(const __grid_constant__ BeginArgs a) {
     if (!gate_open(a.macro, a.gate)) return;
     begin_body<R>(a, blockIdx.x);
 }
 
 template <typename R>
-__global__ void __launch_bounds__(128) kb_begin(const BeginArgs* __restrict__ tab, const int2* __restrict__ map) {
+__global__ void __launch_bounds__(128, BeginMinBlocks<R>::v) kb_begin(const BeginArgs* __restrict__ tab, const int2* __restrict__ map) {
     const int2 m = map[blockIdx.x];
     const BeginArgs& a = tab[m.x];
     if (!gate_open(a.macro, a.gate)) return;
@@ -1723,7 +1728,7 @@ __global__ void __launch_bounds__(END_BLOCK, 6) k_end(const __grid_constant__ En
 }
 
 template <typename R>
-__global__ void __launch_bounds__(END_BLOCK) kb_end(const EndArgs* __restrict__ tab, const int2* __restrict__ map) {
+__global__ void __launch_bounds__(END_BLOCK, 6) kb_end(const EndArgs* __restrict__ tab, const int2* __restrict__ map) {
     const int2 m = map[blockIdx.x];
     const EndArgs& a = tab[m.x];
     if (!gate_open(a.macro, a.gate)) return;
