@@ -193,7 +193,10 @@ constexpr int XW_THREADS = 32 * XW_PEN;
 __host__ __device__ constexpr bool xw_eligible(int n0, size_t es) {
     return es == 8 && (n0 == 32 || n0 == 64 || n0 == 128);
 }
-__host__ __device__ constexpr size_t xw_smem(int n0, size_t es) { return (size_t)(n0 + 9 * n0 * XW_ROW) * es; }
+// rows: components the tile holds (9; 6 when the antisymmetric part is deferred)
+__host__ __device__ constexpr size_t xw_smem(int n0, size_t es, int rows = 9) {
+    return (size_t)(n0 + rows * n0 * XW_ROW) * es;
+}
 
 template <typename T, int E, bool SHARED_C0>
 __device__ __forceinline__ void x_warp_body(const XArgs<T>& a, const GreenK<T>& gk, int bid, unsigned char* smem) {
@@ -206,8 +209,10 @@ __device__ __forceinline__ void x_warp_body(const XArgs<T>& a, const GreenK<T>& 
     const size_t xs = (size_t)g.n1 * nh;
     const T rn[3] = {gk.rn[0], gk.rn[1], gk.rn[2]};
     const int mode = a.mode;
-    // components inverse-transformed along x and stored: [clo, chi)
-    const int clo = mode == XM_FLUSH ? 6 : 0, chi = mode == XM_DEFER ? 6 : 9;
+    // tile rows inverse-transformed along x and stored: [clo, chi), stored as
+    // spectrum components coff + row (the flush keeps the three deferred
+    // components in rows 0..2, so the deferring form's tile holds six rows)
+    const int clo = 0, chi = mode == XM_DEFER ? 6 : mode == XM_FLUSH ? 3 : 9, coff = mode == XM_FLUSH ? 6 : 0;
     load_tw<T>(tw, a.tw, n);
     if (mode != XM_FLUSH)
         for (int i = threadIdx.x; i < 6 * n * XW_PEN; i += blockDim.x) {
@@ -227,21 +232,25 @@ __device__ __forceinline__ void x_warp_body(const XArgs<T>& a, const GreenK<T>& 
         const size_t npen = (size_t)g.n1 * nh;
         C2<T>* dbuf = a.dbuf ? a.dbuf + (size_t)p * n + lane : nullptr;
         if (mode != XM_FLUSH) {
-            C2<T> v[6][E];
+            // one component at a time in registers: forward transform, back to
+            // its column in the transform's output order
+#pragma unroll 1
+            for (int c = 0; c < 6; c++) {
+                C2<T> v[E];
 #pragma unroll
-            for (int c = 0; c < 6; c++)
+                for (int q = 0; q < E; q++) v[q] = col[(c * n + lane + 32 * q) * XW_ROW];
+                warp_fft<T, E, -1>(v, wt);
 #pragma unroll
-                for (int q = 0; q < E; q++) v[c][q] = col[(c * n + lane + 32 * q) * XW_ROW];
-#pragma unroll
-            for (int c = 0; c < 6; c++) warp_fft<T, E, -1>(v[c], wt);
-            // lane l holds kx = k2 + E brev5(l) in v[.][k2]; du goes to the lane's
-            // own slots, which its inverse transforms read back in that order
+                for (int q = 0; q < E; q++) col[(c * n + lane + 32 * q) * XW_ROW] = v[q];
+            }
+            // lane l holds kx = k2 + E brev5(l) in slot k2; du goes to the same
+            // slots, which the inverse transforms read back in that order
             const int kb = E * brev5(lane);
-#pragma unroll
+#pragma unroll 1
             for (int k2 = 0; k2 < E; k2++) {
                 C2<T> sb[6], du[9];
 #pragma unroll
-                for (int c = 0; c < 6; c++) sb[c] = v[c][k2];
+                for (int c = 0; c < 6; c++) sb[c] = col[(c * n + lane + 32 * k2) * XW_ROW];
                 green_point<T, SHARED_C0>(gk, g, rn, k2 + kb, ky, kz, sb, du);
                 if (mode == XM_DEFER) {
 #pragma unroll
@@ -255,10 +264,10 @@ __device__ __forceinline__ void x_warp_body(const XArgs<T>& a, const GreenK<T>& 
             }
         } else {
 #pragma unroll
-            for (int c = 6; c < 9; c++)
+            for (int c = 0; c < 3; c++)
 #pragma unroll
                 for (int q = 0; q < E; q++)
-                    col[(c * n + lane + 32 * q) * XW_ROW] = dbuf[(size_t)(c - 6) * npen * n + 32 * q];
+                    col[(c * n + lane + 32 * q) * XW_ROW] = dbuf[(size_t)c * npen * n + 32 * q];
         }
 #pragma unroll 1
         for (int c = clo; c < chi; c++) {
@@ -272,7 +281,7 @@ __device__ __forceinline__ void x_warp_body(const XArgs<T>& a, const GreenK<T>& 
     }
     __syncthreads();
     for (int i = threadIdx.x; i < (chi - clo) * n * XW_PEN; i += blockDim.x) {
-        const int kk = i % XW_PEN, row = clo * n + i / XW_PEN, c = row >> LOGN, x = row & (n - 1);
+        const int kk = i % XW_PEN, row = clo * n + i / XW_PEN, c = coff + (row >> LOGN), x = row & (n - 1);
         if (kk < np) a.spec[(size_t)c * g.Nh + x * xs + p0 + kk] = tile[row * XW_ROW + kk];
     }
 }
@@ -640,8 +649,11 @@ __global__ void __launch_bounds__(SPEC_THREADS) k_x_green(const __grid_constant_
     x_green_body<T, false>(a, a.gk, blockIdx.x, smem);
 }
 
+// Register budget of three CTAs per SM (80 registers, no spills): with the
+// deferring form's six-row tile (56 KB) three CTAs fit an SM, 24 warps instead
+// of 16 (X pass 0.061 -> 0.057 ms at 128^3; four CTAs at 64 registers spill).
 template <typename T, int E>
-__global__ void __launch_bounds__(XW_THREADS) k_x_warp(const __grid_constant__ XArgs<T> a) {
+__global__ void __launch_bounds__(XW_THREADS, 3) k_x_warp(const __grid_constant__ XArgs<T> a) {
     extern __shared__ __align__(16) unsigned char smem[];
     if (!gate_open(a.macro, a.gate)) return;
     x_warp_body<T, E, false>(a, a.gk, blockIdx.x, smem);
@@ -700,7 +712,7 @@ __global__ void __launch_bounds__(SPEC_THREADS) kb_x_green(const XArgs<T>* __res
 }
 
 template <typename T, int E>
-__global__ void __launch_bounds__(XW_THREADS) kb_x_warp(const XArgs<T>* __restrict__ tab,
+__global__ void __launch_bounds__(XW_THREADS, 3) kb_x_warp(const XArgs<T>* __restrict__ tab,
                                                       const int2* __restrict__ map) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ GreenK<T> gks;
@@ -874,6 +886,7 @@ static void fill_spec_t(Ctx& c, SpecSet<T>& s, const int P[3], const FftPlan pl[
     // transform of the sum), and transformed once before the fold at the end
     // of the increment; their uniform part is summed in Macro::dE9_acc
     s.defer = (sizeof(T) == 4 && s.xw && s.epl) ? 1 : 0;
+    if (s.defer) s.sm_xw = xw_smem(g.n0, es, 6);
     double* acc9 = macro_field<double>(c.macro, offsetof(Macro, dE9_acc));
     C2<T>* acc = spec + 9 * (size_t)g.Nh;   // the sum, zeroed by the increment head
     C2<T>* pend = spec + 12 * (size_t)g.Nh; // this iteration's X pass output
