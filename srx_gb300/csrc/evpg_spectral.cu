@@ -881,10 +881,12 @@ static void fill_spec_t(Ctx& c, SpecSet<T>& s, const int P[3], const FftPlan pl[
     s.sm_p = (size_t)(g.n2 + g.n1 + plane_rows(g.n1) * pa.nhp + PLANE_WARPS * plane_rows(g.n2)) * es;
     // FP32 with both warp-register passes: the antisymmetric components
     // (A12, A13, A23) of the correction feed nothing in the loop (the NR reads
-    // the symmetric strain), so they are summed in the spectrum, in the X
-    // pass's lane order (a linear operation: the sum of the transforms is the
-    // transform of the sum), and transformed once before the fold at the end
-    // of the increment; their uniform part is summed in Macro::dE9_acc
+    // the symmetric strain), so the X pass stores them untransformed, in its
+    // lane order, to a pending buffer, the inverse plane pass adds that to
+    // their running sum (a linear operation: the sum of the transforms is the
+    // transform of the sum), and the sum is transformed once before the fold
+    // at the end of the increment; their uniform part is summed in
+    // Macro::dE9_acc. The X pass's tile then holds six components.
     s.defer = (sizeof(T) == 4 && s.xw && s.epl) ? 1 : 0;
     if (s.defer) s.sm_xw = xw_smem(g.n0, es, 6);
     double* acc9 = macro_field<double>(c.macro, offsetof(Macro, dE9_acc));
